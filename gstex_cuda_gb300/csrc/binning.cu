@@ -1,0 +1,292 @@
+// Tile binning: intersection emission, stable LSD radix sort, tile ranges.
+#include "common.cuh"
+
+namespace gstex {
+
+// ---------------------------------------------------------------------------
+// Emission (reference csrc/forward.cu:13-71, helpers.cuh:37-111)
+// ---------------------------------------------------------------------------
+__global__ void emit_kernel(int n, int num_isect, const float2* __restrict__ centers,
+                            const float2* __restrict__ extents, const float* __restrict__ depths,
+                            const int32_t* __restrict__ cum, int tiles_x, int tiles_y, int bw, int wrapped,
+                            int64_t* __restrict__ keys, int32_t* __restrict__ gids) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int lo = i == 0 ? 0 : cum[i - 1];
+    const int hi = min(cum[i], num_isect);
+    int cur = lo;
+    const float2 e = extents[i];
+    if (!((double)e.x <= 1e-4 && (double)e.y <= 1e-4)) {
+        const float2 c = centers[i];
+        const float fbw = (float)bw;
+        const float tcx = __fdiv_rn(c.x, fbw), tcy = __fdiv_rn(c.y, fbw);
+        const float tex = __fdiv_rn(e.x, fbw), tey = __fdiv_rn(e.y, fbw);
+        int x0 = __float2int_rz(__fsub_rn(tcx, tex));
+        int x1 = __float2int_rz(__fadd_rn(__fadd_rn(tcx, tex), 1.0f));
+        int y0 = __float2int_rz(__fsub_rn(tcy, tey));
+        int y1 = __float2int_rz(__fadd_rn(__fadd_rn(tcy, tey), 1.0f));
+        if (wrapped) {
+            if (x0 <= 0) x0 -= 1;
+            if (y0 <= 0) y0 -= 1;
+        } else {
+            x0 = min(max(0, x0), tiles_x);
+            x1 = min(max(0, x1), tiles_x);
+            y0 = min(max(0, y0), tiles_y);
+            y1 = min(max(0, y1), tiles_y);
+        }
+        const int64_t depth_id = (int64_t)__float_as_int(depths[i]);  // sign-extended (forward.cu:47)
+        for (int ty = y0; ty < y1 && cur < hi; ++ty) {
+            for (int tx = x0; tx < x1 && cur < hi; ++tx) {
+                int ti = ty, tj = tx;
+                if (wrapped) {
+                    ti %= tiles_y; if (ti < 0) ti += tiles_y;
+                    tj %= tiles_x; if (tj < 0) tj += tiles_x;
+                }
+                const int64_t tile = (int64_t)(ti * tiles_x + tj);
+                keys[cur] = (int64_t)(((uint64_t)tile << 32) | (uint64_t)depth_id);
+                gids[cur] = i;
+                ++cur;
+            }
+        }
+    }
+    // slots this Gaussian did not write keep the zero value of the reference's
+    // torch::zeros buffers (bindings.cu:99-102)
+    for (; cur < hi; ++cur) {
+        keys[cur] = 0;
+        gids[cur] = 0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Tile ranges (reference csrc/forward.cu:76-98); tiles outside [0, num_tiles)
+// are ignored.
+// ---------------------------------------------------------------------------
+__global__ void bin_edges_kernel(int n, const int64_t* __restrict__ sorted, int num_tiles, int2* __restrict__ bins) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int cur = (int)(sorted[i] >> 32);
+    const bool ok = cur >= 0 && cur < num_tiles;
+    if (i == 0 && ok) bins[cur].x = 0;
+    if (i == n - 1 && ok) bins[cur].y = n;
+    if (i == 0) return;
+    const int prev = (int)(sorted[i - 1] >> 32);
+    if (prev != cur) {
+        if (prev >= 0 && prev < num_tiles) bins[prev].y = i;
+        if (ok) bins[cur].x = i;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Stable LSD radix sort of (u64 key, u32 value), 8-bit digits.
+//
+// Each pass: per-block digit histograms -> one exclusive scan in
+// (digit, block) order -> stable scatter.  Blocks own contiguous chunks; a
+// block ranks each 2048-item tile with warp match + per-warp counters, so the
+// order of equal digits is the input order.
+// ---------------------------------------------------------------------------
+constexpr int kRadix = 256;
+constexpr int kSortThreads = 256;
+constexpr int kSortWarps = kSortThreads / 32;
+constexpr int kSortItems = 8;
+constexpr int kSortTile = kSortThreads * kSortItems;
+constexpr int kSortMaxBlocks = 1216;
+
+struct SortPlan {
+    int blocks, chunk;
+};
+
+static SortPlan sort_plan(int n) {
+    SortPlan p;
+    int tiles = ceil_div(n, kSortTile);
+    int tiles_per_block = ceil_div(tiles, kSortMaxBlocks);
+    p.chunk = tiles_per_block * kSortTile;
+    p.blocks = ceil_div(n, p.chunk);
+    if (p.blocks < 1) p.blocks = 1;
+    return p;
+}
+
+__global__ void __launch_bounds__(kSortThreads) radix_hist_kernel(const uint64_t* __restrict__ keys, int n, int chunk,
+                                                                  int shift, uint32_t* __restrict__ hist) {
+    __shared__ uint32_t h[kRadix];
+    for (int i = threadIdx.x; i < kRadix; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    const int start = blockIdx.x * chunk;
+    const int end = min(start + chunk, n);
+    const unsigned lane = threadIdx.x & 31;
+    for (int base = start; base < end; base += blockDim.x) {
+        const int i = base + threadIdx.x;
+        const bool valid = i < end;
+        const unsigned mask = __ballot_sync(0xffffffffu, valid);
+        if (valid) {
+            const unsigned d = (unsigned)(keys[i] >> shift) & (kRadix - 1);
+            const unsigned peers = __match_any_sync(mask, d);
+            if (lane == (unsigned)(__ffs(peers) - 1)) atomicAdd(&h[d], (uint32_t)__popc(peers));
+        }
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < kRadix; d += blockDim.x) hist[(size_t)d * gridDim.x + blockIdx.x] = h[d];
+}
+
+// Exclusive scan of total = kRadix * blocks counters by one block.
+__global__ void __launch_bounds__(1024) radix_scan_kernel(uint32_t* __restrict__ data, int total) {
+    __shared__ uint32_t partial[1024];
+    const int per = ceil_div(total, (int)blockDim.x);
+    const int s = threadIdx.x * per;
+    const int e = min(s + per, total);
+    uint32_t sum = 0;
+    for (int i = s; i < e; i++) sum += data[i];
+    partial[threadIdx.x] = sum;
+    __syncthreads();
+    for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+        uint32_t y = threadIdx.x >= (unsigned)o ? partial[threadIdx.x - o] : 0u;
+        __syncthreads();
+        partial[threadIdx.x] += y;
+        __syncthreads();
+    }
+    uint32_t run = partial[threadIdx.x] - sum;
+    for (int i = s; i < e; i++) {
+        const uint32_t v = data[i];
+        data[i] = run;
+        run += v;
+    }
+}
+
+__global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
+    const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
+    uint32_t* __restrict__ vout, int n, int chunk, int shift, const uint32_t* __restrict__ offsets) {
+    __shared__ uint32_t run_off[kRadix];
+    __shared__ uint32_t tile_tot[kRadix];
+    __shared__ uint32_t wcnt[kSortWarps][kRadix];
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const unsigned lane = tid & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    for (int d = tid; d < kRadix; d += blockDim.x) run_off[d] = offsets[(size_t)d * gridDim.x + blockIdx.x];
+    const int start = blockIdx.x * chunk;
+    const int end = min(start + chunk, n);
+    for (int tbase = start; tbase < end; tbase += kSortTile) {
+        for (int k = tid; k < kSortWarps * kRadix; k += blockDim.x) (&wcnt[0][0])[k] = 0;
+        __syncthreads();
+        uint64_t key[kSortItems];
+        uint32_t val[kSortItems];
+        uint32_t rank[kSortItems];
+#pragma unroll
+        for (int k = 0; k < kSortItems; k++) {
+            const int i = tbase + warp * (32 * kSortItems) + k * 32 + (int)lane;
+            const bool valid = i < end;
+            const unsigned mask = __ballot_sync(0xffffffffu, valid);
+            uint32_t d = 0, before = 0, peers = 0;
+            if (valid) {
+                key[k] = kin[i];
+                val[k] = vin[i];
+                d = (uint32_t)(key[k] >> shift) & (kRadix - 1);
+                peers = __match_any_sync(mask, d);
+                before = wcnt[warp][d];
+                rank[k] = before + __popc(peers & lt_mask);
+            }
+            __syncwarp();
+            if (valid && lane == (unsigned)(31 - __clz(peers))) wcnt[warp][d] = before + __popc(peers);
+            __syncwarp();
+        }
+        __syncthreads();
+        for (int d = tid; d < kRadix; d += blockDim.x) {
+            uint32_t tot = 0;
+#pragma unroll
+            for (int w = 0; w < kSortWarps; w++) {
+                const uint32_t c = wcnt[w][d];
+                wcnt[w][d] = tot;
+                tot += c;
+            }
+            tile_tot[d] = tot;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kSortItems; k++) {
+            const int i = tbase + warp * (32 * kSortItems) + k * 32 + (int)lane;
+            if (i < end) {
+                const uint32_t d = (uint32_t)(key[k] >> shift) & (kRadix - 1);
+                const uint32_t pos = run_off[d] + wcnt[warp][d] + rank[k];
+                kout[pos] = key[k];
+                vout[pos] = val[k];
+            }
+        }
+        __syncthreads();
+        for (int d = tid; d < kRadix; d += blockDim.x) run_off[d] += tile_tot[d];
+        __syncthreads();
+    }
+}
+
+static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+}  // namespace gstex
+
+using namespace gstex;
+
+extern "C" int gstex_map_gaussian_to_intersects(int n, int num_isect, const float* centers, const float* extents,
+                                                const float* depths, const int32_t* cum, int tiles_x, int tiles_y,
+                                                int bw, int wrapped, int64_t* keys, int32_t* gids,
+                                                gstex_stream_t stream) {
+    GSTEX_REQUIRE(n >= 0 && num_isect >= 0 && tiles_x > 0 && tiles_y > 0 && bw > 0);
+    if (n == 0 || num_isect == 0) return GSTEX_OK;
+    GSTEX_REQUIRE(centers && extents && depths && cum && keys && gids);
+    emit_kernel<<<ceil_div(n, 256), 256, 0, (cudaStream_t)stream>>>(n, num_isect, (const float2*)centers,
+                                                                     (const float2*)extents, depths, cum, tiles_x,
+                                                                     tiles_y, bw, wrapped, keys, gids);
+    return check_launch("map_gaussian_to_intersects");
+}
+
+extern "C" size_t gstex_sort_workspace_bytes(int n) {
+    if (n < 1) n = 1;
+    const SortPlan p = sort_plan(n);
+    return align_up((size_t)n * 8, 256) + align_up((size_t)n * 4, 256) + (size_t)kRadix * p.blocks * 4;
+}
+
+extern "C" int gstex_sort_pairs(int n, int end_bit, const int64_t* keys_in, const int32_t* vals_in,
+                                int64_t* keys_out, int32_t* vals_out, void* ws, size_t ws_bytes, gstex_stream_t s) {
+    GSTEX_REQUIRE(n >= 0 && end_bit >= 0 && end_bit <= 64);
+    if (n == 0) return GSTEX_OK;
+    GSTEX_REQUIRE(keys_in && vals_in && keys_out && vals_out);
+    cudaStream_t stream = (cudaStream_t)s;
+    const int passes = ceil_div(end_bit, 8);
+    if (passes == 0 || n == 1) {
+        cudaError_t e = cudaMemcpyAsync(keys_out, keys_in, (size_t)n * 8, cudaMemcpyDeviceToDevice, stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(vals_out, vals_in, (size_t)n * 4, cudaMemcpyDeviceToDevice, stream);
+        if (e != cudaSuccess) { set_cuda_error(e, "sort_pairs copy"); return GSTEX_ERR_CUDA; }
+        return GSTEX_OK;
+    }
+    GSTEX_REQUIRE(ws);
+    if (ws_bytes < gstex_sort_workspace_bytes(n)) return GSTEX_ERR_CAPACITY;
+    const SortPlan p = sort_plan(n);
+    char* w = (char*)ws;
+    uint64_t* kalt = (uint64_t*)w;
+    w += align_up((size_t)n * 8, 256);
+    uint32_t* valt = (uint32_t*)w;
+    w += align_up((size_t)n * 4, 256);
+    uint32_t* hist = (uint32_t*)w;
+    // Ping-pong so that the last pass lands in the output buffers.
+    const uint64_t* ksrc = (const uint64_t*)keys_in;
+    const uint32_t* vsrc = (const uint32_t*)vals_in;
+    for (int pass = 0; pass < passes; pass++) {
+        const bool to_out = ((passes - 1 - pass) % 2) == 0;
+        uint64_t* kdst = to_out ? (uint64_t*)keys_out : kalt;
+        uint32_t* vdst = to_out ? (uint32_t*)vals_out : valt;
+        const int shift = pass * 8;
+        radix_hist_kernel<<<p.blocks, kSortThreads, 0, stream>>>(ksrc, n, p.chunk, shift, hist);
+        radix_scan_kernel<<<1, 1024, 0, stream>>>(hist, kRadix * p.blocks);
+        radix_scatter_kernel<<<p.blocks, kSortThreads, 0, stream>>>(ksrc, vsrc, kdst, vdst, n, p.chunk, shift, hist);
+        ksrc = kdst;
+        vsrc = vdst;
+    }
+    return check_launch("sort_pairs");
+}
+
+extern "C" int gstex_get_tile_bin_edges(int num_isect, const int64_t* sorted, int num_tiles, int32_t* bins,
+                                        gstex_stream_t s) {
+    GSTEX_REQUIRE(num_isect >= 0 && num_tiles > 0 && bins);
+    cudaStream_t stream = (cudaStream_t)s;
+    cudaError_t e = cudaMemsetAsync(bins, 0, (size_t)num_tiles * 2 * sizeof(int32_t), stream);
+    if (e != cudaSuccess) { set_cuda_error(e, "tile_bin_edges memset"); return GSTEX_ERR_CUDA; }
+    if (num_isect == 0) return GSTEX_OK;
+    GSTEX_REQUIRE(sorted);
+    bin_edges_kernel<<<ceil_div(num_isect, 256), 256, 0, stream>>>(num_isect, sorted, num_tiles, (int2*)bins);
+    return check_launch("get_tile_bin_edges");
+}

@@ -1,0 +1,202 @@
+/*
+ * gstex_gb300 - C ABI of the GB300-native textured 2D-Gaussian rasteriser.
+ *
+ * Each entry point replaces one native op of the reference's Python
+ * extension (gstex_cuda.csrc, bound in gstex_cuda/cuda/csrc/ext.cpp:8-25 and
+ * looked up lazily in gstex_cuda/cuda/__init__.py:4-27; paths relative to
+ * the reference project).  The conventions differ from the reference in the
+ * ways a C ABI needs:
+ *   - every array is a raw device pointer to contiguous memory, allocated by
+ *     the caller (outputs included); the library allocates nothing;
+ *   - every call takes the CUDA stream to launch on and is asynchronous;
+ *   - every call returns a status code (GSTEX_OK = 0) after validating its
+ *     arguments on the host and checking the launch with cudaGetLastError.
+ * Matrices are row-major float[16]; quaternions are (w, x, y, z).
+ */
+#ifndef GSTEX_GB300_H
+#define GSTEX_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* gstex_stream_t; /* same type as cudaStream_t */
+
+enum gstex_status {
+    GSTEX_OK = 0,
+    GSTEX_ERR_INVALID_ARGUMENT = 1, /* null pointer, bad size or shape */
+    GSTEX_ERR_CAPACITY = 2,         /* a caller-provided buffer is too small */
+    GSTEX_ERR_UNSUPPORTED = 3,      /* e.g. more than 64 texture channels */
+    GSTEX_ERR_CUDA = 4              /* a CUDA launch or runtime call failed */
+};
+
+/* Text for a status code (static storage). */
+const char* gstex_status_string(int status);
+/* Text of the last CUDA error seen by this library on this thread. */
+const char* gstex_last_cuda_error(void);
+/* Library version, e.g. "0.1.0". */
+const char* gstex_version(void);
+
+/* ---------------------------------------------------------------------
+ * Projection
+ * ------------------------------------------------------------------- */
+
+/* Screen-space AABB of each 2D Gaussian's +-3 sigma rectangle.
+ * Replaces _C.get_aabb_2d (csrc/get_aabb_2d.cu:91-126).
+ * means/scales [n,3], quats [n,4] -> centers/extents [n,2]. */
+int gstex_get_aabb_2d(int n, const float* means, const float* scales, float glob_scale, const float* quats,
+                      const float* viewmat, float fx, float fy, float cx, float cy, float* centers,
+                      float* extents, gstex_stream_t stream);
+
+/* Per-Gaussian number of tiles hit, bit-exact with the reference's torch
+ * tile counter.  Replaces get_num_tiles_hit_2d (gstex_cuda/get_aabb_2d.py:70-91). */
+int gstex_num_tiles_hit(int n, const float* centers, const float* extents, int img_height, int img_width,
+                        int block_width, int32_t* num_tiles_hit, gstex_stream_t stream);
+
+/* Inclusive int32 prefix sum of n counts (the reference's torch.cumsum in
+ * compute_cumulative_intersects, gstex_cuda/utils.py:40-59).  total (device,
+ * int64) receives the last value.  workspace: gstex_scan_workspace_bytes(n). */
+size_t gstex_scan_workspace_bytes(int n);
+int gstex_inclusive_scan_i32(int n, const int32_t* counts, int32_t* cum, int64_t* total, void* workspace,
+                             size_t workspace_bytes, gstex_stream_t stream);
+
+/* Spherical harmonics colours from coefficients [n, bases(degree), 3] using
+ * the first bases(degrees_to_use) bases.  Replaces _C.compute_sh_forward
+ * (csrc/bindings.cu:18-43). */
+int gstex_compute_sh_forward(int n, int degree, int degrees_to_use, const float* viewdirs, const float* coeffs,
+                             float* colors, gstex_stream_t stream);
+/* v_coeffs [n, bases(degree), 3] (fully written). Replaces
+ * _C.compute_sh_backward (csrc/bindings.cu:45-75). */
+int gstex_compute_sh_backward(int n, int degree, int degrees_to_use, const float* viewdirs,
+                              const float* v_colors, float* v_coeffs, gstex_stream_t stream);
+
+/* ---------------------------------------------------------------------
+ * Tile binning
+ * ------------------------------------------------------------------- */
+
+/* Emits one (tile << 32 | depth-bits) key and Gaussian id per tile hit into
+ * the slots [cum[i-1], cum[i]) of each Gaussian.  Slots a Gaussian does not
+ * write (tiny extents) are set to zero, as in the reference.  Replaces
+ * _C.map_gaussian_to_intersects (csrc/bindings.cu:77-121, forward.cu:13-71). */
+int gstex_map_gaussian_to_intersects(int n, int num_intersects, const float* centers, const float* extents,
+                                     const float* depths, const int32_t* cum_tiles_hit, int tiles_x, int tiles_y,
+                                     int block_width, int wrapped, int64_t* isect_ids, int32_t* gaussian_ids,
+                                     gstex_stream_t stream);
+
+/* Stable ascending LSD radix sort of (int64 key, int32 value) pairs on key
+ * bits [0, end_bit).  Replaces torch.sort + torch.gather in
+ * bin_and_sort_gaussians (gstex_cuda/utils.py:159-160).  The caller passes
+ * end_bit = 32 + bit_length(num_tiles), which orders every key with a
+ * non-negative depth exactly as a signed 64-bit sort does. */
+size_t gstex_sort_workspace_bytes(int n);
+int gstex_sort_pairs(int n, int end_bit, const int64_t* keys_in, const int32_t* vals_in, int64_t* keys_out,
+                     int32_t* vals_out, void* workspace, size_t workspace_bytes, gstex_stream_t stream);
+
+/* Per-tile [start, end) ranges of a sorted key list (zero for empty tiles).
+ * Replaces _C.get_tile_bin_edges (csrc/bindings.cu:123-140, forward.cu:76-98). */
+int gstex_get_tile_bin_edges(int num_intersects, const int64_t* isect_ids_sorted, int num_tiles,
+                             int32_t* tile_bins, gstex_stream_t stream);
+
+/* ---------------------------------------------------------------------
+ * Textured compositor (texture_forward / texture_backward)
+ * ------------------------------------------------------------------- */
+
+/* Inputs shared by forward and backward (csrc/texture.cuh:92-167). */
+typedef struct gstex_raster_inputs {
+    int num_points;       /* N */
+    int img_width, img_height, block_width;
+    int channels;         /* texture channels C (texture_info[2]), 0..64 */
+    int num_texels;       /* T = rows of texture */
+    int texture_dtype;    /* 0: float32 [T,C]; 1: bfloat16 [T,4] (C == 3 only) */
+    const int32_t* texture_dims;        /* [N,3] (h, w, start) */
+    const int32_t* gaussian_ids_sorted; /* [num_intersects] */
+    const int32_t* tile_bins;           /* [tiles, 2] */
+    const float* colors;                /* [N,3] */
+    const float* opacities;             /* [N] */
+    const float* means;                 /* [N,3] */
+    const float* scales;                /* [N,3] */
+    float glob_scale;
+    const float* quats;                 /* [N,4] */
+    const float* uv0;                   /* [N,2] */
+    const float* umap;                  /* [N,3] */
+    const float* vmap;                  /* [N,3] */
+    const void* texture;                /* see texture_dtype */
+    const float* viewmat;               /* [16] device */
+    float fx, fy, cx, cy;
+    int settings;                       /* reference settings bitfield */
+    const float* background;            /* [3] device */
+} gstex_raster_inputs;
+
+typedef struct gstex_forward_outputs {
+    float* img;        /* [H,W,3] */
+    float* depth;      /* [H,W] */
+    float* reg;        /* [H,W] */
+    float* texture;    /* [H,W,C] */
+    float* normal;     /* [H,W,3] */
+    float* final_T;    /* [H,W] */
+    int32_t* final_idx; /* [H,W] */
+    int32_t* depth_idx; /* [H,W] */
+    float* reg_s;      /* [H,W,3] */
+} gstex_forward_outputs;
+
+/* Replaces _C.texture_forward (csrc/texture.cu:766-901). */
+int gstex_texture_forward(const gstex_raster_inputs* in, const gstex_forward_outputs* out, gstex_stream_t stream);
+
+typedef struct gstex_backward_io {
+    /* saved forward state */
+    const float* final_T;
+    const int32_t* final_idx;
+    const int32_t* depth_idx;
+    const float* reg_s;
+    /* upstream gradients */
+    const float* v_img;     /* [H,W,3] */
+    const float* v_depth;   /* [H,W] */
+    const float* v_reg;     /* [H,W] */
+    const float* v_alpha;   /* [H,W] */
+    const float* v_texture; /* [H,W,C] */
+    const float* v_normal;  /* [H,W,3] */
+    /* outputs (fully written; v_tex_grad is accumulated into and must be
+     * zeroed by the caller) */
+    float* v_colors;  /* [N,3] */
+    float* v_opacity; /* [N] */
+    float* v_means;   /* [N,3] */
+    float* v_scales;  /* [N,3] */
+    float* v_quats;   /* [N,4] */
+    float* v_uv0;     /* [N,2] */
+    float* v_umap;    /* [N,3] */
+    float* v_vmap;    /* [N,3] */
+    float* v_tex_grad; /* [T,C] float32 (or [T,4] when texture_dtype == 1) */
+    /* caller-provided scratch of gstex_backward_workspace_bytes(N) bytes */
+    void* workspace;
+    size_t workspace_bytes;
+} gstex_backward_io;
+
+size_t gstex_backward_workspace_bytes(int num_points);
+
+/* Replaces _C.texture_backward (csrc/texture.cu:915-1053). */
+int gstex_texture_backward(const gstex_raster_inputs* in, const gstex_backward_io* io, gstex_stream_t stream);
+
+/* ---------------------------------------------------------------------
+ * texture_sample
+ * ------------------------------------------------------------------- */
+
+/* Bilinear lookup of nq queries in jagged charts, uv clamped to [0,1].
+ * Replaces _C.texture_sample_forward (csrc/texture_sample.cu:72-105). */
+int gstex_texture_sample_forward(int nq, int channels, const int32_t* texture_dims, const float* uvs,
+                                 const float* texture, float* out, gstex_stream_t stream);
+/* Texel gradients (accumulated into v_texture, zeroed by the caller) and uv
+ * gradients (written).  Replaces _C.texture_sample_backward
+ * (csrc/texture_sample.cu:107-141), which read its upstream gradient from the
+ * wrong buffer and was never called. v_uvs may be null. */
+int gstex_texture_sample_backward(int nq, int channels, const int32_t* texture_dims, const float* uvs,
+                                  const float* texture, const float* v_out, float* v_texture, float* v_uvs,
+                                  gstex_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GSTEX_GB300_H */

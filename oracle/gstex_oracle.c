@@ -811,8 +811,10 @@ static void tile_bbox(float cx, float cy, float ex, float ey, int tiles_x, int t
 
 /* csrc/forward.cu:13-71.  Slots come from the caller's inclusive cumsum; a
  * Gaussian that is skipped (both extents <= 1e-4) leaves its slots at the
- * zero-initialised value, as the reference's torch::zeros buffers do.  Writes
- * past n_isect are dropped (the reference would write out of bounds). */
+ * zero-initialised value, as the reference's torch::zeros buffers do.  Each
+ * Gaussian writes only inside its own slots [cum[i-1], cum[i]): with a
+ * power-of-two tile width the emitted count always equals the slot count;
+ * otherwise the reference would race into its neighbour's slots. */
 void or_map_gaussian_to_intersects(int n, const float* centers, const float* extents, const float* depths,
                                    const int32_t* cum, int tiles_x, int tiles_y, int bw, int wrapped,
                                    long n_isect, int64_t* isect_ids, int32_t* gids) {
@@ -824,6 +826,7 @@ void or_map_gaussian_to_intersects(int n, const float* centers, const float* ext
         int x0, y0, x1, y1;
         tile_bbox(centers[2 * i], centers[2 * i + 1], ex, ey, tiles_x, tiles_y, bw, wrapped, &x0, &y0, &x1, &y1);
         long cur = i == 0 ? 0 : cum[i - 1];
+        long hi = cum[i] < n_isect ? cum[i] : n_isect;
         int32_t dbits;
         memcpy(&dbits, depths + i, 4);
         int64_t depth_id = (int64_t)dbits;  /* sign-extends, forward.cu:47 */
@@ -835,7 +838,7 @@ void or_map_gaussian_to_intersects(int n, const float* centers, const float* ext
                     tj = tj % tiles_x; if (tj < 0) tj += tiles_x;
                 }
                 int64_t tile_id = (int64_t)(ti * tiles_x + tj);
-                if (cur >= 0 && cur < n_isect) {
+                if (cur >= 0 && cur < hi) {
                     isect_ids[cur] = (int64_t)(((uint64_t)tile_id << 32) | (uint64_t)depth_id);
                     gids[cur] = i;
                 }

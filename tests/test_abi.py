@@ -1,0 +1,70 @@
+"""The C-ABI library builds, loads and exports every symbol its header declares
+(no GPU needed: nothing is launched)."""
+import os
+import re
+
+import pytest
+
+from gstex_cuda_gb300 import _lib, build
+
+HEADER_DIR = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+
+
+def declared_functions():
+    names = []
+    for f in sorted(os.listdir(HEADER_DIR)):
+        if f.endswith(".h"):
+            src = open(os.path.join(HEADER_DIR, f)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names += re.findall(r"\b(gstex_\w+)\s*\(", src)
+    return sorted(set(names))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    assert "gstex_texture_forward" in names and "gstex_texture_backward" in names
+    assert len(names) >= 15
+
+
+def test_library_exports_every_declared_symbol():
+    L = _lib.lib()
+    missing = [n for n in declared_functions() if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_status_strings_and_workspace_queries():
+    L = _lib.lib()
+    assert L.gstex_status_string(0) == b"ok"
+    assert L.gstex_status_string(2) == b"buffer too small"
+    assert L.gstex_version().decode().count(".") == 2
+    assert L.gstex_sort_workspace_bytes(1000) >= 1000 * 12
+    assert L.gstex_backward_workspace_bytes(10) >= 10 * 26 * 4
+    assert L.gstex_scan_workspace_bytes(1) > 0
+
+
+def test_invalid_arguments_rejected_without_gpu():
+    """Host-side validation runs before any launch."""
+    L = _lib.lib()
+    assert L.gstex_get_aabb_2d(-1, None, None, 1.0, None, None, 1.0, 1.0, 0.0, 0.0, None, None, None) == 1
+    assert L.gstex_sort_pairs(10, 70, None, None, None, None, None, 0, None) == 1
+    ri = _lib.RasterInputs()
+    ri.num_points, ri.img_width, ri.img_height, ri.block_width, ri.channels = 1, 8, 8, 16, 65
+    import ctypes
+    fo = _lib.ForwardOutputs()
+    # block width 16 is fine, 65 channels is not
+    ri.tile_bins = ri.viewmat = ri.background = 1
+    assert L.gstex_texture_forward(ctypes.byref(ri), ctypes.byref(fo), None) == 3
+    ri.channels, ri.block_width = 3, 17
+    assert L.gstex_texture_forward(ctypes.byref(ri), ctypes.byref(fo), None) == 1
+
+
+def test_cpu_tensors_fail_loudly():
+    torch = pytest.importorskip("torch")
+    import gstex_cuda_gb300 as G
+    with pytest.raises(RuntimeError):
+        G.cuda.compute_sh_forward(1, 0, 0, torch.zeros(1, 3), torch.zeros(1, 1, 3))
+
+
+def test_build_is_incremental():
+    assert os.path.exists(build.build())
+    assert not build._stale()
