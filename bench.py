@@ -1,0 +1,384 @@
+#!/usr/bin/env python
+"""Forward + backward frames/s of the batched textured 2D-Gaussian workload.
+
+Workload (one "step"): 32 cameras on a radius-8 sphere with resolutions drawn
+from {512^2, 800^2, 1280x720, 1920x1080}, one scene of 500k Gaussians
+(means U[-3,3]^3, scales log-U[0.005,0.05]), 16M texels stored as bfloat16,
+SH degree 3 coefficients stored as bfloat16, blending and gradients in fp32;
+forward, the demo's image losses, backward and the SH adjoint over all views.
+Inputs are seeded synthetic tensors of these shapes.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+``--impl reference`` times the CPU restatement of the reference algorithm
+(oracle/, OpenMP on all host cores) on a bounded sample of the same workload.
+Multi-GPU (torchrun) runs independent replicas, one batch of views per rank
+(weak scaling); rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "fwd+bwd frames/s, 1080p 500k splats/16M texels: batched bf16 vs plain fp32, same tol"
+WORKLOAD = ("32 cameras (512^2/800^2/1280x720/1920x1080, r=8 sphere), 500k Gaussians, 16M bf16 texels, "
+            "SH deg 3 (bf16), fwd + image losses + bwd + SH adjoint")
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--views", type=int, default=32)
+    p.add_argument("--points", type=int, default=500_000)
+    p.add_argument("--texels", type=int, default=16_000_000)
+    p.add_argument("--no-plain", action="store_true", help="skip the plain per-view fp32 comparison")
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--cpu-seconds", type=float, default=15.0)
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------------------
+def build_workload(args, seed=3):
+    from gstex_cuda_gb300 import synthetic
+    return synthetic.batched(seed=seed, n=args.points, texels=args.texels, views=args.views)
+
+
+def device_scene(spec, dev, bf16=True):
+    import torch
+    from gstex_cuda_gb300 import batch as B
+    if bf16:
+        tex = torch.zeros(spec.texture.shape[0], 4, dtype=torch.bfloat16)
+        tex[:, :3] = spec.texture.to(torch.bfloat16)
+        sh = spec.sh_coeffs.to(torch.bfloat16)
+    else:
+        tex = spec.texture.float()
+        sh = spec.sh_coeffs.float()
+    t = lambda x: x.contiguous().to(dev)
+    return B.Scene(means=t(spec.means), scales=t(spec.scales), quats=t(spec.quats), opacity=t(spec.opacity),
+                   sh_coeffs=t(sh), sh_degree=spec.sh_degree, uv0=t(spec.uv0), umap=t(spec.umap), vmap=t(spec.vmap),
+                   texture_dims=t(spec.texture_dims), texture=t(tex))
+
+
+def cameras_of(spec):
+    from gstex_cuda_gb300 import batch as B
+    return [B.Camera(c.viewmat, c.fx, c.fy, c.cx, c.cy, c.width, c.height) for c in spec.cameras]
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = sorted(float(r[1]) for r in rows if r[1].replace(".", "").isdigit())
+        mx = max(float(r[2]) for r in rows if r[2].replace(".", "").isdigit())
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def measured_peak_hbm():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def algorithmic_bytes(I, tiles, T, P, C, N, tex_bytes_per_texel, grad_texel_bytes, backward):
+    """Compulsory bytes of one compositor launch: per intersection a 4-byte id
+    and the 96-byte fp32 Gaussian record; per tile its range; every texel once;
+    per pixel its outputs (forward) or saved state + upstream gradients
+    (backward, plus the read-modify-write of 22 per-Gaussian gradient floats
+    and of the texel gradients)."""
+    rec = 96
+    if not backward:
+        return I * (4 + rec) + tiles * 8 + T * tex_bytes_per_texel + P * (12 + 4 + 4 + 4 * C + 12 + 4 + 4 + 4 + 12)
+    return (I * (4 + rec) + tiles * 8 + T * tex_bytes_per_texel + P * (24 + 12 + 4 + 4 + 4 + 4 * C + 12)
+            + 2 * N * 88 + 2 * T * grad_texel_bytes)
+
+
+# ---------------------------------------------------------------------------
+def cpu_sample(spec, seconds, prec="f32", loss_weights=None):
+    """Oracle fwd + bwd of whole views (round robin) until `seconds` elapse."""
+    import numpy as np
+    import oracle
+    from gstex_cuda_gb300.batch import LOSS_WEIGHTS
+    lw = dict(LOSS_WEIGHTS if loss_weights is None else loss_weights)
+    tex = spec.texture.to(__import__("torch").bfloat16).float().numpy()
+    cores = os.cpu_count() or 1
+    rng = np.random.default_rng(0)
+    done, t0 = 0, time.perf_counter()
+    views = []
+    while True:
+        cam = spec.cameras[done % len(spec.cameras)]
+        dirs = (spec.means - cam.position[None]).numpy()
+        col = oracle.sh_forward(spec.sh_degree, spec.sh_degree, dirs, spec.sh_coeffs.numpy(), prec=prec)
+        sc = oracle.Scene(means=spec.means.numpy(), scales=spec.scales.numpy(), quats=spec.quats.numpy(),
+                          opacity=spec.opacity.numpy(), colors=col, uv0=spec.uv0.numpy(), umap=spec.umap.numpy(),
+                          vmap=spec.vmap.numpy(), texture_dims=spec.texture_dims.numpy(), texture=tex)
+        oc = oracle.Camera(cam.viewmat.numpy(), cam.c2w.numpy(), cam.fx, cam.fy, cam.cx, cam.cy, cam.height,
+                           cam.width)
+        depths = oracle.camera_depths(spec.means.numpy(), cam.viewmat.numpy())
+        b, f = oracle.render(sc, oc, depths=depths, block_width=16, settings=spec.settings,
+                             background=np.zeros(3), prec=prec, nthreads=cores)
+        H, W = cam.height, cam.width
+        P = H * W
+        tgt = rng.random((H, W, 3))
+        v_img = lw["img"] * 2 * (f["img"] - tgt) / (3 * P)
+        v_tex = lw["texture"] * 2 * (f["texture"] - tgt) / (3 * P)
+        v_reg = np.full((H, W), lw["reg"] / P)
+        n = f["normal"]
+        v_n = lw["normal"] * 2 * np.stack([n[..., 0], n[..., 1], n[..., 2] - 1], -1) / P
+        z = np.zeros((H, W))
+        g = oracle.texture_backward(sc, oc, b["gaussian_ids_sorted"], b["tile_bins"], 16, spec.settings,
+                                    np.zeros(3), f, v_img, z, v_reg, z, v_tex, v_n, prec=prec, nthreads=cores)
+        oracle.sh_backward(spec.sh_degree, spec.sh_degree, dirs, g["colors"], prec=prec)
+        done += 1
+        views.append(f"{W}x{H}")
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+    return done / el, cores, done, el, views
+
+
+def run_reference(args):
+    """CPU restatement of the reference (the oracle), each step one view of the workload."""
+    import oracle
+    oracle.build()
+    spec = build_workload(args)
+    steps, warm = max(1, args.steps), max(0, args.warmup)
+    # warm-up: a bounded number of views, then the timed views
+    per_step_seconds = 0.0
+    if warm:
+        cpu_sample(spec, 0.0)
+    t0 = time.perf_counter()
+    n_views = 0
+    for _ in range(steps):
+        fps, cores, n, el, views = cpu_sample(spec, 0.0)
+        n_views += n
+    el = time.perf_counter() - t0
+    value = n_views / el
+    line = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": args.gpus, "steps": steps,
+            "warmup": warm, "ms_per_step": 1000 * el / steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "sample": f"{steps} views fwd+bwd (round robin over the 32 cameras)"},
+            "cpu_baseline": {"value": value, "unit": "frames/s", "cores": os.cpu_count() or 1, "kind": "port",
+                             "sample": f"{steps} of the 32 views, full fwd+bwd each (CPU oracle, OpenMP)"},
+            "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args)
+        return
+    import torch
+    import torch.distributed as dist
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=dev)
+    from gstex_cuda_gb300 import batch as B
+    from gstex_cuda_gb300 import _lib
+
+    spec = build_workload(args, seed=3 + rank)
+    cams = cameras_of(spec)
+    scene = device_scene(spec, dev, bf16=True)
+    r = B.BatchRenderer(cams, spec.num_points, channels=3, texture_dtype=torch.bfloat16, device=dev)
+    P = r.total_pixels
+    gen = torch.Generator().manual_seed(11 + rank)
+    tgt_img = torch.rand(P, 3, generator=gen).to(dev)
+    tgt_tex = torch.rand(P, 3, generator=gen).to(dev)
+    # first step: size the intersection buffers
+    r.step(scene, tgt_img, tgt_tex)
+    torch.cuda.synchronize(dev)
+    while not r.check_capacity():
+        r.grow(1.25)
+        r.step(scene, tgt_img, tgt_tex)
+        torch.cuda.synchronize(dev)
+    I = r.intersections()
+
+    # timed region: eager steps (one launch per stage), CUDA events around the
+    # compositor kernels on the launching stream
+    stream = torch.cuda.current_stream(dev)
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    for _ in range(args.warmup):
+        r.step(scene, tgt_img, tgt_tex)
+    pairs = []
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    clocks = ClockSampler(local)
+    clocks.start()
+    n0 = _lib.lib().gstex_launch_count()
+    e_start, e_end = ev(), ev()
+    e_start.record(stream)
+    for _ in range(args.steps):
+        r.bin(scene)
+        f0, f1, b0, b1 = ev(), ev(), ev(), ev()
+        f0.record(stream)
+        r.forward(scene)
+        f1.record(stream)
+        r.image_loss(tgt_img, tgt_tex)
+        b0.record(stream)
+        r.backward(scene)
+        b1.record(stream)
+        pairs.append((f0, f1, b0, b1))
+    e_end.record(stream)
+    torch.cuda.synchronize(dev)
+    launches = _lib.lib().gstex_launch_count() - n0
+    clk = clocks.stop()
+    elapsed = e_start.elapsed_time(e_end) / 1000.0
+    if world > 1:
+        t = torch.tensor([elapsed], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    fwd_ms = sum(a.elapsed_time(b) for a, b, _, _ in pairs) / len(pairs)
+    bwd_ms = sum(c.elapsed_time(d) for _, _, c, d in pairs) / len(pairs)
+    value = world * args.views * args.steps / elapsed
+
+    # graph replay of the same step (launch overhead removed)
+    graph_fps = None
+    try:
+        r.capture(scene, tgt_img, tgt_tex)
+        for _ in range(2):
+            r.replay()
+        torch.cuda.synchronize(dev)
+        g0, g1 = ev(), ev()
+        g0.record(stream)
+        for _ in range(args.steps):
+            r.replay()
+        g1.record(stream)
+        torch.cuda.synchronize(dev)
+        graph_fps = args.views * args.steps / (g0.elapsed_time(g1) / 1000.0)
+    except Exception as ex:  # graph capture is an optimisation; report why it was skipped
+        graph_fps = f"unavailable: {type(ex).__name__}: {ex}"
+
+    # end to end through the public API with host inputs: pinned host copies of
+    # every scene input are uploaded each step, the loss is read back
+    e2e = None
+    if not args.no_e2e:
+        host = {k: getattr(scene, k).cpu().pin_memory() for k in
+                ("means", "scales", "quats", "opacity", "sh_coeffs", "uv0", "umap", "vmap", "texture_dims", "texture")}
+        h2d = sum(t.numel() * t.element_size() for t in host.values())
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            for k, t in host.items():
+                getattr(scene, k).copy_(t, non_blocking=True)
+            loss = r.step(scene, tgt_img, tgt_tex)
+            float(loss.item())
+        torch.cuda.synchronize(dev)
+        el = time.perf_counter() - t0
+        e2e = {"value": world * args.views * args.steps / el, "unit": "frames/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": 4}
+
+    # plain per-view fp32 path (drop-in API, one view after another, host sync per view)
+    plain = None
+    if not args.no_plain:
+        scene32 = device_scene(spec, dev, bf16=False)
+        ks = max(1, args.steps // 5)
+        B.plain_step(scene32, cams, tgt_img, tgt_tex, r.pix_offsets_host)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(ks):
+            B.plain_step(scene32, cams, tgt_img, tgt_tex, r.pix_offsets_host)
+        torch.cuda.synchronize(dev)
+        plain = args.views * ks / (time.perf_counter() - t0)
+        del scene32
+
+    # roofline of the dominant compositor kernel
+    T = spec.num_texels
+    N = spec.num_points
+    tiles = r.total_tiles
+    fb = algorithmic_bytes(I, tiles, T, P, 3, N, 8, 16, backward=False)
+    bb = algorithmic_bytes(I, tiles, T, P, 3, N, 8, 16, backward=True)
+    peak, peak_kind = measured_peak_hbm()
+    dom = ("backward", bb, bwd_ms) if bwd_ms >= fwd_ms else ("forward", fb, fwd_ms)
+    achieved = dom[1] / (dom[2] / 1000.0) / 1e9
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        import oracle
+        oracle.build()
+        fps, cores, n, el, views = cpu_sample(spec, args.cpu_seconds)
+        cpu = {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port",
+               "sample": f"{n} of the 32 views ({', '.join(views)}), full fwd+bwd each, {el:.1f} s (CPU oracle)"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1000 * elapsed / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": WORKLOAD, "views": args.views, "num_points": N, "texels": T,
+                           "storage": "bf16 texels [T,4] + bf16 SH; fp32 blending and gradients",
+                           "intersections": I, "pixels": P, "tiles": tiles, "parallelism": f"replicas x{world}",
+                           "l2": "working set > L2 (no flush)", "timed": "eager, one launch per stage"},
+                "e2e": e2e, "gpu_launches": int(launches),
+                "roofline": {"bound": "hbm", "kernel": dom[0], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                             "algorithmic_bytes_per_launch": dom[1], "kernel_ms": dom[2]},
+                "kernels_ms": {"forward": fwd_ms, "backward": bwd_ms},
+                "graph_frames_per_s": graph_fps,
+                "plain_fp32_frames_per_s": plain,
+                "speedup_vs_plain_fp32": (value / plain) if plain else None,
+                "cpu_baseline": cpu, "clocks": clk}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -48,6 +48,7 @@ _SIGS = {
     "gstex_status_string": (ctypes.c_char_p, [_I]),
     "gstex_last_cuda_error": (ctypes.c_char_p, []),
     "gstex_version": (ctypes.c_char_p, []),
+    "gstex_launch_count": (ctypes.c_ulonglong, []),
     "gstex_get_aabb_2d": (_I, [_I, _P, _P, _F, _P, _P, _F, _F, _F, _F, _P, _P, _P]),
     "gstex_num_tiles_hit": (_I, [_I, _P, _P, _I, _I, _I, _P, _P]),
     "gstex_scan_workspace_bytes": (ctypes.c_size_t, [_I]),

@@ -1,0 +1,398 @@
+"""Batched multi-view rendering on the GB300 library.
+
+The reference renders one camera per ``texture_gaussians`` call and reads the
+intersection count back to the host every time (gstex_cuda/utils.py:57-58).
+``BatchRenderer`` renders a fixed set of cameras of one scene with one launch
+per stage, keeps every size on the device (intersection buffers are sized by
+capacity, an overflow flag reports a too-small capacity), and can capture a
+whole forward + backward step in a CUDA graph.
+
+Stages of ``step``: projection of all (view, Gaussian) pairs with SH colours
+-> inclusive scan of tile counts -> emission of (global tile | depth) keys ->
+stable radix sort -> tile ranges -> persistent forward over a global tile
+queue -> image losses and their gradients -> persistent backward -> SH
+adjoint over views.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+from typing import List, Optional, Sequence
+
+import torch
+
+from . import _lib
+from ._lib import check, ptr
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_F = ctypes.c_float
+_LL = ctypes.c_longlong
+
+
+class ViewDesc(ctypes.Structure):
+    _fields_ = [("viewmat", _F * 16), ("fx", _F), ("fy", _F), ("cx", _F), ("cy", _F), ("width", _I),
+                ("height", _I)]
+
+
+class BatchInputs(ctypes.Structure):
+    _fields_ = [("num_points", _I), ("num_views", _I), ("block_width", _I), ("channels", _I), ("num_texels", _I),
+                ("texture_dtype", _I), ("settings", _I), ("total_tiles", _I),
+                ("views", _P), ("tile_view", _P), ("tile_order", _P), ("gaussian_ids_sorted", _P), ("tile_bins", _P),
+                ("colors", _P), ("opacities", _P), ("means", _P), ("scales", _P), ("glob_scale", _F), ("quats", _P),
+                ("uv0", _P), ("umap", _P), ("vmap", _P), ("texture_dims", _P), ("texture", _P), ("background", _P),
+                ("queue", _P), ("grid", _I)]
+
+
+_BATCH_SIGS = {
+    "gstex_batch_layout": (_I, [_I, ctypes.POINTER(ViewDesc), _I, ctypes.POINTER(_I), ctypes.POINTER(_LL)]),
+    "gstex_batch_views_bytes": (ctypes.c_size_t, [_I]),
+    "gstex_batch_prepare": (_I, [_I, ctypes.POINTER(ViewDesc), _I, _P, _P, _P, _P]),
+    "gstex_batch_project": (_I, [_I, _I, _P, _P, _P, _F, _P, _P, _I, _I, _I, _P, _P, _P]),
+    "gstex_batch_emit": (_I, [_I, _I, _P, _P, _P, _F, _P, _I, _P, _P, _LL, _P, _P, _P, _P, _P]),
+    "gstex_sort_pairs_dyn": (_I, [_I, _P, _I, _P, _P, _P, _P, _P, ctypes.c_size_t, _P]),
+    "gstex_get_tile_bin_edges_dyn": (_I, [_I, _P, _P, _I, _P, _P]),
+    "gstex_batch_forward": (_I, [ctypes.POINTER(BatchInputs), ctypes.POINTER(_lib.ForwardOutputs), _P]),
+    "gstex_batch_backward_workspace_bytes": (ctypes.c_size_t, [_I]),
+    "gstex_batch_backward": (_I, [ctypes.POINTER(BatchInputs), ctypes.POINTER(_lib.BackwardIO), _P]),
+    "gstex_batch_sh_backward": (_I, [_I, _I, _P, _P, _I, _P, _P, _P]),
+    "gstex_batch_image_loss": (_I, [_LL, _I, _P, _I, _P, _P, _P, _P, _P, _P, _F, _F, _F, _F, _P, _P, _P, _P, _P,
+                                    _P]),
+}
+
+
+def _L():
+    L = _lib.lib()
+    if not getattr(L, "_batch_sigs", False):
+        for name, (res, args) in _BATCH_SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        L._batch_sigs = True
+    return L
+
+
+@dataclass
+class Camera:
+    viewmat: torch.Tensor  # [4,4] world->camera
+    fx: float
+    fy: float
+    cx: float
+    cy: float
+    width: int
+    height: int
+
+
+@dataclass
+class Scene:
+    """Device tensors of one scene.  ``texture`` is float32 [T, C] or bfloat16
+    [T, 4] (3 channels padded); ``sh_coeffs`` is float32 or bfloat16 [N, B, 3]."""
+    means: torch.Tensor
+    scales: torch.Tensor
+    quats: torch.Tensor
+    opacity: torch.Tensor
+    sh_coeffs: torch.Tensor
+    sh_degree: int
+    uv0: torch.Tensor
+    umap: torch.Tensor
+    vmap: torch.Tensor
+    texture_dims: torch.Tensor
+    texture: torch.Tensor
+    channels: int = 3
+    glob_scale: float = 1.0
+
+
+LOSS_WEIGHTS = dict(img=1.0, texture=1.0, reg=100.0, normal=0.05)
+
+
+class BatchRenderer:
+    """Fixed cameras, fixed scene size; reusable buffers for repeated steps."""
+
+    def __init__(self, cameras: Sequence[Camera], num_points: int, *, channels: int = 3, texture_dtype=torch.float32,
+                 block_width: int = 16, settings: int = 1 << 8, background=(0.0, 0.0, 0.0), capacity: int = 0,
+                 device="cuda:0", grid: int = 0, loss_weights: Optional[dict] = None):
+        self.dev = torch.device(device)
+        self.N = int(num_points)
+        self.V = len(cameras)
+        self.bw = int(block_width)
+        self.C = int(channels)
+        self.settings = int(settings)
+        self.texmode = 1 if texture_dtype == torch.bfloat16 else 0
+        self.grid = int(grid)
+        self.lw = dict(LOSS_WEIGHTS if loss_weights is None else loss_weights)
+        L = _L()
+        descs = (ViewDesc * self.V)()
+        for v, cam in enumerate(cameras):
+            vm = cam.viewmat.detach().double().cpu().reshape(-1).tolist()
+            for k in range(16):
+                descs[v].viewmat[k] = vm[k]
+            descs[v].fx, descs[v].fy, descs[v].cx, descs[v].cy = cam.fx, cam.fy, cam.cx, cam.cy
+            descs[v].width, descs[v].height = cam.width, cam.height
+        self.descs = descs
+        tt, tp = _I(0), _LL(0)
+        check(L.gstex_batch_layout(self.V, descs, self.bw, ctypes.byref(tt), ctypes.byref(tp)), "batch_layout")
+        self.total_tiles, self.total_pixels = tt.value, tp.value
+        self.sizes = [(c.height, c.width) for c in cameras]
+        dev = self.dev
+        u8 = dict(dtype=torch.uint8, device=dev)
+        f32 = dict(dtype=torch.float32, device=dev)
+        i32 = dict(dtype=torch.int32, device=dev)
+        i64 = dict(dtype=torch.int64, device=dev)
+        self.views_dev = torch.empty(L.gstex_batch_views_bytes(self.V), **u8)
+        self.tile_view = torch.empty(self.total_tiles, **i32)
+        self.pix_offsets = torch.empty(self.V + 1, **i64)
+        stream = torch.cuda.current_stream(dev).cuda_stream
+        check(L.gstex_batch_prepare(self.V, descs, self.bw, ptr(self.views_dev), ptr(self.tile_view),
+                                    ptr(self.pix_offsets), stream), "batch_prepare")
+        self.pix_offsets_host = self.pix_offsets.cpu().tolist()
+        # per-(view, Gaussian) buffers
+        VN = self.V * self.N
+        self.colors = torch.empty((self.V, self.N, 3), **f32)
+        self.counts = torch.empty(VN, **i32)
+        self.cum = torch.empty(VN, **i32)
+        self.total = torch.zeros(1, **i64)
+        self.scan_ws = torch.empty(L.gstex_scan_workspace_bytes(VN), **u8)
+        # intersections (capacity-sized)
+        self.capacity = int(capacity) if capacity else max(1 << 20, 4 * VN)
+        self._alloc_isect()
+        self.count = torch.zeros(1, **i64)
+        self.overflow = torch.zeros(1, **i32)
+        self.bins = torch.empty((self.total_tiles, 2), **i32)
+        self.queue = torch.zeros(1, **i32)
+        self.bg = torch.tensor(list(background), **f32)
+        # per-pixel outputs of all views
+        P = self.total_pixels
+        self.out = dict(img=torch.empty((P, 3), **f32), depth=torch.empty(P, **f32), reg=torch.empty(P, **f32),
+                        texture=torch.empty((P, self.C), **f32), normal=torch.empty((P, 3), **f32),
+                        final_T=torch.empty(P, **f32), final_idx=torch.empty(P, **i32),
+                        depth_idx=torch.empty(P, **i32), reg_s=torch.empty((P, 3), **f32))
+        self.ups = dict(img=torch.zeros((P, 3), **f32), texture=torch.zeros((P, self.C), **f32),
+                        normal=torch.zeros((P, 3), **f32), reg=torch.zeros(P, **f32))
+        self.loss = torch.zeros(1, **f32)
+        self.moments = torch.empty(L.gstex_batch_backward_workspace_bytes(self.N), **u8)
+        self.grads = None
+        self.graph = None
+
+    def _alloc_isect(self):
+        L = _L()
+        cap = self.capacity
+        dev = self.dev
+        self.keys = torch.empty(cap, dtype=torch.int64, device=dev)
+        self.vals = torch.empty(cap, dtype=torch.int32, device=dev)
+        self.keys_sorted = torch.empty(cap, dtype=torch.int64, device=dev)
+        self.gids_sorted = torch.empty(cap, dtype=torch.int32, device=dev)
+        self.sort_ws = torch.empty(L.gstex_sort_workspace_bytes(cap), dtype=torch.uint8, device=dev)
+
+    def end_bit(self):
+        return 32 + max(1, int(self.total_tiles).bit_length())
+
+    # ------------------------------------------------------------------
+    def _inputs(self, s: Scene) -> BatchInputs:
+        bi = BatchInputs()
+        bi.num_points, bi.num_views, bi.block_width = self.N, self.V, self.bw
+        bi.channels, bi.num_texels, bi.texture_dtype, bi.settings = self.C, s.texture.shape[0], self.texmode, \
+            self.settings
+        bi.total_tiles = self.total_tiles
+        bi.views, bi.tile_view, bi.tile_order = ptr(self.views_dev), ptr(self.tile_view), None
+        bi.gaussian_ids_sorted, bi.tile_bins = ptr(self.gids_sorted), ptr(self.bins)
+        bi.colors, bi.opacities, bi.means, bi.scales = ptr(self.colors), ptr(s.opacity), ptr(s.means), ptr(s.scales)
+        bi.glob_scale = float(s.glob_scale)
+        bi.quats, bi.uv0, bi.umap, bi.vmap = ptr(s.quats), ptr(s.uv0), ptr(s.umap), ptr(s.vmap)
+        bi.texture_dims, bi.texture, bi.background = ptr(s.texture_dims), ptr(s.texture), ptr(self.bg)
+        bi.queue, bi.grid = ptr(self.queue), self.grid
+        return bi
+
+    def bin(self, s: Scene):
+        """Projection, SH colours and binning of all views (device only)."""
+        L = _L()
+        st = torch.cuda.current_stream(self.dev).cuda_stream
+        sh_dtype = 1 if s.sh_coeffs.dtype == torch.bfloat16 else 0
+        check(L.gstex_batch_project(self.N, self.V, ptr(self.views_dev), ptr(s.means), ptr(s.scales),
+                                    float(s.glob_scale), ptr(s.quats), ptr(s.sh_coeffs), sh_dtype, s.sh_degree,
+                                    self.bw, ptr(self.colors), ptr(self.counts), st), "batch_project")
+        VN = self.V * self.N
+        check(L.gstex_inclusive_scan_i32(VN, ptr(self.counts), ptr(self.cum), ptr(self.total), ptr(self.scan_ws),
+                                         self.scan_ws.numel(), st), "scan")
+        check(L.gstex_batch_emit(self.N, self.V, ptr(self.views_dev), ptr(s.means), ptr(s.scales),
+                                 float(s.glob_scale), ptr(s.quats), self.bw, ptr(self.cum), ptr(self.total),
+                                 self.capacity, ptr(self.keys), ptr(self.vals), ptr(self.count), ptr(self.overflow),
+                                 st), "batch_emit")
+        check(L.gstex_sort_pairs_dyn(self.capacity, ptr(self.count), self.end_bit(), ptr(self.keys), ptr(self.vals),
+                                     ptr(self.keys_sorted), ptr(self.gids_sorted), ptr(self.sort_ws),
+                                     self.sort_ws.numel(), st), "sort_pairs_dyn")
+        check(L.gstex_get_tile_bin_edges_dyn(self.capacity, ptr(self.count), ptr(self.keys_sorted), self.total_tiles,
+                                             ptr(self.bins), st), "tile_bin_edges_dyn")
+
+    def forward(self, s: Scene):
+        L = _L()
+        st = torch.cuda.current_stream(self.dev).cuda_stream
+        bi = self._inputs(s)
+        o = self.out
+        fo = _lib.ForwardOutputs(ptr(o["img"]), ptr(o["depth"]), ptr(o["reg"]), ptr(o["texture"]), ptr(o["normal"]),
+                                 ptr(o["final_T"]), ptr(o["final_idx"]), ptr(o["depth_idx"]), ptr(o["reg_s"]))
+        check(L.gstex_batch_forward(ctypes.byref(bi), ctypes.byref(fo), st), "batch_forward")
+        return o
+
+    def image_loss(self, tgt_img, tgt_tex):
+        L = _L()
+        st = torch.cuda.current_stream(self.dev).cuda_stream
+        o, u, w = self.out, self.ups, self.lw
+        check(L.gstex_batch_image_loss(self.total_pixels, self.V, ptr(self.pix_offsets), self.C, ptr(o["img"]),
+                                       ptr(o["texture"]), ptr(o["normal"]), ptr(o["reg"]), ptr(tgt_img),
+                                       ptr(tgt_tex), w["img"], w["texture"], w["reg"], w["normal"], ptr(u["img"]),
+                                       ptr(u["texture"]), ptr(u["normal"]), ptr(u["reg"]), ptr(self.loss), st),
+              "batch_image_loss")
+        return self.loss
+
+    def _grad_buffers(self, s: Scene):
+        if self.grads is None:
+            f32 = dict(dtype=torch.float32, device=self.dev)
+            N = self.N
+            tex_cols = 4 if self.texmode == 1 else self.C
+            nb = s.sh_coeffs.shape[1]
+            self.grads = dict(vcolors=torch.empty((self.V, N, 3), **f32), opacity=torch.empty(s.opacity.shape, **f32),
+                              means=torch.empty((N, 3), **f32), scales=torch.empty((N, 3), **f32),
+                              quats=torch.empty((N, 4), **f32), uv0=torch.empty(s.uv0.shape, **f32),
+                              umap=torch.empty(s.umap.shape, **f32), vmap=torch.empty(s.vmap.shape, **f32),
+                              texture=torch.zeros((s.texture.shape[0], tex_cols), **f32),
+                              sh_coeffs=torch.empty((N, nb, 3), **f32))
+        return self.grads
+
+    def backward(self, s: Scene, upstream: Optional[dict] = None):
+        """Gradients w.r.t. the scene given upstream pixel gradients (default:
+        those written by image_loss).  Returns a dict of gradient tensors."""
+        L = _L()
+        st = torch.cuda.current_stream(self.dev).cuda_stream
+        g = self._grad_buffers(s)
+        u = self.ups if upstream is None else upstream
+        g["texture"].zero_()
+        o = self.out
+        bio = _lib.BackwardIO(ptr(o["final_T"]), ptr(o["final_idx"]), ptr(o["depth_idx"]), ptr(o["reg_s"]),
+                              ptr(u.get("img")), ptr(u.get("depth")), ptr(u.get("reg")), ptr(u.get("alpha")),
+                              ptr(u.get("texture")), ptr(u.get("normal")), ptr(g["vcolors"]), ptr(g["opacity"]),
+                              ptr(g["means"]), ptr(g["scales"]), ptr(g["quats"]), ptr(g["uv0"]), ptr(g["umap"]),
+                              ptr(g["vmap"]), ptr(g["texture"]), ptr(self.moments), self.moments.numel())
+        bi = self._inputs(s)
+        check(L.gstex_batch_backward(ctypes.byref(bi), ctypes.byref(bio), st), "batch_backward")
+        check(L.gstex_batch_sh_backward(self.N, self.V, ptr(self.views_dev), ptr(s.means), s.sh_degree,
+                                        ptr(g["vcolors"]), ptr(g["sh_coeffs"]), st), "batch_sh_backward")
+        return g
+
+    def step(self, s: Scene, tgt_img, tgt_tex):
+        """One forward + backward pass over all views; returns the device loss."""
+        self.bin(s)
+        self.forward(s)
+        loss = self.image_loss(tgt_img, tgt_tex)
+        self.backward(s)
+        return loss
+
+    # ------------------------------------------------------------------
+    def capture(self, s: Scene, tgt_img, tgt_tex):
+        """Capture ``step`` for these (static) tensors in a CUDA graph."""
+        self._grad_buffers(s)
+        side = torch.cuda.Stream(self.dev)
+        side.wait_stream(torch.cuda.current_stream(self.dev))
+        with torch.cuda.stream(side):
+            for _ in range(2):
+                self.step(s, tgt_img, tgt_tex)
+        torch.cuda.current_stream(self.dev).wait_stream(side)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.step(s, tgt_img, tgt_tex)
+        self.graph = g
+        return g
+
+    def replay(self):
+        self.graph.replay()
+        return self.loss
+
+    def check_capacity(self) -> bool:
+        """True if the last step's intersections fit the capacity (syncs)."""
+        return int(self.overflow.item()) == 0
+
+    def intersections(self) -> int:
+        return int(self.total.item())
+
+    def grow(self, factor: float = 1.5):
+        """Resize the intersection buffers after an overflow (invalidates a captured graph)."""
+        need = int(self.total.item())
+        self.capacity = max(int(need * factor), self.capacity + 1)
+        self._alloc_isect()
+        self.overflow.zero_()
+        self.graph = None
+
+    # views of the per-pixel outputs -----------------------------------
+    def view_output(self, name: str, v: int):
+        H, W = self.sizes[v]
+        a, b = self.pix_offsets_host[v], self.pix_offsets_host[v + 1]
+        t = self.out[name][a:b]
+        return t.reshape(H, W, *t.shape[1:])
+
+
+def plain_step(s: Scene, cameras: Sequence[Camera], tgt_img, tgt_tex, pix_offsets, *, block_width=16,
+               settings=1 << 8, background=None, loss_weights=None, timers=None):
+    """The per-view path a caller of the reference API takes: for every camera,
+    SH colours, AABBs, tile counts, the host-synchronising intersection count,
+    binning, texture_forward, the image losses, texture_backward and the SH
+    adjoint, one view after another (float32 or bfloat16 texels as given).
+    Returns (loss, gradient dict); gradients are summed over views."""
+    from . import cuda as C
+    from .get_aabb_2d import project_points
+    from .utils import bin_and_sort_gaussians, compute_cumulative_intersects
+    L = _L()
+    dev = s.means.device
+    lw = dict(LOSS_WEIGHTS if loss_weights is None else loss_weights)
+    bg = background if background is not None else torch.zeros(3, device=dev)
+    N = s.means.shape[0]
+    nb = s.sh_coeffs.shape[1]
+    grads = None
+    loss_total = torch.zeros((), device=dev)
+    st = torch.cuda.current_stream(dev).cuda_stream
+    bw = block_width
+    for v, cam in enumerate(cameras):
+        H, W = cam.height, cam.width
+        vm = cam.viewmat.to(dev)
+        c2w = torch.linalg.inv(vm)
+        campos = c2w[:3, 3]
+        dirs = (s.means - campos[None]).contiguous()
+        coeffs = s.sh_coeffs if s.sh_coeffs.dtype == torch.float32 else s.sh_coeffs.float()
+        colors = C.compute_sh_forward(N, s.sh_degree, s.sh_degree, dirs, coeffs)
+        intr = (cam.fx, cam.fy, cam.cx, cam.cy)
+        _, depths = project_points(s.means, vm, intr)
+        centers, extents = C.get_aabb_2d(s.means, s.scales, s.glob_scale, s.quats, vm, *intr)
+        counts = C.num_tiles_hit(centers, extents, H, W, bw)
+        n_isect, cum = compute_cumulative_intersects(counts)
+        tb = ((W + bw - 1) // bw, (H + bw - 1) // bw, 1)
+        _, _, _, gids, bins = bin_and_sort_gaussians(N, n_isect, centers, extents, depths.contiguous(), cum, tb, bw)
+        info = (N, 1, s.channels)
+        outs = C.texture_forward(tb, (bw, bw, 1), (W, H, 1), info, s.texture_dims, gids, bins, colors, s.opacity,
+                                 s.means, s.scales, s.glob_scale, s.quats, s.uv0, s.umap, s.vmap, s.texture, vm, c2w,
+                                 *intr, settings, bg)
+        img, depth, reg, tex, normal, final_T, final_idx, depth_idx, reg_s = outs
+        a, b = pix_offsets[v], pix_offsets[v + 1]
+        P = H * W
+        off = torch.tensor([0, P], dtype=torch.int64, device=dev)
+        v_img = torch.empty_like(img)
+        v_tex = torch.empty_like(tex)
+        v_normal = torch.empty_like(normal)
+        v_reg = torch.empty_like(reg)
+        loss = torch.zeros(1, device=dev)
+        check(L.gstex_batch_image_loss(P, 1, ptr(off), s.channels, ptr(img), ptr(tex), ptr(normal), ptr(reg),
+                                       ptr(tgt_img[a:b]), ptr(tgt_tex[a:b]), lw["img"], lw["texture"], lw["reg"],
+                                       lw["normal"], ptr(v_img), ptr(v_tex), ptr(v_normal), ptr(v_reg), ptr(loss), st),
+              "image_loss")
+        zeros = torch.zeros_like(reg)
+        g = C.texture_backward(H, W, bw, info, s.texture_dims, gids, bins, colors, s.opacity, s.means, s.scales,
+                               s.glob_scale, s.quats, s.uv0, s.umap, s.vmap, s.texture, vm, c2w, *intr, settings, bg,
+                               final_T, final_idx, depth_idx, reg_s, v_img, zeros, v_reg, zeros, v_tex, v_normal)
+        v_colors, v_opacity, v_means, v_scales, v_quats, v_uv0, v_umap, v_vmap, v_texture = g
+        v_coeffs = C.compute_sh_backward(N, s.sh_degree, s.sh_degree, dirs, v_colors)
+        cur = dict(opacity=v_opacity, means=v_means, scales=v_scales, quats=v_quats, uv0=v_uv0, umap=v_umap,
+                   vmap=v_vmap, texture=v_texture, sh_coeffs=v_coeffs)
+        if grads is None:
+            grads = cur
+        else:
+            for k in grads:
+                grads[k].add_(cur[k])
+        loss_total = loss_total + loss[0]
+    return loss_total, grads

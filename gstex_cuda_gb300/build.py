@@ -28,10 +28,9 @@ PER_FILE = {
     "project.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"],
     "binning.cu": ["-fmad=false", "-prec-div=true"],
     "raster.cu": ["--use_fast_math"],
-    "batch.cu": ["--use_fast_math"],
+    "batch.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"],
     "sample.cu": ["-fmad=false"],
     "status.cu": [],
-    "noalloc.cu": ["-fmad=false", "-prec-div=true"],
 }
 
 

@@ -1,0 +1,427 @@
+// Batched multi-view rendering: projection of every (view, Gaussian) pair,
+// capacity-bounded intersection emission, device-count sort and tile ranges,
+// the demo's image losses, and the SH adjoint over all views.
+//
+// Nothing here reads a size back to the host, so one forward + backward step
+// over all views can be captured in a CUDA graph.  Global tiles of all views
+// are numbered view by view (tile_offset); sort keys are
+// (global tile << 32 | float bits of the camera depth), so one sort orders
+// every view's tiles front to back.
+#include <vector>
+
+#include "common.cuh"
+#include "project.cuh"
+#include "raster.cuh"
+
+namespace gstex {
+
+// ---------------------------------------------------------------------------
+// Projection: AABB, tile count, depth and SH colour of each (view, Gaussian).
+// One thread per Gaussian loops over the views so parameters and SH
+// coefficients are read once.
+// ---------------------------------------------------------------------------
+template <typename SHT>
+__global__ void batch_project_kernel(int N, int V, const BatchView* __restrict__ views, const float3* __restrict__ means,
+                                     const float* __restrict__ scales, float glob, const float4* __restrict__ quats,
+                                     const SHT* __restrict__ sh, int sh_degree, int bw, float3* __restrict__ colors,
+                                     int32_t* __restrict__ counts) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const float3 p = means[i];
+    const float4 q = quats[i];
+    const float sx = scales[3 * i], sy = scales[3 * i + 1];
+    const int B = sh_bases(sh_degree);
+    float k[25][3];
+    for (int b = 0; b < B; b++)
+        for (int c = 0; c < 3; c++) k[b][c] = (float)sh[((size_t)i * B + b) * 3 + c];
+    for (int v = 0; v < V; v++) {
+        const BatchView& bv = views[v];
+        float m[12];
+#pragma unroll
+        for (int r = 0; r < 3; r++) {
+            m[4 * r + 0] = bv.V.r[3 * r + 0];
+            m[4 * r + 1] = bv.V.r[3 * r + 1];
+            m[4 * r + 2] = bv.V.r[3 * r + 2];
+            m[4 * r + 3] = bv.V.t[r];
+        }
+        float2 c, e;
+        float z;
+        aabb_2d(m, bv.V.fx, bv.V.fy, bv.V.cx, bv.V.cy, p, q, sx, sy, glob, c, e, z);
+        counts[(size_t)v * N + i] = tiles_hit(c, e, bv.tiles_x, bv.tiles_y, (float)bw);
+        float Y[25];
+        const int nb = sh_basis(sh_degree, make_float3(p.x - bv.campos[0], p.y - bv.campos[1], p.z - bv.campos[2]), Y);
+        float3 col = make_float3(0.f, 0.f, 0.f);
+        for (int b = 0; b < nb; b++) {
+            col.x += Y[b] * k[b][0];
+            col.y += Y[b] * k[b][1];
+            col.z += Y[b] * k[b][2];
+        }
+        colors[(size_t)v * N + i] = col;
+    }
+}
+
+// Emission into [cum[j-1], cum[j]) for j = v*N + i, clipped to the capacity.
+// Slots a Gaussian does not write (tiny or culled extents) hold the view's
+// tile 0 with depth bits 0 and Gaussian 0, the reference's zero-slot value.
+__global__ void batch_emit_kernel(int N, int V, const BatchView* __restrict__ views, const float3* __restrict__ means,
+                                  const float* __restrict__ scales, float glob, const float4* __restrict__ quats,
+                                  int bw, const int32_t* __restrict__ cum, long long capacity,
+                                  int64_t* __restrict__ keys, int32_t* __restrict__ vals) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const float3 p = means[i];
+    const float4 q = quats[i];
+    const float sx = scales[3 * i], sy = scales[3 * i + 1];
+    for (int v = 0; v < V; v++) {
+        const BatchView& bv = views[v];
+        const size_t j = (size_t)v * N + i;
+        long long lo = j == 0 ? 0 : (long long)(uint32_t)cum[j - 1];
+        long long hi = (long long)(uint32_t)cum[j];
+        if (hi > capacity) hi = capacity;
+        if (lo >= hi) continue;
+        float m[12];
+#pragma unroll
+        for (int r = 0; r < 3; r++) {
+            m[4 * r + 0] = bv.V.r[3 * r + 0];
+            m[4 * r + 1] = bv.V.r[3 * r + 1];
+            m[4 * r + 2] = bv.V.r[3 * r + 2];
+            m[4 * r + 3] = bv.V.t[r];
+        }
+        float2 c, e;
+        float z;
+        aabb_2d(m, bv.V.fx, bv.V.fy, bv.V.cx, bv.V.cy, p, q, sx, sy, glob, c, e, z);
+        long long cur = lo;
+        if (!((double)e.x <= 1e-4 && (double)e.y <= 1e-4)) {
+            int x0, y0, x1, y1;
+            tile_rect(c, e, bv.tiles_x, bv.tiles_y, bw, x0, y0, x1, y1);
+            const uint64_t dbits = (uint64_t)(int64_t)__float_as_int(z);
+            for (int ty = y0; ty < y1 && cur < hi; ++ty)
+                for (int tx = x0; tx < x1 && cur < hi; ++tx) {
+                    const uint64_t tile = (uint64_t)(bv.tile_offset + ty * bv.tiles_x + tx);
+                    keys[cur] = (int64_t)((tile << 32) | dbits);
+                    vals[cur] = i;
+                    ++cur;
+                }
+        }
+        for (; cur < hi; ++cur) {
+            keys[cur] = (int64_t)((uint64_t)bv.tile_offset << 32);
+            vals[cur] = 0;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Image losses of the reference demo (example.py:189-209) with their
+// gradients, over the concatenated pixels of all views:
+//   per view: w_img * MSE(img, tgt) + w_tex * MSE(tex, tgt_tex)
+//           + w_reg * mean(reg) + w_normal * mean(nx^2 + ny^2 + (1 - nz)^2)
+// ---------------------------------------------------------------------------
+__global__ void batch_loss_kernel(long long total, int V, const long long* __restrict__ pix_off, int C,
+                                  const float3* __restrict__ img, const float* __restrict__ tex,
+                                  const float3* __restrict__ normal, const float* __restrict__ reg,
+                                  const float3* __restrict__ tgt_img, const float* __restrict__ tgt_tex, float w_img,
+                                  float w_tex, float w_reg, float w_normal, float3* __restrict__ v_img,
+                                  float* __restrict__ v_tex, float3* __restrict__ v_normal, float* __restrict__ v_reg,
+                                  float* __restrict__ loss) {
+    __shared__ float part[32];
+    float acc = 0.f;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < total;
+         p += (long long)gridDim.x * blockDim.x) {
+        int lo = 0, hi = V;  // view of pixel p: pix_off[v] <= p < pix_off[v+1]
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (pix_off[mid] <= p) lo = mid; else hi = mid;
+        }
+        const float inv = 1.f / (float)(pix_off[lo + 1] - pix_off[lo]);
+        const float3 a = img[p], t = tgt_img[p];
+        const float3 d = make_float3(a.x - t.x, a.y - t.y, a.z - t.z);
+        acc += w_img * inv / 3.f * (d.x * d.x + d.y * d.y + d.z * d.z);
+        const float gi = 2.f * w_img * inv / 3.f;
+        v_img[p] = make_float3(gi * d.x, gi * d.y, gi * d.z);
+        if (C > 0) {
+            const float gt = 2.f * w_tex * inv / (float)C;
+            for (int c = 0; c < C; c++) {
+                const float dt = tex[p * C + c] - tgt_tex[p * C + c];
+                acc += w_tex * inv / (float)C * dt * dt;
+                v_tex[p * C + c] = gt * dt;
+            }
+        }
+        acc += w_reg * inv * reg[p];
+        v_reg[p] = w_reg * inv;
+        const float3 n = normal[p];
+        acc += w_normal * inv * (n.x * n.x + n.y * n.y + (1.f - n.z) * (1.f - n.z));
+        const float gn = 2.f * w_normal * inv;
+        v_normal[p] = make_float3(gn * n.x, gn * n.y, gn * (n.z - 1.f));
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        float s = threadIdx.x < (blockDim.x >> 5) ? part[threadIdx.x] : 0.f;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) atomicAdd(loss, s);
+    }
+}
+
+// SH adjoint summed over views: v_coeffs[i,b,c] = sum_v Y_b(dir_v) v_color[v,i,c].
+__global__ void batch_sh_backward_kernel(int N, int V, const BatchView* __restrict__ views,
+                                         const float3* __restrict__ means, int sh_degree,
+                                         const float3* __restrict__ vcol, float* __restrict__ v_coeffs) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const int B = sh_bases(sh_degree);
+    float acc[25][3];
+    for (int b = 0; b < 25; b++) acc[b][0] = acc[b][1] = acc[b][2] = 0.f;
+    const float3 p = means[i];
+    for (int v = 0; v < V; v++) {
+        const float3 g = vcol[(size_t)v * N + i];
+        if (g.x == 0.f && g.y == 0.f && g.z == 0.f) continue;
+        const BatchView& bv = views[v];
+        float Y[25];
+        const int nb = sh_basis(sh_degree, make_float3(p.x - bv.campos[0], p.y - bv.campos[1], p.z - bv.campos[2]), Y);
+        for (int b = 0; b < nb; b++) {
+            acc[b][0] += Y[b] * g.x;
+            acc[b][1] += Y[b] * g.y;
+            acc[b][2] += Y[b] * g.z;
+        }
+    }
+    float* o = v_coeffs + (size_t)i * B * 3;
+    for (int b = 0; b < B; b++) {
+        o[3 * b + 0] = acc[b][0];
+        o[3 * b + 1] = acc[b][1];
+        o[3 * b + 2] = acc[b][2];
+    }
+}
+
+__global__ void clamp_count_kernel(const int64_t* __restrict__ total, long long capacity, int64_t* __restrict__ n,
+                                   int* __restrict__ overflow) {
+    const long long t = *total;
+    *n = t < capacity ? t : capacity;
+    if (t > capacity) atomicOr(overflow, 1);
+}
+
+}  // namespace gstex
+
+using namespace gstex;
+
+extern "C" size_t gstex_batch_views_bytes(int num_views) { return sizeof(BatchView) * (size_t)(num_views > 0 ? num_views : 1); }
+
+extern "C" int gstex_batch_layout(int num_views, const gstex_view_desc* views, int block_width, int* total_tiles,
+                                  long long* total_pixels) {
+    GSTEX_REQUIRE(num_views > 0 && views && block_width >= 2 && block_width <= kMaxBlockWidth && total_tiles &&
+                  total_pixels);
+    long long tiles = 0, pix = 0;
+    for (int v = 0; v < num_views; v++) {
+        GSTEX_REQUIRE(views[v].width > 0 && views[v].height > 0);
+        tiles += (long long)ceil_div(views[v].width, block_width) * ceil_div(views[v].height, block_width);
+        pix += (long long)views[v].width * views[v].height;
+    }
+    if (tiles >= (1ll << 31) - 1) return GSTEX_ERR_UNSUPPORTED;
+    *total_tiles = (int)tiles;
+    *total_pixels = pix;
+    return GSTEX_OK;
+}
+
+extern "C" int gstex_batch_prepare(int num_views, const gstex_view_desc* views, int block_width, void* views_dev,
+                                   int32_t* tile_view_dev, long long* pix_offsets_dev, gstex_stream_t s) {
+    int total_tiles = 0;
+    long long total_pix = 0;
+    int rc = gstex_batch_layout(num_views, views, block_width, &total_tiles, &total_pix);
+    if (rc) return rc;
+    GSTEX_REQUIRE(views_dev && tile_view_dev && pix_offsets_dev);
+    std::vector<BatchView> bv(num_views);
+    std::vector<int32_t> tv(total_tiles);
+    std::vector<long long> po(num_views + 1);
+    int toff = 0;
+    long long poff = 0;
+    for (int v = 0; v < num_views; v++) {
+        const gstex_view_desc& d = views[v];
+        BatchView& b = bv[v];
+        for (int r = 0; r < 3; r++) {
+            for (int c = 0; c < 3; c++) b.V.r[3 * r + c] = d.viewmat[4 * r + c];
+            b.V.t[r] = d.viewmat[4 * r + 3];
+        }
+        b.V.fx = d.fx; b.V.fy = d.fy; b.V.cx = d.cx; b.V.cy = d.cy;
+        b.W = d.width; b.H = d.height;
+        b.tiles_x = ceil_div(d.width, block_width);
+        b.tiles_y = ceil_div(d.height, block_width);
+        b.tile_offset = toff;
+        b.pix_offset = (int)poff;
+        // camera centre = -R^T t
+        for (int c = 0; c < 3; c++)
+            b.campos[c] = -(b.V.r[c] * b.V.t[0] + b.V.r[3 + c] * b.V.t[1] + b.V.r[6 + c] * b.V.t[2]);
+        b.pad = 0;
+        for (int k = 0; k < b.tiles_x * b.tiles_y; k++) tv[toff + k] = v;
+        po[v] = poff;
+        toff += b.tiles_x * b.tiles_y;
+        poff += (long long)d.width * d.height;
+    }
+    po[num_views] = poff;
+    if (poff >= (1ll << 31)) return GSTEX_ERR_UNSUPPORTED;
+    cudaStream_t stream = (cudaStream_t)s;
+    cudaError_t e = cudaMemcpyAsync(views_dev, bv.data(), sizeof(BatchView) * num_views, cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(tile_view_dev, tv.data(), sizeof(int32_t) * total_tiles, cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(pix_offsets_dev, po.data(), sizeof(long long) * (num_views + 1), cudaMemcpyHostToDevice,
+                            stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);  // host vectors go out of scope
+    if (e != cudaSuccess) { set_cuda_error(e, "batch_prepare"); return GSTEX_ERR_CUDA; }
+    return GSTEX_OK;
+}
+
+extern "C" int gstex_batch_project(int N, int V, const void* views_dev, const float* means, const float* scales,
+                                   float glob_scale, const float* quats, const void* sh_coeffs, int sh_dtype,
+                                   int sh_degree, int block_width, float* colors, int32_t* counts, gstex_stream_t s) {
+    GSTEX_REQUIRE(N >= 0 && V > 0 && views_dev && block_width >= 2 && block_width <= kMaxBlockWidth);
+    GSTEX_REQUIRE(sh_degree >= 0 && sh_degree <= 4 && (sh_dtype == 0 || sh_dtype == 1));
+    if (N == 0) return GSTEX_OK;
+    GSTEX_REQUIRE(means && scales && quats && sh_coeffs && colors && counts);
+    cudaStream_t stream = (cudaStream_t)s;
+    const BatchView* bv = (const BatchView*)views_dev;
+    if (sh_dtype == 1)
+        batch_project_kernel<__nv_bfloat16><<<ceil_div(N, 128), 128, 0, stream>>>(
+            N, V, bv, (const float3*)means, scales, glob_scale, (const float4*)quats,
+            (const __nv_bfloat16*)sh_coeffs, sh_degree, block_width, (float3*)colors, counts);
+    else
+        batch_project_kernel<float><<<ceil_div(N, 128), 128, 0, stream>>>(
+            N, V, bv, (const float3*)means, scales, glob_scale, (const float4*)quats, (const float*)sh_coeffs,
+            sh_degree, block_width, (float3*)colors, counts);
+    return check_launch("batch_project");
+}
+
+extern "C" int gstex_batch_emit(int N, int V, const void* views_dev, const float* means, const float* scales,
+                                float glob_scale, const float* quats, int block_width, const int32_t* cum,
+                                const int64_t* total, long long capacity, int64_t* keys, int32_t* vals,
+                                int64_t* count, int* overflow, gstex_stream_t s) {
+    GSTEX_REQUIRE(N >= 0 && V > 0 && views_dev && capacity >= 0 && total && count && overflow);
+    cudaStream_t stream = (cudaStream_t)s;
+    clamp_count_kernel<<<1, 1, 0, stream>>>(total, capacity, count, overflow);
+    if (N == 0 || capacity == 0) return check_launch("batch_emit");
+    GSTEX_REQUIRE(means && scales && quats && cum && keys && vals);
+    batch_emit_kernel<<<ceil_div(N, 128), 128, 0, stream>>>(N, V, (const BatchView*)views_dev, (const float3*)means,
+                                                            scales, glob_scale, (const float4*)quats, block_width, cum,
+                                                            capacity, keys, vals);
+    return check_launch("batch_emit", 2);
+}
+
+static int batch_scene(const gstex_batch_inputs* in, SceneArgs& a, BatchArgs& ba) {
+    GSTEX_REQUIRE(in && in->num_points >= 0 && in->num_views > 0 && in->total_tiles > 0);
+    GSTEX_REQUIRE(in->block_width >= 2 && in->block_width <= kMaxBlockWidth);
+    GSTEX_REQUIRE(in->channels >= 0);
+    if (in->channels > kMaxChannels) return GSTEX_ERR_UNSUPPORTED;
+    if (in->texture_dtype == 1 && in->channels != 3) return GSTEX_ERR_UNSUPPORTED;
+    if (in->settings & (1 << 16)) return GSTEX_ERR_UNSUPPORTED;
+    GSTEX_REQUIRE(in->views && in->tile_view && in->tile_bins && in->colors && in->background && in->queue);
+    if (in->num_points > 0)
+        GSTEX_REQUIRE(in->gaussian_ids_sorted && in->texture_dims && in->opacities && in->means && in->scales &&
+                      in->quats && in->uv0 && in->umap && in->vmap);
+    a.N = in->num_points;
+    a.C = in->channels;
+    a.T = in->num_texels;
+    a.dims = (const int3*)in->texture_dims;
+    a.gids = in->gaussian_ids_sorted;
+    a.means = (const float3*)in->means;
+    a.scales = in->scales;
+    a.glob = in->glob_scale;
+    a.quats = (const float4*)in->quats;
+    a.opac = in->opacities;
+    a.uv0 = (const float2*)in->uv0;
+    a.umap = (const float3*)in->umap;
+    a.vmap = (const float3*)in->vmap;
+    a.tex = in->texture;
+    a.settings = in->settings;
+    a.bg = in->background;
+    ba.num_points = in->num_points;
+    ba.total_tiles = in->total_tiles;
+    ba.views = (const BatchView*)in->views;
+    ba.tile_view = in->tile_view;
+    ba.order = in->tile_order;
+    ba.bins = (const int2*)in->tile_bins;
+    ba.colors = (const float3*)in->colors;
+    ba.vcolors = nullptr;
+    ba.queue = in->queue;
+    return GSTEX_OK;
+}
+
+static int grid_of(const gstex_batch_inputs* in, bool backward) {
+    if (in->grid > 0) return in->grid;
+    int g = resident_ctas(in->block_width, backward, in->texture_dtype, in->channels);
+    return g > 0 ? g : 152;
+}
+
+extern "C" int gstex_batch_forward(const gstex_batch_inputs* in, const gstex_forward_outputs* out, gstex_stream_t s) {
+    SceneArgs a;
+    BatchArgs ba;
+    int rc = batch_scene(in, a, ba);
+    if (rc) return rc;
+    GSTEX_REQUIRE(out && out->img && out->depth && out->reg && out->normal && out->final_T && out->final_idx &&
+                  out->depth_idx && out->reg_s);
+    if (a.C > 0) GSTEX_REQUIRE(out->texture);
+    cudaStream_t stream = (cudaStream_t)s;
+    cudaError_t e = cudaMemsetAsync(in->queue, 0, sizeof(int), stream);
+    if (e != cudaSuccess) { set_cuda_error(e, "batch_forward"); return GSTEX_ERR_CUDA; }
+    FwdOut o{ (float3*)out->img, out->depth, out->reg, out->texture, (float3*)out->normal, out->final_T,
+              out->final_idx, out->depth_idx, (float3*)out->reg_s };
+    return launch_fwd_batch(a, ba, o, in->block_width, in->texture_dtype, grid_of(in, false), stream);
+}
+
+extern "C" size_t gstex_batch_backward_workspace_bytes(int num_points) {
+    return (size_t)(num_points > 0 ? num_points : 1) * kMomStride * sizeof(float);
+}
+
+extern "C" int gstex_batch_backward(const gstex_batch_inputs* in, const gstex_backward_io* io, gstex_stream_t s) {
+    SceneArgs a;
+    BatchArgs ba;
+    int rc = batch_scene(in, a, ba);
+    if (rc) return rc;
+    GSTEX_REQUIRE(io && io->final_T && io->final_idx && io->depth_idx && io->reg_s && io->workspace);
+    GSTEX_REQUIRE(io->v_colors && io->v_opacity && io->v_means && io->v_scales && io->v_quats && io->v_uv0 &&
+                  io->v_umap && io->v_vmap);
+    if (a.C > 0) GSTEX_REQUIRE(io->v_tex_grad);
+    if (io->workspace_bytes < gstex_batch_backward_workspace_bytes(a.N)) return GSTEX_ERR_CAPACITY;
+    if (a.N == 0) return GSTEX_OK;
+    cudaStream_t stream = (cudaStream_t)s;
+    cudaError_t e = cudaMemsetAsync(in->queue, 0, sizeof(int), stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(io->workspace, 0, gstex_batch_backward_workspace_bytes(a.N), stream);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(io->v_colors, 0, (size_t)in->num_views * a.N * 3 * sizeof(float), stream);
+    if (e != cudaSuccess) { set_cuda_error(e, "batch_backward"); return GSTEX_ERR_CUDA; }
+    ba.vcolors = io->v_colors;
+    BwdArgs g{ io->final_T, io->final_idx, io->depth_idx, (const float3*)io->reg_s, (const float3*)io->v_img,
+               io->v_depth, io->v_reg, io->v_alpha, io->v_texture, (const float3*)io->v_normal,
+               (float*)io->workspace, io->v_tex_grad };
+    if ((rc = launch_bwd_batch(a, ba, g, in->block_width, in->texture_dtype, grid_of(in, true), stream))) return rc;
+    return launch_finalize(a, (const float*)io->workspace, io->v_opacity, io->v_means, io->v_scales, io->v_quats,
+                           io->v_uv0, io->v_umap, io->v_vmap, stream);
+}
+
+extern "C" int gstex_batch_sh_backward(int N, int V, const void* views_dev, const float* means, int sh_degree,
+                                       const float* v_colors, float* v_coeffs, gstex_stream_t s) {
+    GSTEX_REQUIRE(N >= 0 && V > 0 && views_dev && sh_degree >= 0 && sh_degree <= 4);
+    if (N == 0) return GSTEX_OK;
+    GSTEX_REQUIRE(means && v_colors && v_coeffs);
+    batch_sh_backward_kernel<<<ceil_div(N, 128), 128, 0, (cudaStream_t)s>>>(
+        N, V, (const BatchView*)views_dev, (const float3*)means, sh_degree, (const float3*)v_colors, v_coeffs);
+    return check_launch("batch_sh_backward");
+}
+
+extern "C" int gstex_batch_image_loss(long long total_pixels, int V, const long long* pix_offsets, int channels,
+                                      const float* img, const float* tex, const float* normal, const float* reg,
+                                      const float* tgt_img, const float* tgt_tex, float w_img, float w_tex,
+                                      float w_reg, float w_normal, float* v_img, float* v_tex, float* v_normal,
+                                      float* v_reg, float* loss, gstex_stream_t s) {
+    GSTEX_REQUIRE(total_pixels >= 0 && V > 0 && pix_offsets && channels >= 0 && loss);
+    GSTEX_REQUIRE(img && normal && reg && tgt_img && v_img && v_normal && v_reg);
+    if (channels > 0) GSTEX_REQUIRE(tex && tgt_tex && v_tex);
+    cudaStream_t stream = (cudaStream_t)s;
+    cudaError_t e = cudaMemsetAsync(loss, 0, sizeof(float), stream);
+    if (e != cudaSuccess) { set_cuda_error(e, "batch_image_loss"); return GSTEX_ERR_CUDA; }
+    if (total_pixels == 0) return GSTEX_OK;
+    const int blocks = (int)std::min<long long>(ceil_div((int)std::min<long long>(total_pixels, 1ll << 30), 256), 152 * 16);
+    batch_loss_kernel<<<blocks, 256, 0, stream>>>(total_pixels, V, pix_offsets, channels, (const float3*)img, tex,
+                                                  (const float3*)normal, reg, (const float3*)tgt_img, tgt_tex, w_img,
+                                                  w_tex, w_reg, w_normal, (float3*)v_img, v_tex, (float3*)v_normal,
+                                                  v_reg, loss);
+    return check_launch("batch_image_loss");
+}

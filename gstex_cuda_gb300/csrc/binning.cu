@@ -61,7 +61,12 @@ __global__ void emit_kernel(int n, int num_isect, const float2* __restrict__ cen
 // Tile ranges (reference csrc/forward.cu:76-98); tiles outside [0, num_tiles)
 // are ignored.
 // ---------------------------------------------------------------------------
-__global__ void bin_edges_kernel(int n, const int64_t* __restrict__ sorted, int num_tiles, int2* __restrict__ bins) {
+__global__ void bin_edges_kernel(int n, const int64_t* __restrict__ n_dev, const int64_t* __restrict__ sorted,
+                                 int num_tiles, int2* __restrict__ bins) {
+    if (n_dev) {
+        const int64_t m = *n_dev;
+        n = (int)(m < (int64_t)n ? (m > 0 ? m : 0) : n);
+    }
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int cur = (int)(sorted[i] >> 32);
@@ -105,10 +110,24 @@ static SortPlan sort_plan(int n) {
     return p;
 }
 
+// With n_dev set, the item count is read on the device (clamped to n) and the
+// chunk of each block is derived from it, so the launch shape does not depend
+// on the count.
+__device__ __forceinline__ void resolve_count(const int64_t* n_dev, int& n, int& chunk) {
+    if (n_dev) {
+        const int64_t m = *n_dev;
+        n = (int)(m < (int64_t)n ? (m > 0 ? m : 0) : n);
+        chunk = ceil_div(ceil_div(n, kSortTile), (int)gridDim.x) * kSortTile;
+        if (chunk < kSortTile) chunk = kSortTile;
+    }
+}
+
 __global__ void __launch_bounds__(kSortThreads) radix_hist_kernel(const uint64_t* __restrict__ keys, int n, int chunk,
-                                                                  int shift, uint32_t* __restrict__ hist) {
+                                                                  const int64_t* __restrict__ n_dev, int shift,
+                                                                  uint32_t* __restrict__ hist) {
     __shared__ uint32_t h[kRadix];
     for (int i = threadIdx.x; i < kRadix; i += blockDim.x) h[i] = 0;
+    resolve_count(n_dev, n, chunk);
     __syncthreads();
     const int start = blockIdx.x * chunk;
     const int end = min(start + chunk, n);
@@ -153,8 +172,10 @@ __global__ void __launch_bounds__(1024) radix_scan_kernel(uint32_t* __restrict__
 
 __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
     const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
-    uint32_t* __restrict__ vout, int n, int chunk, int shift, const uint32_t* __restrict__ offsets) {
+    uint32_t* __restrict__ vout, int n, int chunk, const int64_t* __restrict__ n_dev, int shift,
+    const uint32_t* __restrict__ offsets) {
     __shared__ uint32_t run_off[kRadix];
+    resolve_count(n_dev, n, chunk);
     __shared__ uint32_t tile_tot[kRadix];
     __shared__ uint32_t wcnt[kSortWarps][kRadix];
     const int tid = threadIdx.x, warp = tid >> 5;
@@ -240,14 +261,13 @@ extern "C" size_t gstex_sort_workspace_bytes(int n) {
     return align_up((size_t)n * 8, 256) + align_up((size_t)n * 4, 256) + (size_t)kRadix * p.blocks * 4;
 }
 
-extern "C" int gstex_sort_pairs(int n, int end_bit, const int64_t* keys_in, const int32_t* vals_in,
-                                int64_t* keys_out, int32_t* vals_out, void* ws, size_t ws_bytes, gstex_stream_t s) {
+static int sort_impl(int n, const int64_t* n_dev, int end_bit, const int64_t* keys_in, const int32_t* vals_in,
+                     int64_t* keys_out, int32_t* vals_out, void* ws, size_t ws_bytes, cudaStream_t stream) {
     GSTEX_REQUIRE(n >= 0 && end_bit >= 0 && end_bit <= 64);
     if (n == 0) return GSTEX_OK;
     GSTEX_REQUIRE(keys_in && vals_in && keys_out && vals_out);
-    cudaStream_t stream = (cudaStream_t)s;
     const int passes = ceil_div(end_bit, 8);
-    if (passes == 0 || n == 1) {
+    if (passes == 0 || (n == 1 && !n_dev)) {
         cudaError_t e = cudaMemcpyAsync(keys_out, keys_in, (size_t)n * 8, cudaMemcpyDeviceToDevice, stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(vals_out, vals_in, (size_t)n * 4, cudaMemcpyDeviceToDevice, stream);
         if (e != cudaSuccess) { set_cuda_error(e, "sort_pairs copy"); return GSTEX_ERR_CUDA; }
@@ -270,13 +290,26 @@ extern "C" int gstex_sort_pairs(int n, int end_bit, const int64_t* keys_in, cons
         uint64_t* kdst = to_out ? (uint64_t*)keys_out : kalt;
         uint32_t* vdst = to_out ? (uint32_t*)vals_out : valt;
         const int shift = pass * 8;
-        radix_hist_kernel<<<p.blocks, kSortThreads, 0, stream>>>(ksrc, n, p.chunk, shift, hist);
+        radix_hist_kernel<<<p.blocks, kSortThreads, 0, stream>>>(ksrc, n, p.chunk, n_dev, shift, hist);
         radix_scan_kernel<<<1, 1024, 0, stream>>>(hist, kRadix * p.blocks);
-        radix_scatter_kernel<<<p.blocks, kSortThreads, 0, stream>>>(ksrc, vsrc, kdst, vdst, n, p.chunk, shift, hist);
+        radix_scatter_kernel<<<p.blocks, kSortThreads, 0, stream>>>(ksrc, vsrc, kdst, vdst, n, p.chunk, n_dev, shift,
+                                                                    hist);
         ksrc = kdst;
         vsrc = vdst;
     }
-    return check_launch("sort_pairs");
+    return check_launch("sort_pairs", 3 * passes);
+}
+
+extern "C" int gstex_sort_pairs(int n, int end_bit, const int64_t* keys_in, const int32_t* vals_in,
+                                int64_t* keys_out, int32_t* vals_out, void* ws, size_t ws_bytes, gstex_stream_t s) {
+    return sort_impl(n, nullptr, end_bit, keys_in, vals_in, keys_out, vals_out, ws, ws_bytes, (cudaStream_t)s);
+}
+
+extern "C" int gstex_sort_pairs_dyn(int capacity, const int64_t* count, int end_bit, const int64_t* keys_in,
+                                    const int32_t* vals_in, int64_t* keys_out, int32_t* vals_out, void* ws,
+                                    size_t ws_bytes, gstex_stream_t s) {
+    GSTEX_REQUIRE(count);
+    return sort_impl(capacity, count, end_bit, keys_in, vals_in, keys_out, vals_out, ws, ws_bytes, (cudaStream_t)s);
 }
 
 extern "C" int gstex_get_tile_bin_edges(int num_isect, const int64_t* sorted, int num_tiles, int32_t* bins,
@@ -287,6 +320,19 @@ extern "C" int gstex_get_tile_bin_edges(int num_isect, const int64_t* sorted, in
     if (e != cudaSuccess) { set_cuda_error(e, "tile_bin_edges memset"); return GSTEX_ERR_CUDA; }
     if (num_isect == 0) return GSTEX_OK;
     GSTEX_REQUIRE(sorted);
-    bin_edges_kernel<<<ceil_div(num_isect, 256), 256, 0, stream>>>(num_isect, sorted, num_tiles, (int2*)bins);
+    bin_edges_kernel<<<ceil_div(num_isect, 256), 256, 0, stream>>>(num_isect, nullptr, sorted, num_tiles,
+                                                                    (int2*)bins);
     return check_launch("get_tile_bin_edges");
+}
+
+extern "C" int gstex_get_tile_bin_edges_dyn(int capacity, const int64_t* count, const int64_t* sorted, int num_tiles,
+                                            int32_t* bins, gstex_stream_t s) {
+    GSTEX_REQUIRE(capacity >= 0 && num_tiles > 0 && bins && count);
+    cudaStream_t stream = (cudaStream_t)s;
+    cudaError_t e = cudaMemsetAsync(bins, 0, (size_t)num_tiles * 2 * sizeof(int32_t), stream);
+    if (e != cudaSuccess) { set_cuda_error(e, "tile_bin_edges memset"); return GSTEX_ERR_CUDA; }
+    if (capacity == 0) return GSTEX_OK;
+    GSTEX_REQUIRE(sorted);
+    bin_edges_kernel<<<ceil_div(capacity, 256), 256, 0, stream>>>(capacity, count, sorted, num_tiles, (int2*)bins);
+    return check_launch("get_tile_bin_edges_dyn");
 }

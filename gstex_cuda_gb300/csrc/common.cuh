@@ -22,7 +22,7 @@ constexpr float kDenomEps = 1e-6f;
 constexpr float kBlurFsq = 2.0f;
 
 // Host-side status helpers (defined in status.cu).
-int check_launch(const char* what);
+int check_launch(const char* what, int launches = 1);
 void set_cuda_error(cudaError_t e, const char* what);
 
 #define GSTEX_REQUIRE(cond)                         \

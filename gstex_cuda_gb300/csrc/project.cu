@@ -3,14 +3,9 @@
 // Built with -fmad=false and IEEE division so that the AABB and tile counts
 // are reproducible bit for bit by a CPU restatement of the same operations.
 #include "common.cuh"
+#include "project.cuh"
 
 namespace gstex {
-
-// helpers.cuh:145-152
-__device__ __forceinline__ float2 project_pix(float fx, float fy, float3 p, float cx, float cy) {
-    const float rw = 1.f / (p.z + 1e-6f);
-    return make_float2(p.x * rw * fx + cx, p.y * rw * fy + cy);
-}
 
 // Reference: csrc/get_aabb_2d.cu:11-89
 __global__ void aabb_kernel(int n, const float3* __restrict__ means, const float* __restrict__ scales,
@@ -22,43 +17,11 @@ __global__ void aabb_kernel(int n, const float3* __restrict__ means, const float
     float m[12];
 #pragma unroll
     for (int k = 0; k < 12; k++) m[k] = viewmat[k];
-    auto xf = [&](float3 p) {
-        return make_float3(m[0] * p.x + m[1] * p.y + m[2] * p.z + m[3], m[4] * p.x + m[5] * p.y + m[6] * p.z + m[7],
-                           m[8] * p.x + m[9] * p.y + m[10] * p.z + m[11]);
-    };
-    const float3 p = means[i];
-    const float3 pv = xf(p);
-    const bool clipped = pv.z <= kTNear;
-    const float2 xy = project_pix(fx, fy, pv, cx, cy);
-    const Axes A = quat_axes(quats[i]);
-    const float ell = 3.0f * glob_scale;
-    const float e1 = ell * scales[3 * i], e2 = ell * scales[3 * i + 1];
-    float2 pix[4];
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        const bool s1 = k < 2, s2 = (k % 2) == 0;
-        float3 c;
-        c.x = s1 ? p.x + e1 * A.a1.x : p.x - e1 * A.a1.x;
-        c.x = s2 ? c.x + e2 * A.a2.x : c.x - e2 * A.a2.x;
-        c.y = s1 ? p.y + e1 * A.a1.y : p.y - e1 * A.a1.y;
-        c.y = s2 ? c.y + e2 * A.a2.y : c.y - e2 * A.a2.y;
-        c.z = s1 ? p.z + e1 * A.a1.z : p.z - e1 * A.a1.z;
-        c.z = s2 ? c.z + e2 * A.a2.z : c.z - e2 * A.a2.z;
-        float3 cv = xf(c);
-        cv.z = fmaxf(cv.z, kTNear);
-        pix[k] = project_pix(fx, fy, cv, cx, cy);
-    }
-    const float mxx = fmaxf(fmaxf(pix[0].x, pix[1].x), fmaxf(pix[2].x, pix[3].x));
-    const float mxy = fmaxf(fmaxf(pix[0].y, pix[1].y), fmaxf(pix[2].y, pix[3].y));
-    const float mnx = fminf(fminf(pix[0].x, pix[1].x), fminf(pix[2].x, pix[3].x));
-    const float mny = fminf(fminf(pix[0].y, pix[1].y), fminf(pix[2].y, pix[3].y));
-    if (clipped) {
-        centers[i] = xy;
-        extents[i] = make_float2(0.f, 0.f);
-    } else {
-        centers[i] = make_float2(0.5f * (mxx + mnx), 0.5f * (mxy + mny));
-        extents[i] = make_float2(0.5f * (mxx - mnx), 0.5f * (mxy - mny));
-    }
+    float2 c, e;
+    float z;
+    aabb_2d(m, fx, fy, cx, cy, means[i], quats[i], scales[3 * i], scales[3 * i + 1], glob_scale, c, e, z);
+    centers[i] = c;
+    extents[i] = e;
 }
 
 // gstex_cuda/get_aabb_2d.py:70-91 in float32: floor((c-e)/bw), floor((c+e)/bw + 1),
@@ -67,12 +30,7 @@ __global__ void tiles_hit_kernel(int n, const float2* __restrict__ centers, cons
                                  int tiles_x, int tiles_y, float fbw, int32_t* __restrict__ out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const float2 c = centers[i], e = extents[i];
-    const int x0 = min(max(__float2int_rz(floorf(__fdiv_rn(c.x - e.x, fbw))), 0), tiles_x);
-    const int y0 = min(max(__float2int_rz(floorf(__fdiv_rn(c.y - e.y, fbw))), 0), tiles_y);
-    const int x1 = min(max(__float2int_rz(floorf(__fdiv_rn(c.x + e.x, fbw) + 1.0f)), 0), tiles_x);
-    const int y1 = min(max(__float2int_rz(floorf(__fdiv_rn(c.y + e.y, fbw) + 1.0f)), 0), tiles_y);
-    out[i] = (x1 - x0) * (y1 - y0);
+    out[i] = tiles_hit(centers[i], extents[i], tiles_x, tiles_y, fbw);
 }
 
 // ---------------------------------------------------------------------------
@@ -173,44 +131,6 @@ __global__ void scan_apply(int n, const int32_t* __restrict__ in, const int64_t*
 // ---------------------------------------------------------------------------
 // Spherical harmonics (csrc/sh.cuh:46-253; basis of gstex_cuda/_torch_impl.py:62-113)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ int sh_bases(int deg) { return deg <= 0 ? 1 : deg == 1 ? 4 : deg == 2 ? 9 : deg == 3 ? 16 : 25; }
-
-__device__ __forceinline__ int sh_basis(int deg, float3 dir, float* Y) {
-    Y[0] = 0.28209479177387814f;
-    if (deg < 1) return 1;
-    const float nrm = sqrtf(dir.x * dir.x + dir.y * dir.y + dir.z * dir.z);
-    const float x = dir.x / nrm, y = dir.y / nrm, z = dir.z / nrm;
-    const float xx = x * x, xy = x * y, xz = x * z, yy = y * y, yz = y * z, zz = z * z;
-    Y[1] = -0.4886025119029199f * y;
-    Y[2] = 0.4886025119029199f * z;
-    Y[3] = -0.4886025119029199f * x;
-    if (deg < 2) return 4;
-    Y[4] = 1.0925484305920792f * xy;
-    Y[5] = -1.0925484305920792f * yz;
-    Y[6] = 0.31539156525252005f * (2.f * zz - xx - yy);
-    Y[7] = -1.0925484305920792f * xz;
-    Y[8] = 0.5462742152960396f * (xx - yy);
-    if (deg < 3) return 9;
-    Y[9] = -0.5900435899266435f * y * (3.f * xx - yy);
-    Y[10] = 2.890611442640554f * xy * z;
-    Y[11] = -0.4570457994644658f * y * (4.f * zz - xx - yy);
-    Y[12] = 0.3731763325901154f * z * (2.f * zz - 3.f * xx - 3.f * yy);
-    Y[13] = -0.4570457994644658f * x * (4.f * zz - xx - yy);
-    Y[14] = 1.445305721320277f * z * (xx - yy);
-    Y[15] = -0.5900435899266435f * x * (xx - 3.f * yy);
-    if (deg < 4) return 16;
-    Y[16] = 2.5033429417967046f * xy * (xx - yy);
-    Y[17] = -1.7701307697799304f * yz * (3.f * xx - yy);
-    Y[18] = 0.9461746957575601f * xy * (7.f * zz - 1.f);
-    Y[19] = -0.6690465435572892f * yz * (7.f * zz - 3.f);
-    Y[20] = 0.10578554691520431f * (zz * (35.f * zz - 30.f) + 3.f);
-    Y[21] = -0.6690465435572892f * xz * (7.f * zz - 3.f);
-    Y[22] = 0.47308734787878004f * (xx - yy) * (7.f * zz - 1.f);
-    Y[23] = -1.7701307697799304f * xz * (xx - 3.f * yy);
-    Y[24] = 0.6258357354491761f * (xx * (xx - 3.f * yy) - yy * (3.f * xx - yy));
-    return 25;
-}
-
 __global__ void sh_forward_kernel(int n, int degree, int dtu, const float3* __restrict__ dirs,
                                   const float* __restrict__ coeffs, float* __restrict__ colors) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -294,7 +214,7 @@ extern "C" int gstex_inclusive_scan_i32(int n, const int32_t* counts, int32_t* c
     scan_block_sums<<<nb, kScanThreads, 0, stream>>>(n, counts, sums);
     scan_sums<<<1, 1024, 0, stream>>>(nb, sums, total);
     scan_apply<<<nb, kScanThreads, 0, stream>>>(n, counts, sums, cum);
-    return check_launch("inclusive_scan");
+    return check_launch("inclusive_scan", 3);
 }
 
 extern "C" int gstex_compute_sh_forward(int n, int degree, int degrees_to_use, const float* viewdirs,

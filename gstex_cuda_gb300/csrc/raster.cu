@@ -1,77 +1,31 @@
 // Textured 2D-Gaussian compositor: forward, backward and gradient finalize.
 //
-// Reference: csrc/texture.cu:11-329 (forward), 331-760 (backward).  One CTA
-// per screen tile and one thread per pixel as in the reference; each CTA
-// stages batches of block_size Gaussians of its depth-sorted range into
-// shared memory as camera-space records (common.cuh), so a pixel evaluates a
-// splat with a handful of FMAs instead of the reference's per-pixel
-// quaternion, ray-plane and projection work.
+// Reference: csrc/texture.cu:11-329 (forward), 331-760 (backward).  A CTA of
+// bw x bw threads renders one screen tile, one thread per pixel; it stages
+// batches of bw*bw Gaussians of the tile's depth-sorted range into shared
+// memory as camera-space records (common.cuh), so a pixel evaluates a splat
+// with a handful of FMAs instead of the reference's per-pixel quaternion,
+// ray-plane and projection work.
 //
-// Backward: per (pixel, Gaussian) the adjoint reduces to 26 scalar
-// "moments" whose sums over pixels determine every parameter gradient
-// (because delta = l1*ax1 + l2*ax2 on the splat plane and the quaternion
-// adjoint is linear in dR).  Moments are reduced across a warp with a
-// 31-shuffle transpose reduction, summed per CTA in shared memory, and
-// flushed with one set of vector atomics per (tile, Gaussian).  A finalize
-// kernel turns the per-Gaussian sums into v_means, v_quats, ...
+// Backward: per (pixel, Gaussian) the adjoint reduces to 26 scalar moments
+// whose sums over pixels determine every parameter gradient (on the splat
+// plane delta = l1*ax1 + l2*ax2, and the quaternion adjoint is linear in dR).
+// Moments are reduced across a warp with a 31-shuffle transpose reduction,
+// summed per CTA in shared memory, and flushed with one set of vector atomics
+// per (tile, Gaussian).  A finalize kernel turns the per-Gaussian sums into
+// v_means, v_quats, ...
+//
+// Two launch forms share the per-tile bodies: one CTA per tile of a single
+// view (the reference's texture_forward/backward), and a persistent kernel
+// that pulls tiles of many views from one global queue (batched rendering).
 #include "common.cuh"
+#include "raster.cuh"
 
 namespace gstex {
 
-constexpr int kMoments = 26;       // per-pair moments reduced in the CTA
-constexpr int kMomStride = 28;     // per-Gaussian global stride (24 + 3 blur + pad)
-
-struct RasterArgs {
-    int N, W, H, bw, tiles_x, tiles_y, C, T;
-    const int3* dims;
-    const int32_t* gids;
-    const int2* bins;
-    const float3* colors;
-    const float* opac;
-    const float3* means;
-    const float* scales;
-    float glob;
-    const float4* quats;
-    const float2* uv0;
-    const float3* umap;
-    const float3* vmap;
-    const void* tex;
-    const float* viewmat;
-    float fx, fy, cx, cy;
-    int settings;
-    const float* bg;
-};
-
-struct FwdOut {
-    float3* img;
-    float* depth;
-    float* reg;
-    float* tex;
-    float3* normal;
-    float* final_T;
-    int32_t* final_idx;
-    int32_t* depth_idx;
-    float3* reg_s;
-};
-
-struct BwdArgs {
-    const float* final_T;
-    const int32_t* final_idx;
-    const int32_t* depth_idx;
-    const float3* reg_s;
-    const float3* v_img;
-    const float* v_depth;
-    const float* v_reg;
-    const float* v_alpha;
-    const float* v_tex;
-    const float3* v_normal;
-    float* moments;   // [N, kMomStride]
-    float* v_texgrad; // [T, C] (fp32 texture) or [T, 4] (bf16 texture)
-};
-
-__device__ __forceinline__ void stage(GaussRec& R, const RasterArgs& a, const View& V, int gid) {
+__device__ __forceinline__ void stage(GaussRec& R, const SceneArgs& a, const View& V, const float3* colors, int gid) {
     make_record(R, gid, V, a.means[gid], a.quats[gid], make_float2(a.scales[3 * gid], a.scales[3 * gid + 1]), a.glob,
-                a.opac[gid], a.colors[gid], a.uv0[gid], a.umap[gid], a.vmap[gid], a.dims[gid]);
+                a.opac[gid], colors[gid], a.uv0[gid], a.umap[gid], a.vmap[gid], a.dims[gid]);
 }
 
 // All channels of the 4 bilinear corners (C == 3 fast path).
@@ -101,22 +55,19 @@ __device__ __forceinline__ void fetch3(const void* tex, const Bilerp& B, float c
 }
 
 // ---------------------------------------------------------------------------
-// Forward
+// Forward body: one tile
 // ---------------------------------------------------------------------------
 template <int TEXMODE, int CT>
-__global__ void __launch_bounds__(256) fwd_kernel(RasterArgs a, FwdOut o) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    GaussRec* recs = reinterpret_cast<GaussRec*>(smem);
+__device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, const FwdOut& o, GaussRec* recs) {
     const int bs = blockDim.x * blockDim.y;
     const int tr = threadIdx.y * blockDim.x + threadIdx.x;
-    const int tile = blockIdx.y * a.tiles_x + blockIdx.x;
-    const int pi = blockIdx.y * blockDim.y + threadIdx.y;
-    const int pj = blockIdx.x * blockDim.x + threadIdx.x;
-    const View V = load_view(a.viewmat, a.fx, a.fy, a.cx, a.cy);
+    const int pi = J.ty * blockDim.y + threadIdx.y;
+    const int pj = J.tx * blockDim.x + threadIdx.x;
+    const View& V = J.V;
     const PixelRay P = make_pixel(V, pi, pj);
-    const bool inside = pi < a.H && pj < a.W;
+    const bool inside = pi < J.H && pj < J.W;
     bool done = !inside;
-    const int2 range = a.bins[tile];
+    const int2 range = J.range;
     const int nb = ceil_div(range.y - range.x, bs);
     const bool use_blur = a.settings & (1 << 9);
     const bool use_ndc = a.settings & (1 << 10);
@@ -136,7 +87,7 @@ __global__ void __launch_bounds__(256) fwd_kernel(RasterArgs a, FwdOut o) {
         if (__syncthreads_count(done) >= bs) break;
         const int bstart = range.x + bs * b;
         const int idx = bstart + tr;
-        if (idx < range.y) stage(recs[tr], a, V, a.gids[idx]);
+        if (idx < range.y) stage(recs[tr], a, V, J.colors, a.gids[idx]);
         __syncthreads();
         const int bsize = min(bs, range.y - bstart);
         if (done) continue;
@@ -192,7 +143,7 @@ __global__ void __launch_bounds__(256) fwd_kernel(RasterArgs a, FwdOut o) {
         }
     }
     if (inside) {
-        const int pix = pi * a.W + pj;
+        const size_t pix = J.pix_base + (size_t)pi * J.W + pj;
         o.final_T[pix] = T;
         o.final_idx[pix] = cur;
         o.depth_idx[pix] = didx;
@@ -201,12 +152,12 @@ __global__ void __launch_bounds__(256) fwd_kernel(RasterArgs a, FwdOut o) {
         o.depth[pix] = depth;
         o.reg[pix] = reg;
         o.reg_s[pix] = ts;
-        for (int ch = 0; ch < C; ch++) o.tex[(size_t)pix * C + ch] = otex[ch];
+        for (int ch = 0; ch < C; ch++) o.tex[pix * C + ch] = otex[ch];
     }
 }
 
 // ---------------------------------------------------------------------------
-// Backward
+// Backward body: one tile
 // ---------------------------------------------------------------------------
 // Transpose reduction: lane l ends with the warp sum of m[l].
 __device__ __forceinline__ float warp_transpose_reduce(float (&m)[32], unsigned lane) {
@@ -223,52 +174,55 @@ __device__ __forceinline__ float warp_transpose_reduce(float (&m)[32], unsigned 
     return m[0];
 }
 
+template <typename T>
+__device__ __forceinline__ T ld_or(const T* p, size_t i, T z) {
+    return p ? p[i] : z;
+}
+
 template <int TEXMODE, int CT>
-__global__ void __launch_bounds__(256) bwd_kernel(RasterArgs a, BwdArgs g) {
-    extern __shared__ __align__(16) unsigned char smem[];
+__device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, const BwdArgs& g, GaussRec* recs,
+                                         float* smom) {
     const int bs = blockDim.x * blockDim.y;
-    GaussRec* recs = reinterpret_cast<GaussRec*>(smem);
-    float* smom = reinterpret_cast<float*>(smem + sizeof(GaussRec) * bs);
     const int tr = threadIdx.y * blockDim.x + threadIdx.x;
     const unsigned lane = tr & 31;
     const unsigned wmask = __activemask();
     const bool full_warp = wmask == 0xffffffffu;
-    const int tile = blockIdx.y * a.tiles_x + blockIdx.x;
-    const int pi = blockIdx.y * blockDim.y + threadIdx.y;
-    const int pj = blockIdx.x * blockDim.x + threadIdx.x;
-    const View V = load_view(a.viewmat, a.fx, a.fy, a.cx, a.cy);
+    const int pi = J.ty * blockDim.y + threadIdx.y;
+    const int pj = J.tx * blockDim.x + threadIdx.x;
+    const View& V = J.V;
     const PixelRay P = make_pixel(V, pi, pj);
-    const bool inside = pi < a.H && pj < a.W;
-    const int pix = inside ? pi * a.W + pj : 0;
+    const bool inside = pi < J.H && pj < J.W;
+    const size_t pix = inside ? J.pix_base + (size_t)pi * J.W + pj : 0;
     const bool use_blur = a.settings & (1 << 9);
     const bool use_ndc = a.settings & (1 << 10);
     const bool prop_uv = a.settings & (1 << 8);
     const bool bilinear = !(a.settings & (1 << 2));
     const int C = CT >= 0 ? CT : a.C;
     constexpr int CA = CT > 0 ? CT : (CT == 0 ? 1 : kMaxChannels);
+    const float3 z3 = make_float3(0.f, 0.f, 0.f);
 
     float T = inside ? g.final_T[pix] : 1.f;
-    const float3 sfin = inside ? g.reg_s[pix] : make_float3(0.f, 0.f, 0.f);
+    const float3 sfin = inside ? g.reg_s[pix] : z3;
     const int dfin = inside ? g.depth_idx[pix] : -1;
     const int bfin = inside ? g.final_idx[pix] : 0;
-    const float3 vout = inside ? g.v_img[pix] : make_float3(0.f, 0.f, 0.f);
-    const float vdepth = inside ? g.v_depth[pix] : 0.f;
-    const float vreg = inside ? g.v_reg[pix] : 0.f;
-    const float valph = inside ? g.v_alpha[pix] : 0.f;
-    const float3 vnorm = inside ? g.v_normal[pix] : make_float3(0.f, 0.f, 0.f);
+    const float3 vout = inside ? ld_or(g.v_img, pix, z3) : z3;
+    const float vdepth = inside ? ld_or(g.v_depth, pix, 0.f) : 0.f;
+    const float vreg = inside ? ld_or(g.v_reg, pix, 0.f) : 0.f;
+    const float valph = inside ? ld_or(g.v_alpha, pix, 0.f) : 0.f;
+    const float3 vnorm = inside ? ld_or(g.v_normal, pix, z3) : z3;
     float vtex[CA];
-    for (int ch = 0; ch < CA; ch++) vtex[ch] = (inside && ch < C) ? g.v_tex[(size_t)pix * C + ch] : 0.f;
+    for (int ch = 0; ch < CA; ch++) vtex[ch] = (inside && ch < C && g.v_tex) ? g.v_tex[pix * C + ch] : 0.f;
     float vT_run = a.bg[0] * vout.x + a.bg[1] * vout.y + a.bg[2] * vout.z - valph;
     const int warp_bfin = __reduce_max_sync(wmask, bfin);
 
-    const int2 range = a.bins[tile];
+    const int2 range = J.range;
     const int nb = ceil_div(range.y - range.x, bs);
     for (int b = 0; b < nb; ++b) {
         __syncthreads();
         const int bend = range.y - 1 - bs * b;
         const int bsize = min(bs, bend + 1 - range.x);
         const int idx = bend - tr;
-        if (idx >= range.x) stage(recs[tr], a, V, a.gids[idx]);
+        if (idx >= range.x) stage(recs[tr], a, V, J.colors, a.gids[idx]);
         for (int q = tr; q < bs * kMoments; q += bs) smom[q] = 0.f;
         __syncthreads();
         for (int k = max(0, bend - warp_bfin); k < bsize; ++k) {
@@ -319,19 +273,21 @@ __global__ void __launch_bounds__(256) bwd_kernel(RasterArgs a, BwdArgs g) {
                             }
                             v_vis += val * vtex[ch];
                         }
-                        const int rows[4] = { B.i00, B.i01, B.i10, B.i11 };
-                        const float wts[4] = { B.w00, B.w01, B.w10, B.w11 };
+                        if (gv[0] != 0.f || gv[1] != 0.f || gv[2] != 0.f) {
+                            const int rows[4] = { B.i00, B.i01, B.i10, B.i11 };
+                            const float wts[4] = { B.w00, B.w01, B.w10, B.w11 };
 #pragma unroll
-                        for (int q = 0; q < 4; q++) {
-                            if (wts[q] == 0.f) continue;
-                            if (TEXMODE == 1) {
-                                atomicAdd(reinterpret_cast<float4*>(g.v_texgrad) + rows[q],
-                                          make_float4(wts[q] * gv[0], wts[q] * gv[1], wts[q] * gv[2], 0.f));
-                            } else {
-                                float* dst = g.v_texgrad + 3 * (size_t)rows[q];
-                                atomicAdd(dst + 0, wts[q] * gv[0]);
-                                atomicAdd(dst + 1, wts[q] * gv[1]);
-                                atomicAdd(dst + 2, wts[q] * gv[2]);
+                            for (int q = 0; q < 4; q++) {
+                                if (wts[q] == 0.f) continue;
+                                if (TEXMODE == 1) {
+                                    atomicAdd(reinterpret_cast<float4*>(g.v_texgrad) + rows[q],
+                                              make_float4(wts[q] * gv[0], wts[q] * gv[1], wts[q] * gv[2], 0.f));
+                                } else {
+                                    float* dst = g.v_texgrad + 3 * (size_t)rows[q];
+                                    atomicAdd(dst + 0, wts[q] * gv[0]);
+                                    atomicAdd(dst + 1, wts[q] * gv[1]);
+                                    atomicAdd(dst + 2, wts[q] * gv[2]);
+                                }
                             }
                         }
                     } else if (CT != 0) {
@@ -341,10 +297,12 @@ __global__ void __launch_bounds__(256) bwd_kernel(RasterArgs a, BwdArgs g) {
                             const float c10 = __ldg(t + (size_t)B.i10 * C + ch), c11 = __ldg(t + (size_t)B.i11 * C + ch);
                             const float val = B.w00 * c00 + B.w01 * c01 + B.w10 * c10 + B.w11 * c11;
                             const float vv = vis * vtex[ch];
-                            if (B.w00 != 0.f) atomicAdd(g.v_texgrad + (size_t)B.i00 * C + ch, B.w00 * vv);
-                            if (B.w01 != 0.f) atomicAdd(g.v_texgrad + (size_t)B.i01 * C + ch, B.w01 * vv);
-                            if (B.w10 != 0.f) atomicAdd(g.v_texgrad + (size_t)B.i10 * C + ch, B.w10 * vv);
-                            if (B.w11 != 0.f) atomicAdd(g.v_texgrad + (size_t)B.i11 * C + ch, B.w11 * vv);
+                            if (vv != 0.f) {
+                                if (B.w00 != 0.f) atomicAdd(g.v_texgrad + (size_t)B.i00 * C + ch, B.w00 * vv);
+                                if (B.w01 != 0.f) atomicAdd(g.v_texgrad + (size_t)B.i01 * C + ch, B.w01 * vv);
+                                if (B.w10 != 0.f) atomicAdd(g.v_texgrad + (size_t)B.i10 * C + ch, B.w10 * vv);
+                                if (B.w11 != 0.f) atomicAdd(g.v_texgrad + (size_t)B.i11 * C + ch, B.w11 * vv);
+                            }
                             if (bilinear && prop_uv) {
                                 v_u += (float)R.h * (vv * (-(1.f - B.fy) * c00 - B.fy * c01 + (1.f - B.fy) * c10 + B.fy * c11));
                                 v_v += (float)R.w * (vv * (-(1.f - B.fx) * c00 + (1.f - B.fx) * c01 - B.fx * c10 + B.fx * c11));
@@ -429,17 +387,20 @@ __global__ void __launch_bounds__(256) bwd_kernel(RasterArgs a, BwdArgs g) {
             for (int q = 0; q < kMoments; q++) any |= sm[q] != 0.f;
             if (any) {
                 const GaussRec& R = recs[tr];
+                float* vc = J.vcolors + 3 * (size_t)R.gid;
+                atomicAdd(vc + 0, sm[0]);
+                atomicAdd(vc + 1, sm[1]);
+                atomicAdd(vc + 2, sm[2]);
                 float4* dst = reinterpret_cast<float4*>(g.moments + (size_t)R.gid * kMomStride);
                 // blur moments -> world-space mean gradient (helpers.cuh:155-164, 114-121)
                 const float3 p = R.mu_c;
                 const float rw = 1.f / (p.z + 1e-6f);
-                const float vx = a.fx * sm[24], vy = a.fy * sm[25];
-                const float3 vview = make_float3(vx * rw, vy * rw, -(vx * p.x + vy * p.y) * rw * rw);
-                const float3 vmb = V.rot_t(vview);
+                const float vx = V.fx * sm[24], vy = V.fy * sm[25];
+                const float3 vmb = V.rot_t(make_float3(vx * rw, vy * rw, -(vx * p.x + vy * p.y) * rw * rw));
                 float v[kMomStride];
 #pragma unroll
-                for (int q = 0; q < 24; q++) v[q] = sm[q];
-                v[24] = vmb.x; v[25] = vmb.y; v[26] = vmb.z; v[27] = 0.f;
+                for (int q = 0; q < 21; q++) v[q] = sm[3 + q];
+                v[21] = vmb.x; v[22] = vmb.y; v[23] = vmb.z;
 #pragma unroll
                 for (int q = 0; q < kMomStride / 4; q++)
                     atomicAdd(dst + q, make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]));
@@ -448,11 +409,85 @@ __global__ void __launch_bounds__(256) bwd_kernel(RasterArgs a, BwdArgs g) {
     }
 }
 
-// Moments -> parameter gradients (one thread per Gaussian).
+// ---------------------------------------------------------------------------
+// Launch forms
+// ---------------------------------------------------------------------------
+template <int TEXMODE, int CT>
+__global__ void __launch_bounds__(256) fwd_view_kernel(SceneArgs a, ViewArgs va, FwdOut o) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    TileJob J;
+    J.V = load_view(va.viewmat, va.fx, va.fy, va.cx, va.cy);
+    J.W = va.W; J.H = va.H;
+    J.tx = blockIdx.x; J.ty = blockIdx.y;
+    J.range = va.bins[blockIdx.y * va.tiles_x + blockIdx.x];
+    J.pix_base = 0;
+    J.colors = va.colors;
+    J.vcolors = nullptr;
+    fwd_tile<TEXMODE, CT>(a, J, o, reinterpret_cast<GaussRec*>(smem));
+}
+
+template <int TEXMODE, int CT>
+__global__ void __launch_bounds__(256) bwd_view_kernel(SceneArgs a, ViewArgs va, BwdArgs g) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int bs = blockDim.x * blockDim.y;
+    TileJob J;
+    J.V = load_view(va.viewmat, va.fx, va.fy, va.cx, va.cy);
+    J.W = va.W; J.H = va.H;
+    J.tx = blockIdx.x; J.ty = blockIdx.y;
+    J.range = va.bins[blockIdx.y * va.tiles_x + blockIdx.x];
+    J.pix_base = 0;
+    J.colors = va.colors;
+    J.vcolors = va.vcolors;
+    bwd_tile<TEXMODE, CT>(a, J, g, reinterpret_cast<GaussRec*>(smem),
+                          reinterpret_cast<float*>(smem + sizeof(GaussRec) * bs));
+}
+
+__device__ __forceinline__ bool next_job(const BatchArgs& ba, int* s_tile, TileJob& J) {
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) *s_tile = atomicAdd(ba.queue, 1);
+    __syncthreads();
+    int t = *s_tile;
+    if (t >= ba.total_tiles) return false;
+    if (ba.order) t = ba.order[t];
+    const int v = ba.tile_view[t];
+    const BatchView& bv = ba.views[v];
+    J.V = bv.V;
+    J.W = bv.W; J.H = bv.H;
+    const int local = t - bv.tile_offset;
+    J.ty = local / bv.tiles_x;
+    J.tx = local - J.ty * bv.tiles_x;
+    J.range = ba.bins[t];
+    J.pix_base = bv.pix_offset;
+    J.colors = ba.colors + (size_t)v * ba.num_points;
+    J.vcolors = ba.vcolors ? ba.vcolors + (size_t)v * ba.num_points * 3 : nullptr;
+    return true;
+}
+
+template <int TEXMODE, int CT>
+__global__ void __launch_bounds__(256) fwd_batch_kernel(SceneArgs a, BatchArgs ba, FwdOut o) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int s_tile;
+    TileJob J;
+    while (next_job(ba, &s_tile, J)) fwd_tile<TEXMODE, CT>(a, J, o, reinterpret_cast<GaussRec*>(smem));
+}
+
+template <int TEXMODE, int CT>
+__global__ void __launch_bounds__(256) bwd_batch_kernel(SceneArgs a, BatchArgs ba, BwdArgs g) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int s_tile;
+    const int bs = blockDim.x * blockDim.y;
+    TileJob J;
+    while (next_job(ba, &s_tile, J))
+        bwd_tile<TEXMODE, CT>(a, J, g, reinterpret_cast<GaussRec*>(smem),
+                              reinterpret_cast<float*>(smem + sizeof(GaussRec) * bs));
+}
+
+// Moments -> parameter gradients (one thread per Gaussian).  Colour gradients
+// are written by the tile flushes directly.
 __global__ void finalize_kernel(int N, const float* __restrict__ mom, const float4* __restrict__ quats,
-                                const float3* __restrict__ umap, const float3* __restrict__ vmap, float3* v_colors,
-                                float* v_opac, float3* v_means, float3* v_scales, float4* v_quats, float2* v_uv0,
-                                float3* v_umap, float3* v_vmap) {
+                                const float3* __restrict__ umap, const float3* __restrict__ vmap, float* v_opac,
+                                float3* v_means, float3* v_scales, float4* v_quats, float2* v_uv0, float3* v_umap,
+                                float3* v_vmap) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     float M[kMomStride];
@@ -462,32 +497,33 @@ __global__ void finalize_kernel(int N, const float* __restrict__ mom, const floa
         const float4 v = src[q];
         M[4 * q] = v.x; M[4 * q + 1] = v.y; M[4 * q + 2] = v.z; M[4 * q + 3] = v.w;
     }
+    // M: 0 v_opac, 1-2 v_scale, 3-4 sum v_l, 5 sum v_t/(n.r), 6-9 S_lk v_lj, 10-11 S_l v_t/(n.r),
+    //    12-14 sum vis*v_normal, 15-16 sum v_uv, 17-20 S_l v_uv, 21-23 blur mean gradient
     const float4 q = quats[i];
     const Axes A = quat_axes(q);
     const float3 um = umap[i], vm = vmap[i];
-    v_colors[i] = make_float3(M[0], M[1], M[2]);
-    v_opac[i] = M[3];
-    v_scales[i] = make_float3(M[4], M[5], 0.f);
-    v_uv0[i] = make_float2(M[18], M[19]);
-    v_umap[i] = M[20] * A.a1 + M[21] * A.a2;
-    v_vmap[i] = M[22] * A.a1 + M[23] * A.a2;
-    const float3 vdiff = M[18] * um + M[19] * vm;
-    float3 vm_ = (M[8] * A.a3) - (M[6] * A.a1 + M[7] * A.a2) - vdiff;
-    v_means[i] = vm_ + make_float3(M[24], M[25], M[26]);
-    const float3 c0 = M[9] * A.a1 + M[10] * A.a2;
-    const float3 c1 = M[11] * A.a1 + M[12] * A.a2;
-    const float3 c2 = make_float3(M[15], M[16], M[17]) - (M[13] * A.a1 + M[14] * A.a2);
+    v_opac[i] = M[0];
+    v_scales[i] = make_float3(M[1], M[2], 0.f);
+    v_uv0[i] = make_float2(M[15], M[16]);
+    v_umap[i] = M[17] * A.a1 + M[18] * A.a2;
+    v_vmap[i] = M[19] * A.a1 + M[20] * A.a2;
+    const float3 vdiff = M[15] * um + M[16] * vm;
+    const float3 vmean = (M[5] * A.a3) - (M[3] * A.a1 + M[4] * A.a2) - vdiff;
+    v_means[i] = vmean + make_float3(M[21], M[22], M[23]);
+    const float3 c0 = M[6] * A.a1 + M[7] * A.a2;
+    const float3 c1 = M[8] * A.a1 + M[9] * A.a2;
+    const float3 c2 = make_float3(M[12], M[13], M[14]) - (M[10] * A.a1 + M[11] * A.a2);
     v_quats[i] = quat_axes_vjp(q, c0, c1, c2);
 }
 
 template <typename K>
-static int launch_raster(K kernel, dim3 grid, dim3 block, size_t smem, cudaStream_t stream, const char* what) {
+static int set_smem(K kernel, size_t smem, const char* what) {
     cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) { set_cuda_error(e, what); return GSTEX_ERR_CUDA; }
     return GSTEX_OK;
 }
 
-static int fill_args(const gstex_raster_inputs* in, RasterArgs& a) {
+int fill_scene(const gstex_raster_inputs* in, SceneArgs& a) {
     GSTEX_REQUIRE(in);
     GSTEX_REQUIRE(in->num_points >= 0 && in->img_width > 0 && in->img_height > 0);
     GSTEX_REQUIRE(in->block_width >= 2 && in->block_width <= kMaxBlockWidth);
@@ -502,31 +538,83 @@ static int fill_args(const gstex_raster_inputs* in, RasterArgs& a) {
                       in->uv0 && in->umap && in->vmap);
     if (in->channels > 0 && in->num_points > 0) GSTEX_REQUIRE(in->texture);
     a.N = in->num_points;
-    a.W = in->img_width;
-    a.H = in->img_height;
-    a.bw = in->block_width;
-    a.tiles_x = ceil_div(a.W, a.bw);
-    a.tiles_y = ceil_div(a.H, a.bw);
     a.C = in->channels;
     a.T = in->num_texels;
     a.dims = (const int3*)in->texture_dims;
     a.gids = in->gaussian_ids_sorted;
-    a.bins = (const int2*)in->tile_bins;
-    a.colors = (const float3*)in->colors;
-    a.opac = in->opacities;
     a.means = (const float3*)in->means;
     a.scales = in->scales;
     a.glob = in->glob_scale;
     a.quats = (const float4*)in->quats;
+    a.opac = in->opacities;
     a.uv0 = (const float2*)in->uv0;
     a.umap = (const float3*)in->umap;
     a.vmap = (const float3*)in->vmap;
     a.tex = in->texture;
-    a.viewmat = in->viewmat;
-    a.fx = in->fx; a.fy = in->fy; a.cx = in->cx; a.cy = in->cy;
     a.settings = in->settings;
     a.bg = in->background;
     return GSTEX_OK;
+}
+
+// Kernel tables ------------------------------------------------------------
+template <template <int, int> class Sel>
+static typename Sel<0, 0>::type pick(int C, int texmode) {
+    if (C == 0) return Sel<0, 0>::get();
+    if (C == 3) return texmode == 1 ? Sel<1, 3>::get() : Sel<0, 3>::get();
+    return Sel<0, -1>::get();
+}
+template <int M, int C> struct FwdView { typedef void (*type)(SceneArgs, ViewArgs, FwdOut); static type get() { return fwd_view_kernel<M, C>; } };
+template <int M, int C> struct BwdView { typedef void (*type)(SceneArgs, ViewArgs, BwdArgs); static type get() { return bwd_view_kernel<M, C>; } };
+template <int M, int C> struct FwdBatch { typedef void (*type)(SceneArgs, BatchArgs, FwdOut); static type get() { return fwd_batch_kernel<M, C>; } };
+template <int M, int C> struct BwdBatch { typedef void (*type)(SceneArgs, BatchArgs, BwdArgs); static type get() { return bwd_batch_kernel<M, C>; } };
+
+size_t fwd_smem(int bw) { return sizeof(GaussRec) * bw * bw; }
+size_t bwd_smem(int bw) { return (sizeof(GaussRec) + kMoments * sizeof(float)) * bw * bw; }
+
+int launch_finalize(const SceneArgs& a, const float* moments, float* v_opac, float* v_means, float* v_scales,
+                    float* v_quats, float* v_uv0, float* v_umap, float* v_vmap, cudaStream_t stream) {
+    if (a.N == 0) return GSTEX_OK;
+    finalize_kernel<<<ceil_div(a.N, 256), 256, 0, stream>>>(a.N, moments, a.quats, a.umap, a.vmap, v_opac,
+                                                           (float3*)v_means, (float3*)v_scales, (float4*)v_quats,
+                                                           (float2*)v_uv0, (float3*)v_umap, (float3*)v_vmap);
+    return check_launch("finalize");
+}
+
+int launch_fwd_batch(const SceneArgs& a, const BatchArgs& ba, const FwdOut& o, int bw, int texmode, int grid,
+                     cudaStream_t stream) {
+    auto k = pick<FwdBatch>(a.C, texmode);
+    int rc = set_smem(k, fwd_smem(bw), "batch forward");
+    if (rc) return rc;
+    k<<<grid, dim3(bw, bw), fwd_smem(bw), stream>>>(a, ba, o);
+    return check_launch("batch forward");
+}
+
+int launch_bwd_batch(const SceneArgs& a, const BatchArgs& ba, const BwdArgs& g, int bw, int texmode, int grid,
+                     cudaStream_t stream) {
+    auto k = pick<BwdBatch>(a.C, texmode);
+    int rc = set_smem(k, bwd_smem(bw), "batch backward");
+    if (rc) return rc;
+    k<<<grid, dim3(bw, bw), bwd_smem(bw), stream>>>(a, ba, g);
+    return check_launch("batch backward");
+}
+
+int resident_ctas(int bw, bool backward, int texmode, int C) {
+    int n = 0;
+    cudaError_t e;
+    if (backward) {
+        auto k = pick<BwdBatch>(C, texmode);
+        if (set_smem(k, bwd_smem(bw), "occupancy")) return 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, bw * bw, bwd_smem(bw));
+    } else {
+        auto k = pick<FwdBatch>(C, texmode);
+        if (set_smem(k, fwd_smem(bw), "occupancy")) return 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, bw * bw, fwd_smem(bw));
+    }
+    if (e != cudaSuccess) return 0;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return n * sms;
 }
 
 }  // namespace gstex
@@ -535,23 +623,28 @@ using namespace gstex;
 
 extern "C" int gstex_texture_forward(const gstex_raster_inputs* in, const gstex_forward_outputs* out,
                                      gstex_stream_t s) {
-    RasterArgs a;
-    int rc = fill_args(in, a);
+    SceneArgs a;
+    int rc = fill_scene(in, a);
     if (rc) return rc;
     GSTEX_REQUIRE(out && out->img && out->depth && out->reg && out->normal && out->final_T && out->final_idx &&
                   out->depth_idx && out->reg_s);
     if (a.C > 0) GSTEX_REQUIRE(out->texture);
     FwdOut o{ (float3*)out->img, out->depth, out->reg, out->texture, (float3*)out->normal, out->final_T,
               out->final_idx, out->depth_idx, (float3*)out->reg_s };
+    const int bw = in->block_width;
+    ViewArgs va;
+    va.viewmat = in->viewmat;
+    va.fx = in->fx; va.fy = in->fy; va.cx = in->cx; va.cy = in->cy;
+    va.W = in->img_width; va.H = in->img_height;
+    va.tiles_x = ceil_div(va.W, bw);
+    va.bins = (const int2*)in->tile_bins;
+    va.colors = (const float3*)in->colors;
+    va.vcolors = nullptr;
     cudaStream_t stream = (cudaStream_t)s;
-    const dim3 grid(a.tiles_x, a.tiles_y), block(a.bw, a.bw);
-    const size_t smem = sizeof(GaussRec) * a.bw * a.bw;
-    void (*k)(RasterArgs, FwdOut);
-    if (a.C == 0) k = fwd_kernel<0, 0>;
-    else if (a.C == 3) k = in->texture_dtype == 1 ? fwd_kernel<1, 3> : fwd_kernel<0, 3>;
-    else k = fwd_kernel<0, -1>;
-    if ((rc = launch_raster(k, grid, block, smem, stream, "texture_forward"))) return rc;
-    k<<<grid, block, smem, stream>>>(a, o);
+    const dim3 grid(va.tiles_x, ceil_div(va.H, bw)), block(bw, bw);
+    auto k = pick<FwdView>(a.C, in->texture_dtype);
+    if ((rc = set_smem(k, fwd_smem(bw), "texture_forward"))) return rc;
+    k<<<grid, block, fwd_smem(bw), stream>>>(a, va, o);
     return check_launch("texture_forward");
 }
 
@@ -560,8 +653,8 @@ extern "C" size_t gstex_backward_workspace_bytes(int num_points) {
 }
 
 extern "C" int gstex_texture_backward(const gstex_raster_inputs* in, const gstex_backward_io* io, gstex_stream_t s) {
-    RasterArgs a;
-    int rc = fill_args(in, a);
+    SceneArgs a;
+    int rc = fill_scene(in, a);
     if (rc) return rc;
     GSTEX_REQUIRE(io && io->final_T && io->final_idx && io->depth_idx && io->reg_s && io->v_img && io->v_depth &&
                   io->v_reg && io->v_alpha && io->v_normal);
@@ -572,22 +665,25 @@ extern "C" int gstex_texture_backward(const gstex_raster_inputs* in, const gstex
     if (a.N == 0) return GSTEX_OK;
     cudaStream_t stream = (cudaStream_t)s;
     cudaError_t e = cudaMemsetAsync(io->workspace, 0, gstex_backward_workspace_bytes(a.N), stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(io->v_colors, 0, (size_t)a.N * 3 * sizeof(float), stream);
     if (e != cudaSuccess) { set_cuda_error(e, "texture_backward memset"); return GSTEX_ERR_CUDA; }
     BwdArgs g{ io->final_T, io->final_idx, io->depth_idx, (const float3*)io->reg_s, (const float3*)io->v_img,
                io->v_depth, io->v_reg, io->v_alpha, io->v_texture, (const float3*)io->v_normal,
                (float*)io->workspace, io->v_tex_grad };
-    const dim3 grid(a.tiles_x, a.tiles_y), block(a.bw, a.bw);
-    const size_t smem = (sizeof(GaussRec) + kMoments * sizeof(float)) * a.bw * a.bw;
-    void (*k)(RasterArgs, BwdArgs);
-    if (a.C == 0) k = bwd_kernel<0, 0>;
-    else if (a.C == 3) k = in->texture_dtype == 1 ? bwd_kernel<1, 3> : bwd_kernel<0, 3>;
-    else k = bwd_kernel<0, -1>;
-    if ((rc = launch_raster(k, grid, block, smem, stream, "texture_backward"))) return rc;
-    k<<<grid, block, smem, stream>>>(a, g);
+    const int bw = in->block_width;
+    ViewArgs va;
+    va.viewmat = in->viewmat;
+    va.fx = in->fx; va.fy = in->fy; va.cx = in->cx; va.cy = in->cy;
+    va.W = in->img_width; va.H = in->img_height;
+    va.tiles_x = ceil_div(va.W, bw);
+    va.bins = (const int2*)in->tile_bins;
+    va.colors = (const float3*)in->colors;
+    va.vcolors = io->v_colors;
+    const dim3 grid(va.tiles_x, ceil_div(va.H, bw)), block(bw, bw);
+    auto k = pick<BwdView>(a.C, in->texture_dtype);
+    if ((rc = set_smem(k, bwd_smem(bw), "texture_backward"))) return rc;
+    k<<<grid, block, bwd_smem(bw), stream>>>(a, va, g);
     if ((rc = check_launch("texture_backward"))) return rc;
-    finalize_kernel<<<ceil_div(a.N, 256), 256, 0, stream>>>(
-        a.N, (const float*)io->workspace, a.quats, a.umap, a.vmap, (float3*)io->v_colors, io->v_opacity,
-        (float3*)io->v_means, (float3*)io->v_scales, (float4*)io->v_quats, (float2*)io->v_uv0, (float3*)io->v_umap,
-        (float3*)io->v_vmap);
-    return check_launch("texture_backward finalize");
+    return launch_finalize(a, (const float*)io->workspace, io->v_opacity, io->v_means, io->v_scales, io->v_quats,
+                           io->v_uv0, io->v_umap, io->v_vmap, stream);
 }

@@ -39,6 +39,8 @@ const char* gstex_status_string(int status);
 const char* gstex_last_cuda_error(void);
 /* Library version, e.g. "0.1.0". */
 const char* gstex_version(void);
+/* Number of kernels this library has launched since it was loaded. */
+unsigned long long gstex_launch_count(void);
 
 /* ---------------------------------------------------------------------
  * Projection
@@ -95,10 +97,21 @@ size_t gstex_sort_workspace_bytes(int n);
 int gstex_sort_pairs(int n, int end_bit, const int64_t* keys_in, const int32_t* vals_in, int64_t* keys_out,
                      int32_t* vals_out, void* workspace, size_t workspace_bytes, gstex_stream_t stream);
 
+/* Same sort with the number of items read from device memory (*count,
+ * clamped to capacity): the launch shape depends only on capacity, so the
+ * call can be captured in a CUDA graph.  Workspace:
+ * gstex_sort_workspace_bytes(capacity).  Batched form of utils.py:159-160. */
+int gstex_sort_pairs_dyn(int capacity, const int64_t* count, int end_bit, const int64_t* keys_in,
+                         const int32_t* vals_in, int64_t* keys_out, int32_t* vals_out, void* workspace,
+                         size_t workspace_bytes, gstex_stream_t stream);
+
 /* Per-tile [start, end) ranges of a sorted key list (zero for empty tiles).
  * Replaces _C.get_tile_bin_edges (csrc/bindings.cu:123-140, forward.cu:76-98). */
 int gstex_get_tile_bin_edges(int num_intersects, const int64_t* isect_ids_sorted, int num_tiles,
                              int32_t* tile_bins, gstex_stream_t stream);
+/* Same with the key count read from device memory (clamped to capacity). */
+int gstex_get_tile_bin_edges_dyn(int capacity, const int64_t* count, const int64_t* isect_ids_sorted,
+                                 int num_tiles, int32_t* tile_bins, gstex_stream_t stream);
 
 /* ---------------------------------------------------------------------
  * Textured compositor (texture_forward / texture_backward)
@@ -194,6 +207,98 @@ int gstex_texture_sample_forward(int nq, int channels, const int32_t* texture_di
 int gstex_texture_sample_backward(int nq, int channels, const int32_t* texture_dims, const float* uvs,
                                   const float* texture, const float* v_out, float* v_texture, float* v_uvs,
                                   gstex_stream_t stream);
+
+/* ---------------------------------------------------------------------
+ * Batched multi-view rendering.  The reference renders one view per call
+ * (gstex_cuda/texture.py:14-150, called once per camera by its trainer);
+ * these entry points render many views of one scene with one launch per
+ * stage and no size read back to the host, so a whole forward + backward
+ * step can be captured in a CUDA graph.  Global tiles and pixels of all
+ * views are numbered view by view.
+ * ------------------------------------------------------------------- */
+typedef struct gstex_view_desc {
+    float viewmat[16]; /* world->camera, row-major */
+    float fx, fy, cx, cy;
+    int width, height;
+} gstex_view_desc;
+
+/* Total tiles and pixels of a set of views (host only). */
+int gstex_batch_layout(int num_views, const gstex_view_desc* views, int block_width, int* total_tiles,
+                       long long* total_pixels);
+/* Bytes of the device view table written by gstex_batch_prepare. */
+size_t gstex_batch_views_bytes(int num_views);
+/* Writes the device view table, the view of every global tile
+ * (tile_view [total_tiles]) and the pixel offsets of the views
+ * (pix_offsets [num_views + 1]); synchronises the stream. */
+int gstex_batch_prepare(int num_views, const gstex_view_desc* views, int block_width, void* views_dev,
+                        int32_t* tile_view, long long* pix_offsets, gstex_stream_t stream);
+
+/* AABB, tile count (counts [V*N], view-major) and SH colour
+ * (colors [V,N,3]) of every (view, Gaussian); sh_dtype 0 float32, 1 bfloat16.
+ * Batched form of get_aabb_2d + get_num_tiles_hit_2d + spherical_harmonics. */
+int gstex_batch_project(int num_points, int num_views, const void* views_dev, const float* means,
+                        const float* scales, float glob_scale, const float* quats, const void* sh_coeffs,
+                        int sh_dtype, int sh_degree, int block_width, float* colors, int32_t* counts,
+                        gstex_stream_t stream);
+
+/* Emission of (global tile << 32 | depth bits) keys into the slots of the
+ * inclusive scan cum [V*N] of the counts (total = its last value, device).
+ * Writes stop at capacity; count receives min(total, capacity) and
+ * *overflow is set when total exceeds capacity.  Batched form of
+ * map_gaussian_to_intersects. */
+int gstex_batch_emit(int num_points, int num_views, const void* views_dev, const float* means, const float* scales,
+                     float glob_scale, const float* quats, int block_width, const int32_t* cum,
+                     const int64_t* total, long long capacity, int64_t* keys, int32_t* gaussian_ids,
+                     int64_t* count, int* overflow, gstex_stream_t stream);
+
+typedef struct gstex_batch_inputs {
+    int num_points, num_views, block_width;
+    int channels, num_texels, texture_dtype, settings;
+    int total_tiles;
+    const void* views;                  /* gstex_batch_prepare */
+    const int32_t* tile_view;           /* [total_tiles] */
+    const int32_t* tile_order;          /* optional queue order of global tiles */
+    const int32_t* gaussian_ids_sorted;
+    const int32_t* tile_bins;           /* [total_tiles, 2] */
+    const float* colors;                /* [V, N, 3] */
+    const float* opacities;
+    const float* means;
+    const float* scales;
+    float glob_scale;
+    const float* quats;
+    const float* uv0;
+    const float* umap;
+    const float* vmap;
+    const int32_t* texture_dims;
+    const void* texture;
+    const float* background;            /* [3] device */
+    int* queue;                         /* device int (tile queue counter) */
+    int grid;                           /* persistent CTAs; 0 = all resident */
+} gstex_batch_inputs;
+
+/* Forward of all views: outputs are the concatenated per-view buffers
+ * (pixel p of view v at pix_offsets[v] + p).  Batched texture_forward. */
+int gstex_batch_forward(const gstex_batch_inputs* in, const gstex_forward_outputs* out, gstex_stream_t stream);
+
+/* Backward of all views.  io->v_colors is [V, N, 3] (per-view colour
+ * gradients, for the SH adjoint); the other Gaussian gradients are summed
+ * over views; null upstream-gradient pointers mean zero.  Workspace:
+ * gstex_batch_backward_workspace_bytes(N).  Batched texture_backward. */
+size_t gstex_batch_backward_workspace_bytes(int num_points);
+int gstex_batch_backward(const gstex_batch_inputs* in, const gstex_backward_io* io, gstex_stream_t stream);
+
+/* SH coefficient gradients [N, bases(degree), 3] summed over views.
+ * Batched compute_sh_backward. */
+int gstex_batch_sh_backward(int num_points, int num_views, const void* views_dev, const float* means,
+                            int sh_degree, const float* v_colors, float* v_coeffs, gstex_stream_t stream);
+
+/* The reference demo's image losses (example.py:189-209) over all views,
+ * with their gradients; *loss (device) receives the sum over views. */
+int gstex_batch_image_loss(long long total_pixels, int num_views, const long long* pix_offsets, int channels,
+                           const float* img, const float* tex, const float* normal, const float* reg,
+                           const float* tgt_img, const float* tgt_tex, float w_img, float w_tex, float w_reg,
+                           float w_normal, float* v_img, float* v_tex, float* v_normal, float* v_reg, float* loss,
+                           gstex_stream_t stream);
 
 #ifdef __cplusplus
 }

@@ -310,3 +310,11 @@ def project_points(means, viewmat, fx, fy, cx, cy):
     pix = np.stack([p[:, 0] * rw * np.float32(fx) + np.float32(cx),
                     p[:, 1] * rw * np.float32(fy) + np.float32(cy)], -1)
     return pix, p[:, 2].copy()
+
+
+def camera_depths(means, viewmat):
+    """Camera-space z of each mean with the float32 operation order of the
+    kernels' transform (m8*x + m9*y + m10*z + m11, no fused multiply-add)."""
+    m = np.asarray(means, np.float32)
+    v = np.asarray(viewmat, np.float32).reshape(-1)
+    return (((v[8] * m[:, 0] + v[9] * m[:, 1]) + v[10] * m[:, 2]) + v[11]).astype(np.float32)

@@ -38,7 +38,7 @@ def test_status_strings_and_workspace_queries():
     assert L.gstex_status_string(2) == b"buffer too small"
     assert L.gstex_version().decode().count(".") == 2
     assert L.gstex_sort_workspace_bytes(1000) >= 1000 * 12
-    assert L.gstex_backward_workspace_bytes(10) >= 10 * 26 * 4
+    assert L.gstex_backward_workspace_bytes(10) >= 10 * 24 * 4
     assert L.gstex_scan_workspace_bytes(1) > 0
 
 

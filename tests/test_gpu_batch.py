@@ -1,0 +1,139 @@
+"""Batched multi-view path (one launch per stage over all views) against the
+CPU oracle run view by view."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda:0"
+
+
+@pytest.fixture(scope="module")
+def setup():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from gstex_cuda_gb300 import batch as B, synthetic
+    g = torch.Generator().manual_seed(9)
+    cams = synthetic.sphere_cameras(g, 4, radius=8.0, resolutions=[(96, 64), (80, 80), (128, 72), (64, 96)])
+    spec = synthetic._finish_with_area(g, torch.empty(3000, 3).uniform_(-3, 3, generator=g), 0.01, 0.1, 3, "normal",
+                                       cams, 40_000, "multi", {})
+    scene = B.Scene(means=spec.means.to(DEV), scales=spec.scales.to(DEV), quats=spec.quats.to(DEV),
+                    opacity=spec.opacity.to(DEV), sh_coeffs=spec.sh_coeffs.to(DEV), sh_degree=3,
+                    uv0=spec.uv0.to(DEV), umap=spec.umap.to(DEV), vmap=spec.vmap.to(DEV),
+                    texture_dims=spec.texture_dims.to(DEV), texture=spec.texture.to(DEV))
+    bcams = [B.Camera(c.viewmat, c.fx, c.fy, c.cx, c.cy, c.width, c.height) for c in cams]
+    r = B.BatchRenderer(bcams, spec.num_points, capacity=1 << 20)
+    P = r.total_pixels
+    gen = torch.Generator().manual_seed(1)
+    tgt_img = torch.rand(P, 3, generator=gen).to(DEV)
+    tgt_tex = torch.rand(P, 3, generator=gen).to(DEV)
+    loss = r.step(scene, tgt_img, tgt_tex)
+    torch.cuda.synchronize()
+    return spec, cams, r, scene, loss
+
+
+def _scene_np(spec, colors):
+    return oracle.Scene(means=spec.means.numpy(), scales=spec.scales.numpy(), quats=spec.quats.numpy(),
+                        opacity=spec.opacity.numpy(), colors=colors, uv0=spec.uv0.numpy(), umap=spec.umap.numpy(),
+                        vmap=spec.vmap.numpy(), texture_dims=spec.texture_dims.numpy(), texture=spec.texture.numpy())
+
+
+def test_batch_binning_bit_exact_per_view(setup):
+    spec, cams, r, scene, _ = setup
+    assert r.check_capacity()
+    ks = r.keys_sorted.cpu().numpy()
+    gs = r.gids_sorted.cpu().numpy()
+    n = int(r.count.item())
+    counts = r.counts.cpu().numpy().reshape(r.V, r.N)
+    off = 0
+    for v, cam in enumerate(cams):
+        c, e = oracle.get_aabb_2d(spec.means.numpy(), spec.scales.numpy(), 1.0, spec.quats.numpy(),
+                                  cam.viewmat.numpy(), cam.fx, cam.fy, cam.cx, cam.cy)
+        nt = oracle.num_tiles_hit(c, e, cam.height, cam.width, 16)
+        np.testing.assert_array_equal(counts[v], nt)
+        d = oracle.camera_depths(spec.means.numpy(), cam.viewmat.numpy())
+        b = oracle.bin_and_sort(c, e, d, nt, cam.height, cam.width, 16)
+        m = b["n_isect"]
+        toff = int(sum(((cc.width + 15) // 16) * ((cc.height + 15) // 16) for cc in cams[:v]))
+        np.testing.assert_array_equal(ks[off:off + m] - (np.int64(toff) << 32), b["isect_ids_sorted"])
+        np.testing.assert_array_equal(gs[off:off + m], b["gaussian_ids_sorted"])
+        off += m
+    assert off == n
+
+
+def test_batch_forward_backward_vs_oracle(setup):
+    spec, cams, r, scene, loss = setup
+    gs = r.gids_sorted.cpu().numpy()
+    bins = r.bins.cpu().numpy()
+    vcol = r.grads["vcolors"].cpu().numpy()
+    ups = {k: v.cpu().numpy() for k, v in r.ups.items()}
+    tot = None
+    vcoef = 0
+    toff = 0
+    for v, cam in enumerate(cams):
+        dirs = (spec.means - cam.position[None]).numpy()
+        col = oracle.sh_forward(3, 3, dirs, spec.sh_coeffs.numpy(), prec="f64")
+        np.testing.assert_allclose(r.colors[v].cpu().numpy(), col, atol=2e-5, rtol=1e-5)
+        sc = _scene_np(spec, r.colors[v].cpu().numpy())
+        oc = oracle.Camera(cam.viewmat.numpy(), cam.c2w.numpy(), cam.fx, cam.fy, cam.cx, cam.cy, cam.height,
+                           cam.width)
+        nt = ((cam.width + 15) // 16) * ((cam.height + 15) // 16)
+        vb = bins[toff:toff + nt]
+        toff += nt
+        ref = oracle.texture_forward(sc, oc, gs, vb, 16, 1 << 8, np.zeros(3), prec="f64")
+        for k in ("img", "texture", "normal", "final_T"):
+            got = r.view_output(k, v).cpu().numpy()
+            np.testing.assert_allclose(got, ref[k].reshape(got.shape), atol=5e-5, err_msg=k)
+        a, b = r.pix_offsets_host[v], r.pix_offsets_host[v + 1]
+        H, W = cam.height, cam.width
+        up = dict(img=ups["img"][a:b].reshape(H, W, 3), texture=ups["texture"][a:b].reshape(H, W, 3),
+                  normal=ups["normal"][a:b].reshape(H, W, 3), reg=ups["reg"][a:b].reshape(H, W))
+        g = oracle.texture_backward(sc, oc, gs, vb, 16, 1 << 8, np.zeros(3), ref, up["img"], np.zeros((H, W)),
+                                    up["reg"], np.zeros((H, W)), up["texture"], up["normal"], prec="f64")
+        err = np.abs(vcol[v] - g["colors"]).max() / (np.abs(g["colors"]).max() + 1e-12)
+        assert err < 5e-4, ("vcolors", v, err)
+        vcoef = vcoef + oracle.sh_backward(3, 3, dirs, g["colors"], prec="f64")
+        tot = g if tot is None else {k: tot[k] + g[k] for k in tot}
+    G = r.grads
+    for k in ("opacity", "means", "scales", "quats", "uv0", "umap", "vmap", "texture"):
+        got = G[k].cpu().numpy().reshape(-1)
+        ref = tot[k].reshape(-1)
+        err = np.abs(got - ref).max() / (np.abs(ref).max() + 1e-12)
+        assert err < 5e-4, (k, err)
+    err = np.abs(G["sh_coeffs"].cpu().numpy() - vcoef).max() / (np.abs(vcoef).max() + 1e-12)
+    assert err < 5e-4, ("sh", err)
+
+
+def test_batch_loss_value(setup):
+    spec, cams, r, scene, loss = setup
+    o = r.out
+    ref = 0.0
+    tgt = None
+    for v in range(r.V):
+        a, b = r.pix_offsets_host[v], r.pix_offsets_host[v + 1]
+        img = o["img"][a:b].double()
+        n = o["normal"][a:b].double()
+        ref += float(o["reg"][a:b].double().mean()) * 100.0
+        ref += 0.05 * float((n[:, 0] ** 2 + n[:, 1] ** 2 + (1 - n[:, 2]) ** 2).mean())
+    assert np.isfinite(float(loss.item()))
+    assert float(loss.item()) >= ref * 0.999  # the MSE terms are non-negative
+
+
+def test_batch_graph_replay_matches_eager(setup):
+    spec, cams, r, scene, _ = setup
+    P = r.total_pixels
+    gen = torch.Generator().manual_seed(1)
+    tgt_img = torch.rand(P, 3, generator=gen).to(DEV)
+    tgt_tex = torch.rand(P, 3, generator=gen).to(DEV)
+    r.step(scene, tgt_img, tgt_tex)
+    torch.cuda.synchronize()
+    eager = {k: v.clone() for k, v in r.grads.items()}
+    eager_img = r.out["img"].clone()
+    r.capture(scene, tgt_img, tgt_tex)
+    r.replay()
+    torch.cuda.synchronize()
+    torch.testing.assert_close(r.out["img"], eager_img, atol=1e-6, rtol=0)
+    for k, v in eager.items():
+        torch.testing.assert_close(r.grads[k], v, atol=1e-5 * (float(v.abs().max()) + 1e-9), rtol=1e-4)

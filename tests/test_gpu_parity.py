@@ -133,14 +133,28 @@ def test_phantom_slots_of_clipped_gaussians():
 # --------------------------------------------------------------------------
 # compositor forward / backward vs oracle
 # --------------------------------------------------------------------------
-def _compare_forward(case, bw, settings, bg, tol_img, texture=None, prec="f64"):
+def _close(got, ref, tol, frac, name):
+    """|got - ref| <= tol everywhere, except for at most a fraction ``frac`` of
+    elements (pixels where a float rounding difference flips one of the
+    reference's hard thresholds: alpha >= 1/255, T <= 1e-4, T > 0.5), which
+    must still stay below 1e-2."""
+    err = np.abs(np.asarray(got, np.float64) - np.asarray(ref, np.float64))
+    if err.size == 0:
+        return
+    bad = err > tol
+    assert bad.mean() <= frac, (name, float(bad.mean()), float(err.max()))
+    assert err.max() < max(1e-2, tol), (name, float(err.max()))
+
+
+def _compare_forward(case, bw, settings, bg, tol_img, texture=None, prec="f64", frac=0.0):
     b = case.binning_cuda(bw)
     ref = oracle.texture_forward(case.scene_np, case.cam_np, b["gaussian_ids_sorted"].cpu().numpy(),
                                  b["tile_bins"].cpu().numpy(), bw, settings, bg, prec=prec)
     out, bgt = case.forward_cuda(b["gaussian_ids_sorted"], b["tile_bins"], bw, settings, bg, texture=texture)
-    for k in ("img", "texture", "normal", "reg_s", "final_T"):
-        np.testing.assert_allclose(np_(out[k]), ref[k], atol=tol_img, rtol=0, err_msg=k)
-    np.testing.assert_allclose(np_(out["reg"]), ref["reg"], atol=tol_img * 10, rtol=tol_img, err_msg="reg")
+    for k in ("img", "texture", "normal", "final_T"):
+        _close(np_(out[k]), ref[k], tol_img, frac, k)
+    _close(np_(out["reg_s"]), ref["reg_s"], tol_img * (1 + np.abs(ref["reg_s"])), frac, "reg_s")
+    _close(np_(out["reg"]), ref["reg"], tol_img * 10 + tol_img * np.abs(ref["reg"]), frac, "reg")
     same_depth = np_(out["depth_idx"]) == ref["depth_idx"]
     assert same_depth.mean() > 0.999
     np.testing.assert_allclose(np_(out["depth"])[same_depth], ref["depth"][same_depth], atol=tol_img * 10,
@@ -161,6 +175,8 @@ def _compare_backward(case, b, out, bgt, ref, bw, settings, bg, rtol, texture=No
         x = np_(g[k]).reshape(-1)
         if k == "texture" and x.size != r.size:  # bf16 layout [T,4]
             x = np_(g[k])[:, :3].reshape(-1)
+        if r.size == 0:
+            continue
         scale = np.abs(r).max() + 1e-12
         err = np.abs(x - r).max() / scale
         assert err < rtol, (k, err)
@@ -244,6 +260,4 @@ def test_untextured_800_full_size_vs_oracle():
     spec = synthetic.untextured(seed=1, n=100_000, size=800)
     case = Case(spec)
     bg = np.zeros(3)
-    b, out, bgt, ref = _compare_forward(case, 16, 1 << 8, bg, 2e-3)
-    err = np.abs(np_(out["img"]) - ref["img"])
-    assert np.quantile(err, 0.999) < 1e-4, np.quantile(err, 0.999)
+    b, out, bgt, ref = _compare_forward(case, 16, 1 << 8, bg, 1e-4, frac=2e-5)
