@@ -35,6 +35,10 @@ WORKLOAD = ("32 cameras (512^2/800^2/1280x720/1920x1080, r=8 sphere), 500k Gauss
             "SH deg 3 (bf16), fwd + image losses + bwd + SH adjoint")
 
 
+def log(msg):
+    print(f"[bench] {msg}", file=sys.stderr, flush=True)
+
+
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -250,6 +254,7 @@ def main():
         r.step(scene, tgt_img, tgt_tex)
         torch.cuda.synchronize(dev)
     I = r.intersections()
+    log(f"intersections {I}, pixels {P}, tiles {r.total_tiles}, capacity {r.capacity}")
 
     # timed region: eager steps (one launch per stage), CUDA events around the
     # compositor kernels on the launching stream
@@ -289,6 +294,7 @@ def main():
     fwd_ms = sum(a.elapsed_time(b) for a, b, _, _ in pairs) / len(pairs)
     bwd_ms = sum(c.elapsed_time(d) for _, _, c, d in pairs) / len(pairs)
     value = world * args.views * args.steps / elapsed
+    log(f"eager: {1000 * elapsed / args.steps:.2f} ms/step, {value:.1f} frames/s; fwd {fwd_ms:.2f} ms, bwd {bwd_ms:.2f} ms")
 
     # graph replay of the same step (launch overhead removed)
     graph_fps = None
@@ -306,6 +312,7 @@ def main():
         graph_fps = args.views * args.steps / (g0.elapsed_time(g1) / 1000.0)
     except Exception as ex:  # graph capture is an optimisation; report why it was skipped
         graph_fps = f"unavailable: {type(ex).__name__}: {ex}"
+    log(f"graph: {graph_fps}")
 
     # end to end through the public API with host inputs: pinned host copies of
     # every scene input are uploaded each step, the loss is read back
@@ -325,20 +332,25 @@ def main():
         el = time.perf_counter() - t0
         e2e = {"value": world * args.views * args.steps / el, "unit": "frames/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": 4}
+        log(f"e2e: {e2e}")
 
     # plain per-view fp32 path (drop-in API, one view after another, host sync per view)
     plain = None
     if not args.no_plain:
-        scene32 = device_scene(spec, dev, bf16=False)
-        ks = max(1, args.steps // 5)
-        B.plain_step(scene32, cams, tgt_img, tgt_tex, r.pix_offsets_host)
-        torch.cuda.synchronize(dev)
-        t0 = time.perf_counter()
-        for _ in range(ks):
+        try:
+            scene32 = device_scene(spec, dev, bf16=False)
+            ks = max(1, args.steps // 5)
             B.plain_step(scene32, cams, tgt_img, tgt_tex, r.pix_offsets_host)
-        torch.cuda.synchronize(dev)
-        plain = args.views * ks / (time.perf_counter() - t0)
-        del scene32
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            for _ in range(ks):
+                B.plain_step(scene32, cams, tgt_img, tgt_tex, r.pix_offsets_host)
+            torch.cuda.synchronize(dev)
+            plain = args.views * ks / (time.perf_counter() - t0)
+            del scene32
+        except Exception as ex:
+            plain = f"unavailable: {type(ex).__name__}: {ex}"
+        log(f"plain fp32 per-view: {plain}")
 
     # roofline of the dominant compositor kernel
     T = spec.num_texels
@@ -354,9 +366,13 @@ def main():
     if rank == 0 and not args.no_cpu:
         import oracle
         oracle.build()
-        fps, cores, n, el, views = cpu_sample(spec, args.cpu_seconds)
-        cpu = {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port",
-               "sample": f"{n} of the 32 views ({', '.join(views)}), full fwd+bwd each, {el:.1f} s (CPU oracle)"}
+        try:
+            fps, cores, n, el, views = cpu_sample(spec, args.cpu_seconds)
+            cpu = {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port",
+                   "sample": f"{n} of the 32 views ({', '.join(views)}), full fwd+bwd each, {el:.1f} s (CPU oracle)"}
+        except Exception as ex:
+            cpu = {"value": None, "unavailable": f"{type(ex).__name__}: {ex}"}
+        log(f"cpu: {cpu}")
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,

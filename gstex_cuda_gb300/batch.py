@@ -351,8 +351,8 @@ def plain_step(s: Scene, cameras: Sequence[Camera], tgt_img, tgt_tex, pix_offset
     bw = block_width
     for v, cam in enumerate(cameras):
         H, W = cam.height, cam.width
-        vm = cam.viewmat.to(dev)
-        c2w = torch.linalg.inv(vm)
+        vm = cam.viewmat.to(dev).contiguous()
+        c2w = torch.linalg.inv(vm).contiguous()
         campos = c2w[:3, 3]
         dirs = (s.means - campos[None]).contiguous()
         coeffs = s.sh_coeffs if s.sh_coeffs.dtype == torch.float32 else s.sh_coeffs.float()

