@@ -31,6 +31,7 @@ PER_FILE = {
     "batch.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"],
     "sample.cu": ["-fmad=false"],
     "status.cu": [],
+    "sort_static.cu": [],
 }
 
 

@@ -97,6 +97,24 @@ size_t gstex_sort_workspace_bytes(int n);
 int gstex_sort_pairs(int n, int end_bit, const int64_t* keys_in, const int32_t* vals_in, int64_t* keys_out,
                      int32_t* vals_out, void* workspace, size_t workspace_bytes, gstex_stream_t stream);
 
+/* Largest n accepted by gstex_sort_pairs_static. */
+#define GSTEX_SORT_STATIC_MAX_ITEMS 1048576
+
+/* The same stable pair sort for callers that cannot allocate device memory
+ * (a host framework that owns all device allocations, a plugin handed only a
+ * stream and raw pointers, real-time code where an allocation could stall or
+ * fail mid-frame).  No counterpart in the reference, which allocates with
+ * torch inside each op.  Scratch is one file-scope device array of 13.1 MB
+ * sized for GSTEX_SORT_STATIC_MAX_ITEMS pairs, held by every GPU that loads
+ * the library until exit; larger n returns GSTEX_ERR_CAPACITY.  The first
+ * call on a device looks up the array's device address (do it before any
+ * stream capture).  All calls on a device share the array: calls that
+ * overlap on the GPU race and must be serialised by the caller; nothing in it
+ * needs clearing between calls.  Allocates nothing and calls no allocating
+ * routine. */
+int gstex_sort_pairs_static(int n, int end_bit, const int64_t* keys_in, const int32_t* vals_in,
+                            int64_t* keys_out, int32_t* vals_out, gstex_stream_t stream);
+
 /* Same sort with the number of items read from device memory (*count,
  * clamped to capacity): the launch shape depends only on capacity, so the
  * call can be captured in a CUDA graph.  Workspace:
