@@ -255,6 +255,8 @@ def main():
         torch.cuda.synchronize(dev)
     I = r.intersections()
     log(f"intersections {I}, pixels {P}, tiles {r.total_tiles}, capacity {r.capacity}")
+    tuned = r.autotune(scene, tgt_img, tgt_tex)
+    log(f"autotune: {tuned}")
 
     # timed region: eager steps (one launch per stage), CUDA events around the
     # compositor kernels on the launching stream
@@ -381,7 +383,8 @@ def main():
                 "config": {"workload": WORKLOAD, "views": args.views, "num_points": N, "texels": T,
                            "storage": "bf16 texels [T,4] + bf16 SH; fp32 blending and gradients",
                            "intersections": I, "pixels": P, "tiles": tiles, "parallelism": f"replicas x{world}",
-                           "l2": "working set > L2 (no flush)", "timed": "eager, one launch per stage"},
+                           "l2": "working set > L2 (no flush)", "timed": "eager, one launch per stage",
+                           "autotune": tuned},
                 "e2e": e2e, "gpu_launches": int(launches),
                 "roofline": {"bound": "hbm", "kernel": dom[0], "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,

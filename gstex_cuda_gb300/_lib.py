@@ -27,7 +27,8 @@ class RasterInputs(ctypes.Structure):
                 ("texture_dims", _P), ("gaussian_ids_sorted", _P), ("tile_bins", _P), ("colors", _P),
                 ("opacities", _P), ("means", _P), ("scales", _P), ("glob_scale", _F), ("quats", _P),
                 ("uv0", _P), ("umap", _P), ("vmap", _P), ("texture", _P), ("viewmat", _P),
-                ("fx", _F), ("fy", _F), ("cx", _F), ("cy", _F), ("settings", _I), ("background", _P)]
+                ("fx", _F), ("fy", _F), ("cx", _F), ("cy", _F), ("settings", _I), ("background", _P),
+                ("pixels_per_thread", _I)]
 
 
 class ForwardOutputs(ctypes.Structure):

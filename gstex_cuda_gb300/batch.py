@@ -41,7 +41,7 @@ class BatchInputs(ctypes.Structure):
                 ("views", _P), ("tile_view", _P), ("tile_order", _P), ("gaussian_ids_sorted", _P), ("tile_bins", _P),
                 ("colors", _P), ("opacities", _P), ("means", _P), ("scales", _P), ("glob_scale", _F), ("quats", _P),
                 ("uv0", _P), ("umap", _P), ("vmap", _P), ("texture_dims", _P), ("texture", _P), ("background", _P),
-                ("queue", _P), ("grid", _I)]
+                ("queue", _P), ("grid", _I), ("pixels_per_thread", _I)]
 
 
 _BATCH_SIGS = {
@@ -110,7 +110,8 @@ class BatchRenderer:
 
     def __init__(self, cameras: Sequence[Camera], num_points: int, *, channels: int = 3, texture_dtype=torch.float32,
                  block_width: int = 16, settings: int = 1 << 8, background=(0.0, 0.0, 0.0), capacity: int = 0,
-                 device="cuda:0", grid: int = 0, loss_weights: Optional[dict] = None):
+                 device="cuda:0", grid: int = 0, loss_weights: Optional[dict] = None, fwd_ppt: int = 1,
+                 bwd_ppt: int = 1):
         self.dev = torch.device(device)
         self.N = int(num_points)
         self.V = len(cameras)
@@ -119,6 +120,7 @@ class BatchRenderer:
         self.settings = int(settings)
         self.texmode = 1 if texture_dtype == torch.bfloat16 else 0
         self.grid = int(grid)
+        self.fwd_ppt, self.bwd_ppt = int(fwd_ppt), int(bwd_ppt)
         self.lw = dict(LOSS_WEIGHTS if loss_weights is None else loss_weights)
         L = _L()
         descs = (ViewDesc * self.V)()
@@ -187,7 +189,7 @@ class BatchRenderer:
         return 32 + max(1, int(self.total_tiles).bit_length())
 
     # ------------------------------------------------------------------
-    def _inputs(self, s: Scene) -> BatchInputs:
+    def _inputs(self, s: Scene, backward: bool = False) -> BatchInputs:
         bi = BatchInputs()
         bi.num_points, bi.num_views, bi.block_width = self.N, self.V, self.bw
         bi.channels, bi.num_texels, bi.texture_dtype, bi.settings = self.C, s.texture.shape[0], self.texmode, \
@@ -200,6 +202,7 @@ class BatchRenderer:
         bi.quats, bi.uv0, bi.umap, bi.vmap = ptr(s.quats), ptr(s.uv0), ptr(s.umap), ptr(s.vmap)
         bi.texture_dims, bi.texture, bi.background = ptr(s.texture_dims), ptr(s.texture), ptr(self.bg)
         bi.queue, bi.grid = ptr(self.queue), self.grid
+        bi.pixels_per_thread = self.bwd_ppt if backward else self.fwd_ppt
         return bi
 
     def bin(self, s: Scene):
@@ -272,7 +275,7 @@ class BatchRenderer:
                               ptr(u.get("texture")), ptr(u.get("normal")), ptr(g["vcolors"]), ptr(g["opacity"]),
                               ptr(g["means"]), ptr(g["scales"]), ptr(g["quats"]), ptr(g["uv0"]), ptr(g["umap"]),
                               ptr(g["vmap"]), ptr(g["texture"]), ptr(self.moments), self.moments.numel())
-        bi = self._inputs(s)
+        bi = self._inputs(s, backward=True)
         check(L.gstex_batch_backward(ctypes.byref(bi), ctypes.byref(bio), st), "batch_backward")
         check(L.gstex_batch_sh_backward(self.N, self.V, ptr(self.views_dev), ptr(s.means), s.sh_degree,
                                         ptr(g["vcolors"]), ptr(g["sh_coeffs"]), st), "batch_sh_backward")
@@ -287,6 +290,43 @@ class BatchRenderer:
         return loss
 
     # ------------------------------------------------------------------
+    def autotune(self, s: Scene, tgt_img, tgt_tex, reps: int = 2) -> dict:
+        """Choose pixels-per-thread for the forward and the backward kernel by
+        timing each candidate on this scene and these cameras (CUDA events)."""
+        stream = torch.cuda.current_stream(self.dev)
+        self.bin(s)
+
+        def timed(fn):
+            fn()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(reps):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize(self.dev)
+            return e0.elapsed_time(e1) / reps
+
+        result = {}
+        best = None
+        for ppt in (1, 2):
+            self.fwd_ppt = ppt
+            ms = timed(lambda: self.forward(s))
+            result[f"forward_ppt{ppt}_ms"] = ms
+            best = (ms, ppt) if best is None or ms < best[0] else best
+        self.fwd_ppt = best[1]
+        self.forward(s)
+        self.image_loss(tgt_img, tgt_tex)
+        best = None
+        for ppt in (1, 2):
+            self.bwd_ppt = ppt
+            ms = timed(lambda: self.backward(s))
+            result[f"backward_ppt{ppt}_ms"] = ms
+            best = (ms, ppt) if best is None or ms < best[0] else best
+        self.bwd_ppt = best[1]
+        result.update(fwd_ppt=self.fwd_ppt, bwd_ppt=self.bwd_ppt)
+        self.graph = None
+        return result
+
     def capture(self, s: Scene, tgt_img, tgt_tex):
         """Capture ``step`` for these (static) tensors in a CUDA graph."""
         self._grad_buffers(s)

@@ -116,99 +116,155 @@ __device__ __forceinline__ View load_view(const float* viewmat, float fx, float 
 // Gaussians with mu_z <= 0.01 (only reachable through the reference's
 // zero-slot entries) and pixels whose ray is within the reference's 1e-6
 // denominator clamp use the direct camera-space form instead.
+//
+// The record also carries a conservative screen box of the region where the
+// splat can reach alpha >= 1/255: sigma <= ln(255 * opacity) is an ellipse
+// in the splat plane, inside the rectangle +-a*s1*ax1 +-a*s2*ax2 with
+// a = sqrt(2 ln(255 opacity)) (inflated slightly); when all four corners are
+// in front of the camera the projected rectangle, hence the box of its
+// projected corners, contains every pixel whose ray meets the ellipse.  A
+// pixel outside the box is a pixel the reference skips (alpha < 1/255).
+//
+// Fields are grouped by how often the per-pixel loop reads them.
 // ---------------------------------------------------------------------------
-struct GaussRec {
-    float px0, py0;        // projected centre, pixels
-    float g, nu, nv;       // den = g + nu*du + nv*dv
-    float tvn;             // n_c . mu_c
-    float p1u, p1v, p2u, p2v;  // plane coordinates l1, l2 numerators (unscaled)
-    float is1, is2;        // 1 / (scale * glob_scale)
-    float opac;
-    float3 color;
-    float3 mu_c;           // camera-space mean (direct form)
-    float3 a1c, a2c, nc;   // camera-space axes
-    float uu, uv_, vu, vv; // texture uv numerators: u = uv0.x + (uu*du + uv_*dv)/den
-    float uv0x, uv0y;
-    float3 umc, vmc;       // camera-space umap / vmap (direct form, backward)
-    float3 nw;             // world-space normal (axis 3)
-    float bx, by;          // reference projected centre (helpers.cuh:145-152), for the blur term
-    int h, w, start;       // texture chart
-    int gid;
-    int flags;             // bit 0: direct form only
+struct RecHot {   // every (pixel, Gaussian) pair
+    float4 a;     // px0, py0, g, tvn
+    float4 b;     // nu, nv, box x0, box x1
+    float4 c;     // p1u, p1v, p2u, p2v (scaled by 1 / (scale * glob_scale))
+    float4 d;     // box y0, box y1, opacity, flags (int bits; bit 0: direct form only)
+};
+struct RecWarm {  // pairs that pass the alpha test
+    float4 uvm;   // uu, uv_, vu, vv: texture uv numerators
+    float4 uvs;   // uv0.x, uv0.y, blur centre x, blur centre y
+    float4 col;   // colour rgb, 1 / (scale_x * glob_scale)
+    float4 nrm;   // world normal (axis 3), 1 / (scale_y * glob_scale)
+    int4 tex;     // chart h, w, start, Gaussian id
+};
+struct RecCold {  // direct form and the backward's ray terms
+    float4 mu;    // camera-space mean
+    float4 a1;    // camera-space axis 1
+    float4 a2;    // camera-space axis 2
+    float4 n;     // camera-space normal
+    float4 um;    // camera-space umap
+    float4 vm;    // camera-space vmap
+};
+constexpr int kRecBytes = sizeof(RecHot) + sizeof(RecWarm) + sizeof(RecCold);
+
+struct Recs {
+    RecHot* hot;
+    RecWarm* warm;
+    RecCold* cold;
+    __device__ __forceinline__ static Recs carve(unsigned char* smem, int n) {
+        Recs r;
+        r.hot = reinterpret_cast<RecHot*>(smem);
+        r.warm = reinterpret_cast<RecWarm*>(smem + sizeof(RecHot) * n);
+        r.cold = reinterpret_cast<RecCold*>(smem + (sizeof(RecHot) + sizeof(RecWarm)) * n);
+        return r;
+    }
 };
 
-__device__ __forceinline__ void make_record(GaussRec& R, int gid, const View& V, const float3 mean,
-                                            const float4 quat, const float2 scale, float glob_scale, float opac,
-                                            float3 color, float2 uv0, float3 umap, float3 vmap, int3 dims) {
+__device__ __forceinline__ float4 f4(float3 v, float w) { return make_float4(v.x, v.y, v.z, w); }
+__device__ __forceinline__ float3 f3(float4 v) { return make_float3(v.x, v.y, v.z); }
+
+__device__ __forceinline__ void make_record(RecHot& H, RecWarm& Wm, RecCold& Cd, int gid, const View& V,
+                                            const float3 mean, const float4 quat, const float2 scale,
+                                            float glob_scale, float opac, float3 color, float2 uv0, float3 umap,
+                                            float3 vmap, int3 dims, bool use_blur) {
     const Axes A = quat_axes(quat);
     const float3 mc = V.xform(mean);
     const float3 a1c = V.rot(A.a1), a2c = V.rot(A.a2), nc = V.rot(A.a3);
     const float3 umc = V.rot(umap), vmc = V.rot(vmap);
-    R.gid = gid;
-    R.mu_c = mc; R.a1c = a1c; R.a2c = a2c; R.nc = nc; R.umc = umc; R.vmc = vmc;
-    R.nw = A.a3;
-    R.is1 = 1.f / (scale.x * glob_scale);
-    R.is2 = 1.f / (scale.y * glob_scale);
-    R.opac = opac;
-    R.color = color;
-    R.uv0x = uv0.x; R.uv0y = uv0.y;
-    R.h = dims.x; R.w = dims.y; R.start = dims.z;
-    // blur centre exactly as the reference projects it
-    {
-        const float rw = 1.f / (mc.z + 1e-6f);
-        R.bx = mc.x * rw * V.fx + V.cx;
-        R.by = mc.y * rw * V.fy + V.cy;
+    const float is1 = 1.f / (scale.x * glob_scale), is2 = 1.f / (scale.y * glob_scale);
+    const float tvn = dot3(nc, mc);
+    // blur centre exactly as the reference projects it (helpers.cuh:145-152)
+    const float rwb = 1.f / (mc.z + 1e-6f);
+    const float bx = mc.x * rwb * V.fx + V.cx, by = mc.y * rwb * V.fy + V.cy;
+    Cd.mu = f4(mc, 0.f);
+    Cd.a1 = f4(a1c, is1);
+    Cd.a2 = f4(a2c, is2);
+    Cd.n = f4(nc, 0.f);
+    Cd.um = f4(umc, 0.f);
+    Cd.vm = f4(vmc, 0.f);
+    Wm.uvs = make_float4(uv0.x, uv0.y, bx, by);
+    Wm.col = f4(color, is1);
+    Wm.nrm = f4(A.a3, is2);
+    Wm.tex = make_int4(dims.x, dims.y, dims.z, gid);
+
+    // screen box of alpha >= 1/255 (empty when the splat can never reach it)
+    float x0 = INFINITY, x1 = -INFINITY, y0 = INFINITY, y1 = -INFINITY;
+    const float smax = __logf(255.f * opac);
+    int flags = 0;
+    if (!(mc.z > kTNear)) flags = 1;
+    if (smax > 0.f) {
+        const float a = sqrtf(2.f * smax + 1e-3f) * 1.002f;
+        const float e1 = a / is1, e2 = a / is2;
+        bool front = !flags;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const float s1 = (k & 1) ? -e1 : e1, s2 = (k & 2) ? -e2 : e2;
+            const float3 c = make_float3(mc.x + s1 * a1c.x + s2 * a2c.x, mc.y + s1 * a1c.y + s2 * a2c.y,
+                                         mc.z + s1 * a1c.z + s2 * a2c.z);
+            front = front && c.z > 1e-3f;
+            const float iz = 1.f / c.z;
+            const float px = V.fx * c.x * iz + V.cx, py = V.fy * c.y * iz + V.cy;
+            x0 = fminf(x0, px); x1 = fmaxf(x1, px);
+            y0 = fminf(y0, py); y1 = fmaxf(y1, py);
+        }
+        if (front) {
+            const float mx = 1e-2f + 1e-5f * (fabsf(x0) + fabsf(x1)), my = 1e-2f + 1e-5f * (fabsf(y0) + fabsf(y1));
+            x0 -= mx; x1 += mx; y0 -= my; y1 += my;
+        } else {
+            x0 = y0 = -INFINITY;
+            x1 = y1 = INFINITY;
+        }
+        if (use_blur) {
+            const float r = sqrtf(smax) * 1.002f + 1e-2f;
+            x0 = fminf(x0, bx - r); x1 = fmaxf(x1, bx + r);
+            y0 = fminf(y0, by - r); y1 = fmaxf(y1, by + r);
+        }
+    } else if (opac != opac) {
+        // a NaN opacity gives alpha = fminf(0.99, NaN) = 0.99 in the reference: never cull it
+        x0 = y0 = -INFINITY;
+        x1 = y1 = INFINITY;
     }
-    R.tvn = dot3(nc, mc);
-    if (!(mc.z > kTNear)) {
-        R.flags = 1;
-        R.px0 = V.cx; R.py0 = V.cy;
-        R.g = R.nu = R.nv = 0.f;
-        R.p1u = R.p1v = R.p2u = R.p2v = 0.f;
-        R.uu = R.uv_ = R.vu = R.vv = 0.f;
+
+    if (flags) {
+        H.a = make_float4(V.cx, V.cy, 0.f, tvn);
+        H.b = make_float4(0.f, 0.f, x0, x1);
+        H.c = make_float4(0.f, 0.f, 0.f, 0.f);
+        H.d = make_float4(y0, y1, opac, __int_as_float(flags));
+        Wm.uvm = make_float4(0.f, 0.f, 0.f, 0.f);
         return;
     }
-    R.flags = 0;
-    // Near edge-on splats: the coefficient algebra runs in double.
     const float u0f = mc.x / mc.z, v0f = mc.y / mc.z;
     const float gf = nc.x * u0f + nc.y * v0f + nc.z;
     if (fabsf(gf) < 0.05f) {
+        // near edge-on splat: the coefficient algebra runs in double
         const double mz = mc.z, u0 = (double)mc.x / mz, v0 = (double)mc.y / mz;
         const double g = (double)nc.x * u0 + (double)nc.y * v0 + nc.z;
         const double ifx = 1.0 / V.fx, ify = 1.0 / V.fy;
         const double a1d = a1c.x * u0 + a1c.y * v0 + a1c.z, a2d = a2c.x * u0 + a2c.y * v0 + a2c.z;
         const double umd = umc.x * u0 + umc.y * v0 + umc.z, vmd = vmc.x * u0 + vmc.y * v0 + vmc.z;
-        R.px0 = (float)(V.fx * u0 + V.cx);
-        R.py0 = (float)(V.fy * v0 + V.cy);
-        R.g = (float)g;
-        R.nu = (float)(nc.x * ifx);
-        R.nv = (float)(nc.y * ify);
-        R.p1u = (float)(mz * (g * a1c.x - a1d * nc.x) * ifx);
-        R.p1v = (float)(mz * (g * a1c.y - a1d * nc.y) * ify);
-        R.p2u = (float)(mz * (g * a2c.x - a2d * nc.x) * ifx);
-        R.p2v = (float)(mz * (g * a2c.y - a2d * nc.y) * ify);
-        R.uu = (float)(mz * (g * umc.x - umd * nc.x) * ifx);
-        R.uv_ = (float)(mz * (g * umc.y - umd * nc.y) * ify);
-        R.vu = (float)(mz * (g * vmc.x - vmd * nc.x) * ifx);
-        R.vv = (float)(mz * (g * vmc.y - vmd * nc.y) * ify);
-        return;
+        H.a = make_float4((float)(V.fx * u0 + V.cx), (float)(V.fy * v0 + V.cy), (float)g, tvn);
+        H.b = make_float4((float)(nc.x * ifx), (float)(nc.y * ify), x0, x1);
+        H.c = make_float4((float)(mz * (g * a1c.x - a1d * nc.x) * ifx * is1),
+                          (float)(mz * (g * a1c.y - a1d * nc.y) * ify * is1),
+                          (float)(mz * (g * a2c.x - a2d * nc.x) * ifx * is2),
+                          (float)(mz * (g * a2c.y - a2d * nc.y) * ify * is2));
+        Wm.uvm = make_float4((float)(mz * (g * umc.x - umd * nc.x) * ifx), (float)(mz * (g * umc.y - umd * nc.y) * ify),
+                             (float)(mz * (g * vmc.x - vmd * nc.x) * ifx), (float)(mz * (g * vmc.y - vmd * nc.y) * ify));
+    } else {
+        const float mz = mc.z, ifx = 1.f / V.fx, ify = 1.f / V.fy;
+        const float a1d = a1c.x * u0f + a1c.y * v0f + a1c.z, a2d = a2c.x * u0f + a2c.y * v0f + a2c.z;
+        const float umd = umc.x * u0f + umc.y * v0f + umc.z, vmd = vmc.x * u0f + vmc.y * v0f + vmc.z;
+        H.a = make_float4(V.fx * u0f + V.cx, V.fy * v0f + V.cy, gf, tvn);
+        H.b = make_float4(nc.x * ifx, nc.y * ify, x0, x1);
+        H.c = make_float4(mz * (gf * a1c.x - a1d * nc.x) * ifx * is1, mz * (gf * a1c.y - a1d * nc.y) * ify * is1,
+                          mz * (gf * a2c.x - a2d * nc.x) * ifx * is2, mz * (gf * a2c.y - a2d * nc.y) * ify * is2);
+        Wm.uvm = make_float4(mz * (gf * umc.x - umd * nc.x) * ifx, mz * (gf * umc.y - umd * nc.y) * ify,
+                             mz * (gf * vmc.x - vmd * nc.x) * ifx, mz * (gf * vmc.y - vmd * nc.y) * ify);
     }
-    const float mz = mc.z, ifx = 1.f / V.fx, ify = 1.f / V.fy;
-    const float a1d = a1c.x * u0f + a1c.y * v0f + a1c.z, a2d = a2c.x * u0f + a2c.y * v0f + a2c.z;
-    const float umd = umc.x * u0f + umc.y * v0f + umc.z, vmd = vmc.x * u0f + vmc.y * v0f + vmc.z;
-    R.px0 = V.fx * u0f + V.cx;
-    R.py0 = V.fy * v0f + V.cy;
-    R.g = gf;
-    R.nu = nc.x * ifx;
-    R.nv = nc.y * ify;
-    R.p1u = mz * (gf * a1c.x - a1d * nc.x) * ifx;
-    R.p1v = mz * (gf * a1c.y - a1d * nc.y) * ify;
-    R.p2u = mz * (gf * a2c.x - a2d * nc.x) * ifx;
-    R.p2v = mz * (gf * a2c.y - a2d * nc.y) * ify;
-    R.uu = mz * (gf * umc.x - umd * nc.x) * ifx;
-    R.uv_ = mz * (gf * umc.y - umd * nc.y) * ify;
-    R.vu = mz * (gf * vmc.x - vmd * nc.x) * ifx;
-    R.vv = mz * (gf * vmc.y - vmd * nc.y) * ify;
+    H.d = make_float4(y0, y1, opac, __int_as_float(flags));
 }
 
 // Per-pixel constants: pixel centre, camera direction d = (u, v, 1), |d|.
@@ -230,14 +286,18 @@ __device__ __forceinline__ PixelRay make_pixel(const View& V, int i, int j) {
     return P;
 }
 
+__device__ __forceinline__ bool outside_box(const RecHot& H, const PixelRay& P) {
+    return P.px < H.b.z || P.px > H.b.w || P.py < H.d.x || P.py > H.d.y;
+}
+
 // Intersection of a pixel ray with a staged splat.
 struct Hit {
-    float t;       // ray parameter along the unit ray (reference t)
-    float tcam;    // camera z of the hit (reference t * view_depth)
-    float l1, l2;  // plane coordinates
-    float du, dv;  // pixel offset from the projected centre
-    float inv;     // 1 / den (pixel-direction denominator, unnormalised)
-    float tu, tv;  // texture uv before clamping
+    float t;         // ray parameter along the unit ray (reference t)
+    float tcam;      // camera z of the hit (reference t * view_depth)
+    float l1s, l2s;  // plane coordinates divided by the scales
+    float du, dv;    // pixel offset from the projected centre (fast form)
+    float inv;       // d t_cam / d tvn: 1 / den (fast form), idn / den_ref (direct form)
+    bool direct;
 };
 
 __device__ __forceinline__ float clamp_denom(float d) {
@@ -246,36 +306,44 @@ __device__ __forceinline__ float clamp_denom(float d) {
     return d;
 }
 
-__device__ __forceinline__ Hit intersect(const GaussRec& R, const PixelRay& P) {
+__device__ __forceinline__ Hit intersect(const RecHot& Hr, const RecCold* Cd, const PixelRay& P) {
     Hit H;
-    H.du = P.px - R.px0;
-    H.dv = P.py - R.py0;
-    const float den = R.g + R.nu * H.du + R.nv * H.dv;
-    if (!R.flags && fabsf(den) >= kDenomEps * P.dn) {
-        const float inv = __frcp_rn(den);
+    H.du = P.px - Hr.a.x;
+    H.dv = P.py - Hr.a.y;
+    const float den = Hr.a.z + Hr.b.x * H.du + Hr.b.y * H.dv;
+    H.direct = __float_as_int(Hr.d.w) != 0 || !(fabsf(den) >= kDenomEps * P.dn);
+    if (!H.direct) {
+        const float inv = __fdividef(1.f, den);
         H.inv = inv;
-        H.tcam = R.tvn * inv;
+        H.tcam = Hr.a.w * inv;
         H.t = H.tcam * P.dn;
-        H.l1 = (R.p1u * H.du + R.p1v * H.dv) * inv;
-        H.l2 = (R.p2u * H.du + R.p2v * H.dv) * inv;
-        H.tu = R.uv0x + (R.uu * H.du + R.uv_ * H.dv) * inv;
-        H.tv = R.uv0y + (R.vu * H.du + R.vv * H.dv) * inv;
+        H.l1s = (Hr.c.x * H.du + Hr.c.y * H.dv) * inv;
+        H.l2s = (Hr.c.z * H.du + Hr.c.w * H.dv) * inv;
         return H;
     }
-    // direct camera-space form (with the reference's denominator clamp)
+    // direct camera-space form with the reference's denominator clamp
+    const RecCold& C = *Cd;
     const float3 d = make_float3(P.u, P.v, 1.f);
-    const float dref = clamp_denom(dot3(R.nc, d) * P.idn);
-    const float t = R.tvn / dref;
-    const float3 r = P.idn * d;
-    const float3 delta = t * r - R.mu_c;
+    const float dref = clamp_denom(dot3(f3(C.n), d) * P.idn);
+    const float t = Hr.a.w / dref;
+    const float3 delta = t * (P.idn * d) - f3(C.mu);
     H.inv = P.idn / dref;
     H.t = t;
     H.tcam = t * P.idn;
-    H.l1 = dot3(R.a1c, delta);
-    H.l2 = dot3(R.a2c, delta);
-    H.tu = R.uv0x + dot3(R.umc, delta);
-    H.tv = R.uv0y + dot3(R.vmc, delta);
+    H.l1s = dot3(f3(C.a1), delta) * C.a1.w;
+    H.l2s = dot3(f3(C.a2), delta) * C.a2.w;
     return H;
+}
+
+// Texture coordinates of the hit (before clamping).
+__device__ __forceinline__ float2 hit_uv(const Hit& H, const RecWarm& Wm, const RecCold* Cd, const PixelRay& P) {
+    if (!H.direct)
+        return make_float2(Wm.uvs.x + (Wm.uvm.x * H.du + Wm.uvm.y * H.dv) * H.inv,
+                           Wm.uvs.y + (Wm.uvm.z * H.du + Wm.uvm.w * H.dv) * H.inv);
+    const RecCold& C = *Cd;
+    const float3 d = make_float3(P.u, P.v, 1.f);
+    const float3 delta = H.t * (P.idn * d) - f3(C.mu);
+    return make_float2(Wm.uvs.x + dot3(f3(C.um), delta), Wm.uvs.y + dot3(f3(C.vm), delta));
 }
 
 __device__ __forceinline__ float clamp01(float x) {

@@ -23,9 +23,11 @@
 
 namespace gstex {
 
-__device__ __forceinline__ void stage(GaussRec& R, const SceneArgs& a, const View& V, const float3* colors, int gid) {
-    make_record(R, gid, V, a.means[gid], a.quats[gid], make_float2(a.scales[3 * gid], a.scales[3 * gid + 1]), a.glob,
-                a.opac[gid], colors[gid], a.uv0[gid], a.umap[gid], a.vmap[gid], a.dims[gid]);
+__device__ __forceinline__ void stage(const Recs& R, int slot, const SceneArgs& a, const View& V, const float3* colors,
+                                      int gid, bool use_blur) {
+    make_record(R.hot[slot], R.warm[slot], R.cold[slot], gid, V, a.means[gid], a.quats[gid],
+                make_float2(a.scales[3 * gid], a.scales[3 * gid + 1]), a.glob, a.opac[gid], colors[gid], a.uv0[gid],
+                a.umap[gid], a.vmap[gid], a.dims[gid], use_blur);
 }
 
 // All channels of the 4 bilinear corners (C == 3 fast path).
@@ -55,104 +57,148 @@ __device__ __forceinline__ void fetch3(const void* tex, const Bilerp& B, float c
 }
 
 // ---------------------------------------------------------------------------
-// Forward body: one tile
+// Forward body: one tile.  A block of bw x (bw / PPT) threads covers the
+// bw x bw tile; thread (x, y) owns pixels (x, PPT*y + p), p < PPT, so a warp
+// covers a compact 16 x (2*PPT) strip and every staged record read from
+// shared memory is used for PPT pixels.
 // ---------------------------------------------------------------------------
-template <int TEXMODE, int CT>
-__device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, const FwdOut& o, GaussRec* recs) {
-    const int bs = blockDim.x * blockDim.y;
+template <int TEXMODE, int CT, int PPT>
+__device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, const FwdOut& o, const Recs& R) {
+    const int nthr = blockDim.x * blockDim.y;
     const int tr = threadIdx.y * blockDim.x + threadIdx.x;
-    const int pi = J.ty * blockDim.y + threadIdx.y;
-    const int pj = J.tx * blockDim.x + threadIdx.x;
+    const int bw = blockDim.x;
     const View& V = J.V;
-    const PixelRay P = make_pixel(V, pi, pj);
-    const bool inside = pi < J.H && pj < J.W;
-    bool done = !inside;
-    const int2 range = J.range;
-    const int nb = ceil_div(range.y - range.x, bs);
     const bool use_blur = a.settings & (1 << 9);
     const bool use_ndc = a.settings & (1 << 10);
     const bool flip = a.settings & (1 << 15);
     const bool bilinear = !(a.settings & (1 << 2));
     const int C = CT >= 0 ? CT : a.C;
     constexpr int CA = CT > 0 ? CT : (CT == 0 ? 1 : kMaxChannels);
-    float otex[CA];
+    const int pj = J.tx * bw + threadIdx.x;
+    PixelRay P[PPT];
+    bool inside[PPT], done[PPT];
+    float T[PPT], depth[PPT], reg[PPT];
+    int cur[PPT], didx[PPT];
+    float3 out[PPT], nrm[PPT], ts[PPT];
+    float otex[PPT][CA];
+    bool all_done = true;
 #pragma unroll
-    for (int k = 0; k < CA; k++) otex[k] = 0.f;
-    float T = 1.f;
-    int cur = 0, didx = -1;
-    float3 out = make_float3(0.f, 0.f, 0.f), nrm = make_float3(0.f, 0.f, 0.f), ts = make_float3(0.f, 0.f, 0.f);
-    float depth = 0.f, reg = 0.f;
+    for (int p = 0; p < PPT; p++) {
+        const int pi = J.ty * bw + threadIdx.y * PPT + p;
+        P[p] = make_pixel(V, pi, pj);
+        inside[p] = pi < J.H && pj < J.W;
+        done[p] = !inside[p];
+        all_done = all_done && done[p];
+        T[p] = 1.f;
+        depth[p] = 0.f;
+        reg[p] = 0.f;
+        cur[p] = 0;
+        didx[p] = -1;
+        out[p] = nrm[p] = ts[p] = make_float3(0.f, 0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < CA; k++) otex[p][k] = 0.f;
+    }
+    const int2 range = J.range;
+    const int nb = ceil_div(range.y - range.x, nthr);
 
     for (int b = 0; b < nb; ++b) {
-        if (__syncthreads_count(done) >= bs) break;
-        const int bstart = range.x + bs * b;
+        if (__syncthreads_count(all_done) >= nthr) break;
+        const int bstart = range.x + nthr * b;
         const int idx = bstart + tr;
-        if (idx < range.y) stage(recs[tr], a, V, J.colors, a.gids[idx]);
+        if (idx < range.y) stage(R, tr, a, V, J.colors, a.gids[idx], use_blur);
         __syncthreads();
-        const int bsize = min(bs, range.y - bstart);
-        if (done) continue;
+        const int bsize = min(nthr, range.y - bstart);
+        if (all_done) continue;
         for (int k = 0; k < bsize; ++k) {
-            const GaussRec& R = recs[k];
-            const Hit H = intersect(R, P);
-            const float l1s = H.l1 * R.is1, l2s = H.l2 * R.is2;
-            const float sigma = 0.5f * (l1s * l1s + l2s * l2s);
-            float nbf = 1.f, bf = 0.f, sigma_blur = 0.f;
-            if (use_blur) {
-                const float dx = R.bx - P.px, dy = R.by - P.py;
-                sigma_blur = 0.5f * kBlurFsq * (dx * dx + dy * dy);
-                if (sigma_blur < sigma) { bf = 1.f; nbf = 0.f; }
-            }
-            const float alpha = fminf(kAlphaMax, R.opac * (nbf * __expf(-sigma) + bf * __expf(-sigma_blur)));
-            const bool skip = H.t < kTNear || H.t > kTFar || alpha < kAlphaMin;
-            const float next_T = T * (1.f - alpha);
-            if (next_T <= kTDone) { done = true; break; }
-            if (skip) continue;
-            const float vis = alpha * T;
-            out.x = out.x + R.color.x * vis;
-            out.y = out.y + R.color.y * vis;
-            out.z = out.z + R.color.z * vis;
-            float3 hn = R.nw;
-            if (flip && dot3(make_float3(P.u, P.v, 1.f), R.nc) > 0.f) hn = make_float3(-hn.x, -hn.y, -hn.z);
-            nrm.x += vis * hn.x; nrm.y += vis * hn.y; nrm.z += vis * hn.z;
-            if (C > 0) {
-                const Bilerp B = bilerp(R.h, R.w, R.start, clamp01(H.tu), clamp01(H.tv), bilinear);
-                if (CT == 3) {
-                    float c[4][3];
-                    fetch3<TEXMODE>(a.tex, B, c);
+            const float4 hb = R.hot[k].b, hd = R.hot[k].d;
+            bool need = false;
 #pragma unroll
-                    for (int ch = 0; ch < 3; ch++)
-                        otex[ch] += vis * (B.w00 * c[0][ch] + B.w01 * c[1][ch] + B.w10 * c[2][ch] + B.w11 * c[3][ch]);
-                } else if (CT != 0) {
-                    const float* t = (const float*)a.tex;
-                    for (int ch = 0; ch < C; ch++) {
-                        const float v = B.w00 * __ldg(t + (size_t)B.i00 * C + ch) + B.w01 * __ldg(t + (size_t)B.i01 * C + ch) +
-                                        B.w10 * __ldg(t + (size_t)B.i10 * C + ch) + B.w11 * __ldg(t + (size_t)B.i11 * C + ch);
-                        otex[ch] += vis * v;
+            for (int p = 0; p < PPT; p++) {
+                // outside the splat's alpha >= 1/255 box the reference skips the pair; it
+                // can only end the pixel there when T <= 1e-4 * 255/254
+                const bool out_box = P[p].px < hb.z || P[p].px > hb.w || P[p].py < hd.x || P[p].py > hd.y;
+                need = need || (!done[p] && !(out_box && T[p] > 1.01e-4f));
+            }
+            if (!need) continue;
+            const RecHot Hr = R.hot[k];
+#pragma unroll
+            for (int p = 0; p < PPT; p++) {
+                if (done[p]) continue;
+                if (outside_box(Hr, P[p]) && T[p] > 1.01e-4f) continue;
+                const Hit H = intersect(Hr, R.cold + k, P[p]);
+                const float sigma = 0.5f * (H.l1s * H.l1s + H.l2s * H.l2s);
+                float nbf = 1.f, bf = 0.f, sigma_blur = 0.f;
+                if (use_blur) {
+                    const float4 uvs = R.warm[k].uvs;
+                    const float dx = uvs.z - P[p].px, dy = uvs.w - P[p].py;
+                    sigma_blur = 0.5f * kBlurFsq * (dx * dx + dy * dy);
+                    if (sigma_blur < sigma) { bf = 1.f; nbf = 0.f; }
+                }
+                const float alpha = fminf(kAlphaMax, Hr.d.z * (nbf * __expf(-sigma) + bf * __expf(-sigma_blur)));
+                const bool skip = H.t < kTNear || H.t > kTFar || alpha < kAlphaMin;
+                const float next_T = T[p] * (1.f - alpha);
+                if (next_T <= kTDone) { done[p] = true; continue; }
+                if (skip) continue;
+                const RecWarm& Wm = R.warm[k];
+                const float vis = alpha * T[p];
+                const float4 col = Wm.col;
+                out[p].x = out[p].x + col.x * vis;
+                out[p].y = out[p].y + col.y * vis;
+                out[p].z = out[p].z + col.z * vis;
+                float3 hn = f3(Wm.nrm);
+                if (flip && dot3(make_float3(P[p].u, P[p].v, 1.f), f3(R.cold[k].n)) > 0.f)
+                    hn = make_float3(-hn.x, -hn.y, -hn.z);
+                nrm[p].x += vis * hn.x; nrm[p].y += vis * hn.y; nrm[p].z += vis * hn.z;
+                if (C > 0) {
+                    const float2 uv = hit_uv(H, Wm, R.cold + k, P[p]);
+                    const int4 tx = Wm.tex;
+                    const Bilerp B = bilerp(tx.x, tx.y, tx.z, clamp01(uv.x), clamp01(uv.y), bilinear);
+                    if (CT == 3) {
+                        float c[4][3];
+                        fetch3<TEXMODE>(a.tex, B, c);
+#pragma unroll
+                        for (int ch = 0; ch < 3; ch++)
+                            otex[p][ch] += vis * (B.w00 * c[0][ch] + B.w01 * c[1][ch] + B.w10 * c[2][ch] + B.w11 * c[3][ch]);
+                    } else if (CT != 0) {
+                        const float* t = (const float*)a.tex;
+                        for (int ch = 0; ch < C; ch++) {
+                            const float v = B.w00 * __ldg(t + (size_t)B.i00 * C + ch) + B.w01 * __ldg(t + (size_t)B.i01 * C + ch) +
+                                            B.w10 * __ldg(t + (size_t)B.i10 * C + ch) + B.w11 * __ldg(t + (size_t)B.i11 * C + ch);
+                            otex[p][ch] += vis * v;
+                        }
                     }
                 }
+                const float t_view = H.tcam;
+                if (T[p] > 0.5f) { depth[p] = t_view; didx[p] = bstart + k; }
+                const float dv = use_ndc ? (kTFar * t_view - kTFar * kTNear) / ((kTFar - kTNear) * t_view) : H.t;
+                reg[p] += vis * (dv * dv * ts[p].x + ts[p].z - 2.f * dv * ts[p].y);
+                ts[p].x += vis;
+                ts[p].y += vis * dv;
+                ts[p].z += vis * dv * dv;
+                T[p] = next_T;
+                cur[p] = bstart + k;
             }
-            const float t_view = H.tcam;
-            if (T > 0.5f) { depth = t_view; didx = bstart + k; }
-            const float dv = use_ndc ? (kTFar * t_view - kTFar * kTNear) / ((kTFar - kTNear) * t_view) : H.t;
-            reg += vis * (dv * dv * ts.x + ts.z - 2.f * dv * ts.y);
-            ts.x += vis;
-            ts.y += vis * dv;
-            ts.z += vis * dv * dv;
-            T = next_T;
-            cur = bstart + k;
+            bool ad = true;
+#pragma unroll
+            for (int p = 0; p < PPT; p++) ad = ad && done[p];
+            all_done = ad;
+            if (all_done) break;
         }
     }
-    if (inside) {
+#pragma unroll
+    for (int p = 0; p < PPT; p++) {
+        if (!inside[p]) continue;
+        const int pi = J.ty * bw + threadIdx.y * PPT + p;
         const size_t pix = J.pix_base + (size_t)pi * J.W + pj;
-        o.final_T[pix] = T;
-        o.final_idx[pix] = cur;
-        o.depth_idx[pix] = didx;
-        o.img[pix] = make_float3(out.x + T * a.bg[0], out.y + T * a.bg[1], out.z + T * a.bg[2]);
-        o.normal[pix] = nrm;
-        o.depth[pix] = depth;
-        o.reg[pix] = reg;
-        o.reg_s[pix] = ts;
-        for (int ch = 0; ch < C; ch++) o.tex[pix * C + ch] = otex[ch];
+        o.final_T[pix] = T[p];
+        o.final_idx[pix] = cur[p];
+        o.depth_idx[pix] = didx[p];
+        o.img[pix] = make_float3(out[p].x + T[p] * a.bg[0], out[p].y + T[p] * a.bg[1], out[p].z + T[p] * a.bg[2]);
+        o.normal[pix] = nrm[p];
+        o.depth[pix] = depth[p];
+        o.reg[pix] = reg[p];
+        o.reg_s[pix] = ts[p];
+        for (int ch = 0; ch < C; ch++) o.tex[pix * C + ch] = otex[p][ch];
     }
 }
 
@@ -179,20 +225,168 @@ __device__ __forceinline__ T ld_or(const T* p, size_t i, T z) {
     return p ? p[i] : z;
 }
 
-template <int TEXMODE, int CT>
-__device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, const BwdArgs& g, GaussRec* recs,
+// Per-pixel state of the backward walk.
+template <int CA>
+struct BwdPix {
+    PixelRay P;
+    bool inside;
+    float T, vT_run;
+    float3 sfin, vout, vnorm;
+    int dfin, bfin;
+    float vdepth, vreg;
+    float vtex[CA];
+};
+
+// Adjoint of one (pixel, Gaussian) pair; adds its moments to m and returns
+// false when the pair is skipped.  Follows csrc/texture.cu:577-708.
+template <int TEXMODE, int CT, int CA>
+__device__ __forceinline__ void bwd_pair(const SceneArgs& a, const BwdArgs& g, const Recs& R, int k, int gidx,
+                                         const RecHot& Hr, const Hit& H, float alpha, float e, float eb, float nbf,
+                                         float bf, BwdPix<CA>& S, int C, bool use_ndc, bool prop_uv, bool bilinear,
+                                         float (&m)[32]) {
+    const RecWarm& Wm = R.warm[k];
+    const float4 col = Wm.col, nw = Wm.nrm;
+    const float is1 = col.w, is2 = nw.w;
+    const PixelRay& P = S.P;
+    S.T = __fdividef(S.T, 1.f - alpha);
+    const float T = S.T;
+    const float vis = alpha * T;
+    const float3 vout = S.vout, vnorm = S.vnorm;
+    float v_vis = col.x * vout.x + col.y * vout.y + col.z * vout.z + nw.x * vnorm.x + nw.y * vnorm.y + nw.z * vnorm.z;
+    float v_u = 0.f, v_v = 0.f;
+    if (C > 0) {
+        const float2 uv = hit_uv(H, Wm, R.cold + k, P);
+        const int4 tx = Wm.tex;
+        const Bilerp B = bilerp(tx.x, tx.y, tx.z, clamp01(uv.x), clamp01(uv.y), bilinear);
+        const float fh = (float)tx.x, fw = (float)tx.y;
+        if (CT == 3) {
+            float c[4][3];
+            fetch3<TEXMODE>(a.tex, B, c);
+            float gv[3];
+#pragma unroll
+            for (int ch = 0; ch < 3; ch++) {
+                const float val = B.w00 * c[0][ch] + B.w01 * c[1][ch] + B.w10 * c[2][ch] + B.w11 * c[3][ch];
+                const float vv = vis * S.vtex[ch];
+                gv[ch] = vv;
+                if (bilinear && prop_uv) {
+                    v_u += fh * (vv * (-(1.f - B.fy) * c[0][ch] - B.fy * c[1][ch] + (1.f - B.fy) * c[2][ch] + B.fy * c[3][ch]));
+                    v_v += fw * (vv * (-(1.f - B.fx) * c[0][ch] + (1.f - B.fx) * c[1][ch] - B.fx * c[2][ch] + B.fx * c[3][ch]));
+                }
+                v_vis += val * S.vtex[ch];
+            }
+            if (gv[0] != 0.f || gv[1] != 0.f || gv[2] != 0.f) {
+                const int rows[4] = { B.i00, B.i01, B.i10, B.i11 };
+                const float wts[4] = { B.w00, B.w01, B.w10, B.w11 };
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    if (wts[q] == 0.f) continue;
+                    if (TEXMODE == 1) {
+                        atomicAdd(reinterpret_cast<float4*>(g.v_texgrad) + rows[q],
+                                  make_float4(wts[q] * gv[0], wts[q] * gv[1], wts[q] * gv[2], 0.f));
+                    } else {
+                        float* dst = g.v_texgrad + 3 * (size_t)rows[q];
+                        atomicAdd(dst + 0, wts[q] * gv[0]);
+                        atomicAdd(dst + 1, wts[q] * gv[1]);
+                        atomicAdd(dst + 2, wts[q] * gv[2]);
+                    }
+                }
+            }
+        } else if (CT != 0) {
+            const float* t = (const float*)a.tex;
+            for (int ch = 0; ch < C; ch++) {
+                const float c00 = __ldg(t + (size_t)B.i00 * C + ch), c01 = __ldg(t + (size_t)B.i01 * C + ch);
+                const float c10 = __ldg(t + (size_t)B.i10 * C + ch), c11 = __ldg(t + (size_t)B.i11 * C + ch);
+                const float val = B.w00 * c00 + B.w01 * c01 + B.w10 * c10 + B.w11 * c11;
+                const float vv = vis * S.vtex[ch];
+                if (vv != 0.f) {
+                    if (B.w00 != 0.f) atomicAdd(g.v_texgrad + (size_t)B.i00 * C + ch, B.w00 * vv);
+                    if (B.w01 != 0.f) atomicAdd(g.v_texgrad + (size_t)B.i01 * C + ch, B.w01 * vv);
+                    if (B.w10 != 0.f) atomicAdd(g.v_texgrad + (size_t)B.i10 * C + ch, B.w10 * vv);
+                    if (B.w11 != 0.f) atomicAdd(g.v_texgrad + (size_t)B.i11 * C + ch, B.w11 * vv);
+                }
+                if (bilinear && prop_uv) {
+                    v_u += fh * (vv * (-(1.f - B.fy) * c00 - B.fy * c01 + (1.f - B.fy) * c10 + B.fy * c11));
+                    v_v += fw * (vv * (-(1.f - B.fx) * c00 + (1.f - B.fx) * c01 - B.fx * c10 + B.fx * c11));
+                }
+                v_vis += val * S.vtex[ch];
+            }
+        }
+    }
+    const float vT_run = S.vT_run;
+    float v_alpha = T * v_vis - T * vT_run;
+    float vT_cur = alpha * v_vis + (1.f - alpha) * vT_run;
+    const float t_view = H.tcam;
+    const float3 sfin = S.sfin;
+    float v_t = 0.f, v_t_ndc = 0.f, v_w = 0.f;
+    if (use_ndc) {
+        const float t_ndc = (kTFar * t_view - kTFar * kTNear) / ((kTFar - kTNear) * t_view);
+        v_t_ndc = 2.f * (vis * t_ndc * sfin.x - vis * sfin.y) * S.vreg;
+        v_w = (t_ndc * t_ndc * sfin.x - 2.f * t_ndc * sfin.y + sfin.z) * S.vreg;
+    } else {
+        v_t = 2.f * (vis * H.t * sfin.x - vis * sfin.y) * S.vreg;
+        v_w = (H.t * H.t * sfin.x - 2.f * H.t * sfin.y + sfin.z) * S.vreg;
+    }
+    v_alpha += v_w * T;
+    vT_cur += v_w * alpha;
+    S.vT_run = vT_cur;
+    const float v_sigma = -nbf * Hr.d.z * e * v_alpha;
+    // sigma = (l1s^2 + l2s^2) / 2 with l_ks = l_k * is_k
+    const float l1 = __fdividef(H.l1s, is1), l2 = __fdividef(H.l2s, is2);
+    const float v_l1 = H.l1s * is1 * v_sigma;
+    const float v_l2 = H.l2s * is2 * v_sigma;
+    const RecCold& Cd = R.cold[k];
+    const float ra1 = (Cd.a1.x * P.u + Cd.a1.y * P.v + Cd.a1.z) * P.idn;
+    const float ra2 = (Cd.a2.x * P.u + Cd.a2.y * P.v + Cd.a2.z) * P.idn;
+    v_t += v_l1 * ra1 + v_l2 * ra2;
+    if (prop_uv) {
+        const float rum = (Cd.um.x * P.u + Cd.um.y * P.v + Cd.um.z) * P.idn;
+        const float rvm = (Cd.vm.x * P.u + Cd.vm.y * P.v + Cd.vm.z) * P.idn;
+        v_t += v_u * rum + v_v * rvm;
+    }
+    float v_t_view = 0.f;
+    if (gidx == S.dfin && S.dfin != -1) v_t_view += S.vdepth;
+    if (use_ndc) v_t_view += (kTFar * kTNear) / ((kTFar - kTNear) * t_view * t_view) * v_t_ndc;
+    v_t += P.idn * v_t_view;
+    const float vtd = v_t * (P.dn * H.inv);  // v_t / (n . r)
+    const float v_sb = -bf * Hr.d.z * eb * v_alpha;
+    m[0] += vis * vout.x;
+    m[1] += vis * vout.y;
+    m[2] += vis * vout.z;
+    m[3] += (nbf * e + bf * eb) * v_alpha;
+    m[4] += -(H.l1s * H.l1s) * v_sigma * is1 * a.glob;
+    m[5] += -(H.l2s * H.l2s) * v_sigma * is2 * a.glob;
+    m[6] += v_l1;
+    m[7] += v_l2;
+    m[8] += vtd;
+    m[9] += l1 * v_l1;
+    m[10] += l2 * v_l1;
+    m[11] += l1 * v_l2;
+    m[12] += l2 * v_l2;
+    m[13] += l1 * vtd;
+    m[14] += l2 * vtd;
+    m[15] += vis * vnorm.x;
+    m[16] += vis * vnorm.y;
+    m[17] += vis * vnorm.z;
+    m[18] += v_u;
+    m[19] += v_v;
+    m[20] += l1 * v_u;
+    m[21] += l2 * v_u;
+    m[22] += l1 * v_v;
+    m[23] += l2 * v_v;
+    m[24] += kBlurFsq * v_sb * (Wm.uvs.z - P.px);
+    m[25] += kBlurFsq * v_sb * (Wm.uvs.w - P.py);
+}
+
+template <int TEXMODE, int CT, int PPT>
+__device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, const BwdArgs& g, const Recs& R,
                                          float* smom) {
-    const int bs = blockDim.x * blockDim.y;
+    const int nthr = blockDim.x * blockDim.y;
     const int tr = threadIdx.y * blockDim.x + threadIdx.x;
+    const int bw = blockDim.x;
     const unsigned lane = tr & 31;
     const unsigned wmask = __activemask();
     const bool full_warp = wmask == 0xffffffffu;
-    const int pi = J.ty * blockDim.y + threadIdx.y;
-    const int pj = J.tx * blockDim.x + threadIdx.x;
     const View& V = J.V;
-    const PixelRay P = make_pixel(V, pi, pj);
-    const bool inside = pi < J.H && pj < J.W;
-    const size_t pix = inside ? J.pix_base + (size_t)pi * J.W + pj : 0;
     const bool use_blur = a.settings & (1 << 9);
     const bool use_ndc = a.settings & (1 << 10);
     const bool prop_uv = a.settings & (1 << 8);
@@ -200,181 +394,94 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
     const int C = CT >= 0 ? CT : a.C;
     constexpr int CA = CT > 0 ? CT : (CT == 0 ? 1 : kMaxChannels);
     const float3 z3 = make_float3(0.f, 0.f, 0.f);
-
-    float T = inside ? g.final_T[pix] : 1.f;
-    const float3 sfin = inside ? g.reg_s[pix] : z3;
-    const int dfin = inside ? g.depth_idx[pix] : -1;
-    const int bfin = inside ? g.final_idx[pix] : 0;
-    const float3 vout = inside ? ld_or(g.v_img, pix, z3) : z3;
-    const float vdepth = inside ? ld_or(g.v_depth, pix, 0.f) : 0.f;
-    const float vreg = inside ? ld_or(g.v_reg, pix, 0.f) : 0.f;
-    const float valph = inside ? ld_or(g.v_alpha, pix, 0.f) : 0.f;
-    const float3 vnorm = inside ? ld_or(g.v_normal, pix, z3) : z3;
-    float vtex[CA];
-    for (int ch = 0; ch < CA; ch++) vtex[ch] = (inside && ch < C && g.v_tex) ? g.v_tex[pix * C + ch] : 0.f;
-    float vT_run = a.bg[0] * vout.x + a.bg[1] * vout.y + a.bg[2] * vout.z - valph;
-    const int warp_bfin = __reduce_max_sync(wmask, bfin);
+    const int pj = J.tx * bw + threadIdx.x;
+    BwdPix<CA> S[PPT];
+    int my_bfin = -1;
+#pragma unroll
+    for (int p = 0; p < PPT; p++) {
+        const int pi = J.ty * bw + threadIdx.y * PPT + p;
+        BwdPix<CA>& s = S[p];
+        s.P = make_pixel(V, pi, pj);
+        s.inside = pi < J.H && pj < J.W;
+        const size_t pix = s.inside ? J.pix_base + (size_t)pi * J.W + pj : 0;
+        s.T = s.inside ? g.final_T[pix] : 1.f;
+        s.sfin = s.inside ? g.reg_s[pix] : z3;
+        s.dfin = s.inside ? g.depth_idx[pix] : -1;
+        s.bfin = s.inside ? g.final_idx[pix] : 0;
+        s.vout = s.inside ? ld_or(g.v_img, pix, z3) : z3;
+        s.vdepth = s.inside ? ld_or(g.v_depth, pix, 0.f) : 0.f;
+        s.vreg = s.inside ? ld_or(g.v_reg, pix, 0.f) : 0.f;
+        const float valph = s.inside ? ld_or(g.v_alpha, pix, 0.f) : 0.f;
+        s.vnorm = s.inside ? ld_or(g.v_normal, pix, z3) : z3;
+        for (int ch = 0; ch < CA; ch++) s.vtex[ch] = (s.inside && ch < C && g.v_tex) ? g.v_tex[pix * C + ch] : 0.f;
+        s.vT_run = a.bg[0] * s.vout.x + a.bg[1] * s.vout.y + a.bg[2] * s.vout.z - valph;
+        if (s.inside) my_bfin = max(my_bfin, s.bfin);
+    }
+    const int warp_bfin = __reduce_max_sync(wmask, my_bfin);
 
     const int2 range = J.range;
-    const int nb = ceil_div(range.y - range.x, bs);
+    const int nb = ceil_div(range.y - range.x, nthr);
     for (int b = 0; b < nb; ++b) {
         __syncthreads();
-        const int bend = range.y - 1 - bs * b;
-        const int bsize = min(bs, bend + 1 - range.x);
+        const int bend = range.y - 1 - nthr * b;
+        const int bsize = min(nthr, bend + 1 - range.x);
         const int idx = bend - tr;
-        if (idx >= range.x) stage(recs[tr], a, V, J.colors, a.gids[idx]);
-        for (int q = tr; q < bs * kMoments; q += bs) smom[q] = 0.f;
+        if (idx >= range.x) stage(R, tr, a, V, J.colors, a.gids[idx], use_blur);
+        for (int q = tr; q < nthr * kMoments; q += nthr) smom[q] = 0.f;
         __syncthreads();
         for (int k = max(0, bend - warp_bfin); k < bsize; ++k) {
             const int gidx = bend - k;
-            bool valid = inside && gidx <= bfin;
-            const GaussRec& R = recs[k];
-            Hit H;
-            float l1s = 0.f, l2s = 0.f, e = 0.f, eb = 0.f, nbf = 1.f, bf = 0.f, alpha = 0.f;
-            if (valid) {
-                H = intersect(R, P);
-                l1s = H.l1 * R.is1;
-                l2s = H.l2 * R.is2;
-                const float sigma = 0.5f * (l1s * l1s + l2s * l2s);
-                float sigma_blur = 0.f;
-                if (use_blur) {
-                    const float dx = R.bx - P.px, dy = R.by - P.py;
-                    sigma_blur = 0.5f * kBlurFsq * (dx * dx + dy * dy);
-                    if (sigma_blur < sigma) { bf = 1.f; nbf = 0.f; }
-                }
-                e = __expf(-sigma);
-                eb = use_blur ? __expf(-sigma_blur) : 0.f;
-                alpha = fminf(kAlphaMax, R.opac * (nbf * e + bf * eb));
-                if (H.t < kTNear || H.t > kTFar || alpha < kAlphaMin) valid = false;
+            {
+                const float4 hb = R.hot[k].b, hd = R.hot[k].d;
+                bool need = false;
+#pragma unroll
+                for (int p = 0; p < PPT; p++)
+                    need = need || (S[p].inside && gidx <= S[p].bfin &&
+                                    !(S[p].P.px < hb.z || S[p].P.px > hb.w || S[p].P.py < hd.x || S[p].P.py > hd.y));
+                if (!__any_sync(wmask, need)) continue;
             }
-            if (!__any_sync(wmask, valid)) continue;
+            const RecHot Hr = R.hot[k];
+            bool valid[PPT];
+            Hit H[PPT];
+            float e[PPT], eb[PPT], nbf[PPT], bf[PPT], alpha[PPT];
+            bool any = false;
+#pragma unroll
+            for (int p = 0; p < PPT; p++) {
+                valid[p] = S[p].inside && gidx <= S[p].bfin && !outside_box(Hr, S[p].P);
+                e[p] = eb[p] = alpha[p] = bf[p] = 0.f;
+                nbf[p] = 1.f;
+                if (valid[p]) {
+                    H[p] = intersect(Hr, R.cold + k, S[p].P);
+                    const float sigma = 0.5f * (H[p].l1s * H[p].l1s + H[p].l2s * H[p].l2s);
+                    float sigma_blur = 0.f;
+                    if (use_blur) {
+                        const float4 uvs = R.warm[k].uvs;
+                        const float dx = uvs.z - S[p].P.px, dy = uvs.w - S[p].P.py;
+                        sigma_blur = 0.5f * kBlurFsq * (dx * dx + dy * dy);
+                        if (sigma_blur < sigma) { bf[p] = 1.f; nbf[p] = 0.f; }
+                    }
+                    e[p] = __expf(-sigma);
+                    eb[p] = use_blur ? __expf(-sigma_blur) : 0.f;
+                    alpha[p] = fminf(kAlphaMax, Hr.d.z * (nbf[p] * e[p] + bf[p] * eb[p]));
+                    if (H[p].t < kTNear || H[p].t > kTFar || alpha[p] < kAlphaMin) valid[p] = false;
+                }
+                any = any || valid[p];
+            }
+            const unsigned vmask = __ballot_sync(wmask, any);
+            if (!vmask) continue;
             float m[32];
 #pragma unroll
             for (int q = 0; q < 32; q++) m[q] = 0.f;
-            if (valid) {
-                T = T * __frcp_rn(1.f - alpha);
-                const float vis = alpha * T;
-                float v_vis = R.color.x * vout.x + R.color.y * vout.y + R.color.z * vout.z + dot3(R.nw, vnorm);
-                float v_u = 0.f, v_v = 0.f;
-                if (C > 0) {
-                    const Bilerp B = bilerp(R.h, R.w, R.start, clamp01(H.tu), clamp01(H.tv), bilinear);
-                    if (CT == 3) {
-                        float c[4][3];
-                        fetch3<TEXMODE>(a.tex, B, c);
-                        float gv[3];
 #pragma unroll
-                        for (int ch = 0; ch < 3; ch++) {
-                            const float val = B.w00 * c[0][ch] + B.w01 * c[1][ch] + B.w10 * c[2][ch] + B.w11 * c[3][ch];
-                            const float vv = vis * vtex[ch];
-                            gv[ch] = vv;
-                            if (bilinear && prop_uv) {
-                                v_u += (float)R.h * (vv * (-(1.f - B.fy) * c[0][ch] - B.fy * c[1][ch] + (1.f - B.fy) * c[2][ch] + B.fy * c[3][ch]));
-                                v_v += (float)R.w * (vv * (-(1.f - B.fx) * c[0][ch] + (1.f - B.fx) * c[1][ch] - B.fx * c[2][ch] + B.fx * c[3][ch]));
-                            }
-                            v_vis += val * vtex[ch];
-                        }
-                        if (gv[0] != 0.f || gv[1] != 0.f || gv[2] != 0.f) {
-                            const int rows[4] = { B.i00, B.i01, B.i10, B.i11 };
-                            const float wts[4] = { B.w00, B.w01, B.w10, B.w11 };
-#pragma unroll
-                            for (int q = 0; q < 4; q++) {
-                                if (wts[q] == 0.f) continue;
-                                if (TEXMODE == 1) {
-                                    atomicAdd(reinterpret_cast<float4*>(g.v_texgrad) + rows[q],
-                                              make_float4(wts[q] * gv[0], wts[q] * gv[1], wts[q] * gv[2], 0.f));
-                                } else {
-                                    float* dst = g.v_texgrad + 3 * (size_t)rows[q];
-                                    atomicAdd(dst + 0, wts[q] * gv[0]);
-                                    atomicAdd(dst + 1, wts[q] * gv[1]);
-                                    atomicAdd(dst + 2, wts[q] * gv[2]);
-                                }
-                            }
-                        }
-                    } else if (CT != 0) {
-                        const float* t = (const float*)a.tex;
-                        for (int ch = 0; ch < C; ch++) {
-                            const float c00 = __ldg(t + (size_t)B.i00 * C + ch), c01 = __ldg(t + (size_t)B.i01 * C + ch);
-                            const float c10 = __ldg(t + (size_t)B.i10 * C + ch), c11 = __ldg(t + (size_t)B.i11 * C + ch);
-                            const float val = B.w00 * c00 + B.w01 * c01 + B.w10 * c10 + B.w11 * c11;
-                            const float vv = vis * vtex[ch];
-                            if (vv != 0.f) {
-                                if (B.w00 != 0.f) atomicAdd(g.v_texgrad + (size_t)B.i00 * C + ch, B.w00 * vv);
-                                if (B.w01 != 0.f) atomicAdd(g.v_texgrad + (size_t)B.i01 * C + ch, B.w01 * vv);
-                                if (B.w10 != 0.f) atomicAdd(g.v_texgrad + (size_t)B.i10 * C + ch, B.w10 * vv);
-                                if (B.w11 != 0.f) atomicAdd(g.v_texgrad + (size_t)B.i11 * C + ch, B.w11 * vv);
-                            }
-                            if (bilinear && prop_uv) {
-                                v_u += (float)R.h * (vv * (-(1.f - B.fy) * c00 - B.fy * c01 + (1.f - B.fy) * c10 + B.fy * c11));
-                                v_v += (float)R.w * (vv * (-(1.f - B.fx) * c00 + (1.f - B.fx) * c01 - B.fx * c10 + B.fx * c11));
-                            }
-                            v_vis += val * vtex[ch];
-                        }
-                    }
-                }
-                float v_alpha = T * v_vis - T * vT_run;
-                float vT_cur = alpha * v_vis + (1.f - alpha) * vT_run;
-                const float t_view = H.tcam;
-                float v_t = 0.f, v_t_ndc = 0.f, v_w = 0.f;
-                if (use_ndc) {
-                    const float t_ndc = (kTFar * t_view - kTFar * kTNear) / ((kTFar - kTNear) * t_view);
-                    v_t_ndc = 2.f * (vis * t_ndc * sfin.x - vis * sfin.y) * vreg;
-                    v_w = (t_ndc * t_ndc * sfin.x - 2.f * t_ndc * sfin.y + sfin.z) * vreg;
-                } else {
-                    v_t = 2.f * (vis * H.t * sfin.x - vis * sfin.y) * vreg;
-                    v_w = (H.t * H.t * sfin.x - 2.f * H.t * sfin.y + sfin.z) * vreg;
-                }
-                v_alpha += v_w * T;
-                vT_cur += v_w * alpha;
-                vT_run = vT_cur;
-                const float v_sigma = -nbf * R.opac * e * v_alpha;
-                const float v_l1 = H.l1 * R.is1 * R.is1 * v_sigma;
-                const float v_l2 = H.l2 * R.is2 * R.is2 * v_sigma;
-                const float ra1 = (R.a1c.x * P.u + R.a1c.y * P.v + R.a1c.z) * P.idn;
-                const float ra2 = (R.a2c.x * P.u + R.a2c.y * P.v + R.a2c.z) * P.idn;
-                v_t += v_l1 * ra1 + v_l2 * ra2;
-                if (prop_uv) {
-                    const float rum = (R.umc.x * P.u + R.umc.y * P.v + R.umc.z) * P.idn;
-                    const float rvm = (R.vmc.x * P.u + R.vmc.y * P.v + R.vmc.z) * P.idn;
-                    v_t += v_u * rum + v_v * rvm;
-                }
-                float v_t_view = 0.f;
-                if (gidx == dfin && dfin != -1) v_t_view += vdepth;
-                if (use_ndc) v_t_view += (kTFar * kTNear) / ((kTFar - kTNear) * t_view * t_view) * v_t_ndc;
-                v_t += P.idn * v_t_view;
-                const float vtd = v_t * (P.dn * H.inv);  // v_t / (n . r)
-                const float v_sb = -bf * R.opac * eb * v_alpha;
-                m[0] = vis * vout.x;
-                m[1] = vis * vout.y;
-                m[2] = vis * vout.z;
-                m[3] = (nbf * e + bf * eb) * v_alpha;
-                m[4] = -(l1s * l1s) * v_sigma * R.is1 * a.glob;
-                m[5] = -(l2s * l2s) * v_sigma * R.is2 * a.glob;
-                m[6] = v_l1;
-                m[7] = v_l2;
-                m[8] = vtd;
-                m[9] = H.l1 * v_l1;
-                m[10] = H.l2 * v_l1;
-                m[11] = H.l1 * v_l2;
-                m[12] = H.l2 * v_l2;
-                m[13] = H.l1 * vtd;
-                m[14] = H.l2 * vtd;
-                m[15] = vis * vnorm.x;
-                m[16] = vis * vnorm.y;
-                m[17] = vis * vnorm.z;
-                m[18] = v_u;
-                m[19] = v_v;
-                m[20] = H.l1 * v_u;
-                m[21] = H.l2 * v_u;
-                m[22] = H.l1 * v_v;
-                m[23] = H.l2 * v_v;
-                m[24] = kBlurFsq * v_sb * (R.bx - P.px);
-                m[25] = kBlurFsq * v_sb * (R.by - P.py);
-            }
+            for (int p = 0; p < PPT; p++)
+                if (valid[p])
+                    bwd_pair<TEXMODE, CT, CA>(a, g, R, k, gidx, Hr, H[p], alpha[p], e[p], eb[p], nbf[p], bf[p], S[p],
+                                              C, use_ndc, prop_uv, bilinear, m);
             float* dst = smom + k * kMoments;
             if (full_warp) {
                 const float s = warp_transpose_reduce(m, lane);
                 if (lane < (unsigned)kMoments) atomicAdd(dst + lane, s);
-            } else if (valid) {
+            } else if (any) {
 #pragma unroll
                 for (int q = 0; q < kMoments; q++) atomicAdd(dst + q, m[q]);
             }
@@ -386,14 +493,14 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
 #pragma unroll
             for (int q = 0; q < kMoments; q++) any |= sm[q] != 0.f;
             if (any) {
-                const GaussRec& R = recs[tr];
-                float* vc = J.vcolors + 3 * (size_t)R.gid;
+                const int gid = R.warm[tr].tex.w;
+                float* vc = J.vcolors + 3 * (size_t)gid;
                 atomicAdd(vc + 0, sm[0]);
                 atomicAdd(vc + 1, sm[1]);
                 atomicAdd(vc + 2, sm[2]);
-                float4* dst = reinterpret_cast<float4*>(g.moments + (size_t)R.gid * kMomStride);
+                float4* dst = reinterpret_cast<float4*>(g.moments + (size_t)gid * kMomStride);
                 // blur moments -> world-space mean gradient (helpers.cuh:155-164, 114-121)
-                const float3 p = R.mu_c;
+                const float3 p = f3(R.cold[tr].mu);
                 const float rw = 1.f / (p.z + 1e-6f);
                 const float vx = V.fx * sm[24], vy = V.fy * sm[25];
                 const float3 vmb = V.rot_t(make_float3(vx * rw, vy * rw, -(vx * p.x + vy * p.y) * rw * rw));
@@ -412,8 +519,18 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
 // ---------------------------------------------------------------------------
 // Launch forms
 // ---------------------------------------------------------------------------
-template <int TEXMODE, int CT>
-__global__ void __launch_bounds__(256) fwd_view_kernel(SceneArgs a, ViewArgs va, FwdOut o) {
+// Minimum resident CTAs per SM asked of the register allocator.
+#ifndef GSTEX_FWD_MINB
+#define GSTEX_FWD_MINB 5
+#endif
+#ifndef GSTEX_BWD_MINB
+#define GSTEX_BWD_MINB 4
+#endif
+#define FWD_BOUNDS(PPT) __launch_bounds__((PPT) == 2 ? 128 : 256, (PPT) == 2 ? GSTEX_FWD_MINB : 3)
+#define BWD_BOUNDS(PPT) __launch_bounds__((PPT) == 2 ? 128 : 256, (PPT) == 2 ? GSTEX_BWD_MINB : 2)
+
+template <int TEXMODE, int CT, int PPT>
+__global__ void FWD_BOUNDS(PPT) fwd_view_kernel(SceneArgs a, ViewArgs va, FwdOut o) {
     extern __shared__ __align__(16) unsigned char smem[];
     TileJob J;
     J.V = load_view(va.viewmat, va.fx, va.fy, va.cx, va.cy);
@@ -423,13 +540,13 @@ __global__ void __launch_bounds__(256) fwd_view_kernel(SceneArgs a, ViewArgs va,
     J.pix_base = 0;
     J.colors = va.colors;
     J.vcolors = nullptr;
-    fwd_tile<TEXMODE, CT>(a, J, o, reinterpret_cast<GaussRec*>(smem));
+    fwd_tile<TEXMODE, CT, PPT>(a, J, o, Recs::carve(smem, blockDim.x * blockDim.y));
 }
 
-template <int TEXMODE, int CT>
-__global__ void __launch_bounds__(256) bwd_view_kernel(SceneArgs a, ViewArgs va, BwdArgs g) {
+template <int TEXMODE, int CT, int PPT>
+__global__ void BWD_BOUNDS(PPT) bwd_view_kernel(SceneArgs a, ViewArgs va, BwdArgs g) {
     extern __shared__ __align__(16) unsigned char smem[];
-    const int bs = blockDim.x * blockDim.y;
+    const int nthr = blockDim.x * blockDim.y;
     TileJob J;
     J.V = load_view(va.viewmat, va.fx, va.fy, va.cx, va.cy);
     J.W = va.W; J.H = va.H;
@@ -438,8 +555,7 @@ __global__ void __launch_bounds__(256) bwd_view_kernel(SceneArgs a, ViewArgs va,
     J.pix_base = 0;
     J.colors = va.colors;
     J.vcolors = va.vcolors;
-    bwd_tile<TEXMODE, CT>(a, J, g, reinterpret_cast<GaussRec*>(smem),
-                          reinterpret_cast<float*>(smem + sizeof(GaussRec) * bs));
+    bwd_tile<TEXMODE, CT, PPT>(a, J, g, Recs::carve(smem, nthr), reinterpret_cast<float*>(smem + (size_t)kRecBytes * nthr));
 }
 
 __device__ __forceinline__ bool next_job(const BatchArgs& ba, int* s_tile, TileJob& J) {
@@ -463,23 +579,24 @@ __device__ __forceinline__ bool next_job(const BatchArgs& ba, int* s_tile, TileJ
     return true;
 }
 
-template <int TEXMODE, int CT>
-__global__ void __launch_bounds__(256) fwd_batch_kernel(SceneArgs a, BatchArgs ba, FwdOut o) {
+template <int TEXMODE, int CT, int PPT>
+__global__ void FWD_BOUNDS(PPT) fwd_batch_kernel(SceneArgs a, BatchArgs ba, FwdOut o) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_tile;
     TileJob J;
-    while (next_job(ba, &s_tile, J)) fwd_tile<TEXMODE, CT>(a, J, o, reinterpret_cast<GaussRec*>(smem));
+    const Recs R = Recs::carve(smem, blockDim.x * blockDim.y);
+    while (next_job(ba, &s_tile, J)) fwd_tile<TEXMODE, CT, PPT>(a, J, o, R);
 }
 
-template <int TEXMODE, int CT>
-__global__ void __launch_bounds__(256) bwd_batch_kernel(SceneArgs a, BatchArgs ba, BwdArgs g) {
+template <int TEXMODE, int CT, int PPT>
+__global__ void BWD_BOUNDS(PPT) bwd_batch_kernel(SceneArgs a, BatchArgs ba, BwdArgs g) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_tile;
-    const int bs = blockDim.x * blockDim.y;
+    const int nthr = blockDim.x * blockDim.y;
     TileJob J;
-    while (next_job(ba, &s_tile, J))
-        bwd_tile<TEXMODE, CT>(a, J, g, reinterpret_cast<GaussRec*>(smem),
-                              reinterpret_cast<float*>(smem + sizeof(GaussRec) * bs));
+    const Recs R = Recs::carve(smem, nthr);
+    float* smom = reinterpret_cast<float*>(smem + (size_t)kRecBytes * nthr);
+    while (next_job(ba, &s_tile, J)) bwd_tile<TEXMODE, CT, PPT>(a, J, g, R, smom);
 }
 
 // Moments -> parameter gradients (one thread per Gaussian).  Colour gradients
@@ -557,19 +674,29 @@ int fill_scene(const gstex_raster_inputs* in, SceneArgs& a) {
 }
 
 // Kernel tables ------------------------------------------------------------
-template <template <int, int> class Sel>
-static typename Sel<0, 0>::type pick(int C, int texmode) {
-    if (C == 0) return Sel<0, 0>::get();
-    if (C == 3) return texmode == 1 ? Sel<1, 3>::get() : Sel<0, 3>::get();
-    return Sel<0, -1>::get();
-}
-template <int M, int C> struct FwdView { typedef void (*type)(SceneArgs, ViewArgs, FwdOut); static type get() { return fwd_view_kernel<M, C>; } };
-template <int M, int C> struct BwdView { typedef void (*type)(SceneArgs, ViewArgs, BwdArgs); static type get() { return bwd_view_kernel<M, C>; } };
-template <int M, int C> struct FwdBatch { typedef void (*type)(SceneArgs, BatchArgs, FwdOut); static type get() { return fwd_batch_kernel<M, C>; } };
-template <int M, int C> struct BwdBatch { typedef void (*type)(SceneArgs, BatchArgs, BwdArgs); static type get() { return bwd_batch_kernel<M, C>; } };
+// Pixels per thread: 1 (block bw x bw) or 2 (block bw x bw/2, even bw only).
+int ppt_of(int bw, int requested) { return (requested == 2 && bw % 2 == 0) ? 2 : 1; }
 
-size_t fwd_smem(int bw) { return sizeof(GaussRec) * bw * bw; }
-size_t bwd_smem(int bw) { return (sizeof(GaussRec) + kMoments * sizeof(float)) * bw * bw; }
+template <template <int, int, int> class Sel>
+static typename Sel<0, 0, 1>::type pick(int C, int texmode, int ppt) {
+    if (ppt == 2) {
+        if (C == 0) return Sel<0, 0, 2>::get();
+        if (C == 3) return texmode == 1 ? Sel<1, 3, 2>::get() : Sel<0, 3, 2>::get();
+        return Sel<0, -1, 2>::get();
+    }
+    if (C == 0) return Sel<0, 0, 1>::get();
+    if (C == 3) return texmode == 1 ? Sel<1, 3, 1>::get() : Sel<0, 3, 1>::get();
+    return Sel<0, -1, 1>::get();
+}
+template <int M, int C, int P> struct FwdView { typedef void (*type)(SceneArgs, ViewArgs, FwdOut); static type get() { return fwd_view_kernel<M, C, P>; } };
+template <int M, int C, int P> struct BwdView { typedef void (*type)(SceneArgs, ViewArgs, BwdArgs); static type get() { return bwd_view_kernel<M, C, P>; } };
+template <int M, int C, int P> struct FwdBatch { typedef void (*type)(SceneArgs, BatchArgs, FwdOut); static type get() { return fwd_batch_kernel<M, C, P>; } };
+template <int M, int C, int P> struct BwdBatch { typedef void (*type)(SceneArgs, BatchArgs, BwdArgs); static type get() { return bwd_batch_kernel<M, C, P>; } };
+
+static dim3 block_of(int bw, int ppt) { return dim3(bw, bw / ppt); }
+static int threads_of(int bw, int ppt) { return bw * (bw / ppt); }
+size_t fwd_smem(int bw, int ppt) { return (size_t)kRecBytes * threads_of(bw, ppt); }
+size_t bwd_smem(int bw, int ppt) { return ((size_t)kRecBytes + kMoments * sizeof(float)) * threads_of(bw, ppt); }
 
 int launch_finalize(const SceneArgs& a, const float* moments, float* v_opac, float* v_means, float* v_scales,
                     float* v_quats, float* v_uv0, float* v_umap, float* v_vmap, cudaStream_t stream) {
@@ -580,35 +707,38 @@ int launch_finalize(const SceneArgs& a, const float* moments, float* v_opac, flo
     return check_launch("finalize");
 }
 
-int launch_fwd_batch(const SceneArgs& a, const BatchArgs& ba, const FwdOut& o, int bw, int texmode, int grid,
+int launch_fwd_batch(const SceneArgs& a, const BatchArgs& ba, const FwdOut& o, int bw, int texmode, int ppt, int grid,
                      cudaStream_t stream) {
-    auto k = pick<FwdBatch>(a.C, texmode);
-    int rc = set_smem(k, fwd_smem(bw), "batch forward");
+    ppt = ppt_of(bw, ppt);
+    auto k = pick<FwdBatch>(a.C, texmode, ppt);
+    int rc = set_smem(k, fwd_smem(bw, ppt), "batch forward");
     if (rc) return rc;
-    k<<<grid, dim3(bw, bw), fwd_smem(bw), stream>>>(a, ba, o);
+    k<<<grid, block_of(bw, ppt), fwd_smem(bw, ppt), stream>>>(a, ba, o);
     return check_launch("batch forward");
 }
 
-int launch_bwd_batch(const SceneArgs& a, const BatchArgs& ba, const BwdArgs& g, int bw, int texmode, int grid,
+int launch_bwd_batch(const SceneArgs& a, const BatchArgs& ba, const BwdArgs& g, int bw, int texmode, int ppt, int grid,
                      cudaStream_t stream) {
-    auto k = pick<BwdBatch>(a.C, texmode);
-    int rc = set_smem(k, bwd_smem(bw), "batch backward");
+    ppt = ppt_of(bw, ppt);
+    auto k = pick<BwdBatch>(a.C, texmode, ppt);
+    int rc = set_smem(k, bwd_smem(bw, ppt), "batch backward");
     if (rc) return rc;
-    k<<<grid, dim3(bw, bw), bwd_smem(bw), stream>>>(a, ba, g);
+    k<<<grid, block_of(bw, ppt), bwd_smem(bw, ppt), stream>>>(a, ba, g);
     return check_launch("batch backward");
 }
 
-int resident_ctas(int bw, bool backward, int texmode, int C) {
+int resident_ctas(int bw, bool backward, int texmode, int C, int ppt) {
     int n = 0;
     cudaError_t e;
+    ppt = ppt_of(bw, ppt);
     if (backward) {
-        auto k = pick<BwdBatch>(C, texmode);
-        if (set_smem(k, bwd_smem(bw), "occupancy")) return 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, bw * bw, bwd_smem(bw));
+        auto k = pick<BwdBatch>(C, texmode, ppt);
+        if (set_smem(k, bwd_smem(bw, ppt), "occupancy")) return 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, threads_of(bw, ppt), bwd_smem(bw, ppt));
     } else {
-        auto k = pick<FwdBatch>(C, texmode);
-        if (set_smem(k, fwd_smem(bw), "occupancy")) return 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, bw * bw, fwd_smem(bw));
+        auto k = pick<FwdBatch>(C, texmode, ppt);
+        if (set_smem(k, fwd_smem(bw, ppt), "occupancy")) return 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, threads_of(bw, ppt), fwd_smem(bw, ppt));
     }
     if (e != cudaSuccess) return 0;
     int dev = 0, sms = 0;
@@ -641,10 +771,11 @@ extern "C" int gstex_texture_forward(const gstex_raster_inputs* in, const gstex_
     va.colors = (const float3*)in->colors;
     va.vcolors = nullptr;
     cudaStream_t stream = (cudaStream_t)s;
-    const dim3 grid(va.tiles_x, ceil_div(va.H, bw)), block(bw, bw);
-    auto k = pick<FwdView>(a.C, in->texture_dtype);
-    if ((rc = set_smem(k, fwd_smem(bw), "texture_forward"))) return rc;
-    k<<<grid, block, fwd_smem(bw), stream>>>(a, va, o);
+    const dim3 grid(va.tiles_x, ceil_div(va.H, bw));
+    const int ppt = ppt_of(bw, in->pixels_per_thread);
+    auto k = pick<FwdView>(a.C, in->texture_dtype, ppt);
+    if ((rc = set_smem(k, fwd_smem(bw, ppt), "texture_forward"))) return rc;
+    k<<<grid, block_of(bw, ppt), fwd_smem(bw, ppt), stream>>>(a, va, o);
     return check_launch("texture_forward");
 }
 
@@ -679,10 +810,11 @@ extern "C" int gstex_texture_backward(const gstex_raster_inputs* in, const gstex
     va.bins = (const int2*)in->tile_bins;
     va.colors = (const float3*)in->colors;
     va.vcolors = io->v_colors;
-    const dim3 grid(va.tiles_x, ceil_div(va.H, bw)), block(bw, bw);
-    auto k = pick<BwdView>(a.C, in->texture_dtype);
-    if ((rc = set_smem(k, bwd_smem(bw), "texture_backward"))) return rc;
-    k<<<grid, block, bwd_smem(bw), stream>>>(a, va, g);
+    const dim3 grid(va.tiles_x, ceil_div(va.H, bw));
+    const int ppt = ppt_of(bw, in->pixels_per_thread);
+    auto k = pick<BwdView>(a.C, in->texture_dtype, ppt);
+    if ((rc = set_smem(k, bwd_smem(bw, ppt), "texture_backward"))) return rc;
+    k<<<grid, block_of(bw, ppt), bwd_smem(bw, ppt), stream>>>(a, va, g);
     if ((rc = check_launch("texture_backward"))) return rc;
     return launch_finalize(a, (const float*)io->workspace, io->v_opacity, io->v_means, io->v_scales, io->v_quats,
                            io->v_uv0, io->v_umap, io->v_vmap, stream);

@@ -95,14 +95,15 @@ struct BwdArgs {
 };
 
 int fill_scene(const gstex_raster_inputs* in, SceneArgs& a);
-size_t fwd_smem(int bw);
-size_t bwd_smem(int bw);
-int launch_fwd_batch(const SceneArgs& a, const BatchArgs& ba, const FwdOut& o, int bw, int texmode, int grid,
+int ppt_of(int bw, int requested);
+size_t fwd_smem(int bw, int ppt);
+size_t bwd_smem(int bw, int ppt);
+int launch_fwd_batch(const SceneArgs& a, const BatchArgs& ba, const FwdOut& o, int bw, int texmode, int ppt, int grid,
                      cudaStream_t stream);
-int launch_bwd_batch(const SceneArgs& a, const BatchArgs& ba, const BwdArgs& g, int bw, int texmode, int grid,
+int launch_bwd_batch(const SceneArgs& a, const BatchArgs& ba, const BwdArgs& g, int bw, int texmode, int ppt, int grid,
                      cudaStream_t stream);
 int launch_finalize(const SceneArgs& a, const float* moments, float* v_opac, float* v_means, float* v_scales,
                     float* v_quats, float* v_uv0, float* v_umap, float* v_vmap, cudaStream_t stream);
-int resident_ctas(int bw, bool backward, int texmode, int C);
+int resident_ctas(int bw, bool backward, int texmode, int C, int ppt);
 
 }  // namespace gstex

@@ -179,6 +179,9 @@ def _texture_mode(texture, channels):
     raise _lib.GstexError(f"texture must be float32 or bfloat16, got {texture.dtype}")
 
 
+PIXELS_PER_THREAD = 1  # 1 or 2 (2 halves the threads per tile; even block widths only)
+
+
 def _raster_inputs(img_w, img_h, bw, texture_info, texture_dims, gaussian_ids_sorted, tile_bins, colors, opacities,
                    means, scales, glob_scale, quats, uv0, umap, vmap, texture, viewmat, fx, fy, cx, cy, settings,
                    background):
@@ -210,6 +213,7 @@ def _raster_inputs(img_w, img_h, bw, texture_info, texture_dims, gaussian_ids_so
     ri.fx, ri.fy, ri.cx, ri.cy = float(fx), float(fy), float(cx), float(cy)
     ri.settings = int(settings)
     ri.background = ptr(background)
+    ri.pixels_per_thread = int(PIXELS_PER_THREAD)
     return ri, C
 
 

@@ -159,6 +159,7 @@ typedef struct gstex_raster_inputs {
     float fx, fy, cx, cy;
     int settings;                       /* reference settings bitfield */
     const float* background;            /* [3] device */
+    int pixels_per_thread;              /* 0 = default (1); 2 needs an even block width */
 } gstex_raster_inputs;
 
 typedef struct gstex_forward_outputs {
@@ -292,6 +293,7 @@ typedef struct gstex_batch_inputs {
     const float* background;            /* [3] device */
     int* queue;                         /* device int (tile queue counter) */
     int grid;                           /* persistent CTAs; 0 = all resident */
+    int pixels_per_thread;              /* 0 = default (1); 2 needs an even block width */
 } gstex_batch_inputs;
 
 /* Forward of all views: outputs are the concatenated per-view buffers

@@ -10,8 +10,8 @@ pytestmark = pytest.mark.gpu
 DEV = "cuda:0"
 
 
-@pytest.fixture(scope="module")
-def setup():
+@pytest.fixture(scope="module", params=[(1, 1), (2, 2)], ids=["1px", "2px"])
+def setup(request):
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     from gstex_cuda_gb300 import batch as B, synthetic
@@ -24,7 +24,8 @@ def setup():
                     uv0=spec.uv0.to(DEV), umap=spec.umap.to(DEV), vmap=spec.vmap.to(DEV),
                     texture_dims=spec.texture_dims.to(DEV), texture=spec.texture.to(DEV))
     bcams = [B.Camera(c.viewmat, c.fx, c.fy, c.cx, c.cy, c.width, c.height) for c in cams]
-    r = B.BatchRenderer(bcams, spec.num_points, capacity=1 << 20)
+    r = B.BatchRenderer(bcams, spec.num_points, capacity=1 << 20, fwd_ppt=request.param[0],
+                        bwd_ppt=request.param[1])
     P = r.total_pixels
     gen = torch.Generator().manual_seed(1)
     tgt_img = torch.rand(P, 3, generator=gen).to(DEV)

@@ -133,7 +133,7 @@ def test_phantom_slots_of_clipped_gaussians():
 # --------------------------------------------------------------------------
 # compositor forward / backward vs oracle
 # --------------------------------------------------------------------------
-def _close(got, ref, tol, frac, name):
+def _close(got, ref, tol, frac, name, cap=None):
     """|got - ref| <= tol everywhere, except for at most a fraction ``frac`` of
     elements (pixels where a float rounding difference flips one of the
     reference's hard thresholds: alpha >= 1/255, T <= 1e-4, T > 0.5), which
@@ -143,7 +143,8 @@ def _close(got, ref, tol, frac, name):
         return
     bad = err > tol
     assert bad.mean() <= frac, (name, float(bad.mean()), float(err.max()))
-    assert np.all(err < np.maximum(1e-2 * (1 + np.abs(ref)), tol)), (name, float(err.max()))
+    cap = 1e-2 * (1 + np.abs(ref)) if cap is None else cap
+    assert np.all(err < np.maximum(cap, tol)), (name, float(err.max()))
 
 
 def _compare_forward(case, bw, settings, bg, tol_img, texture=None, prec="f64", frac=0.0):
@@ -153,7 +154,10 @@ def _compare_forward(case, bw, settings, bg, tol_img, texture=None, prec="f64", 
     out, bgt = case.forward_cuda(b["gaussian_ids_sorted"], b["tile_bins"], bw, settings, bg, texture=texture)
     for k in ("img", "texture", "normal", "final_T"):
         _close(np_(out[k]), ref[k], tol_img, frac, k)
-    _close(np_(out["reg_s"]), ref["reg_s"], tol_img * (1 + np.abs(ref["reg_s"])), frac, "reg_s")
+    # one flip of alpha >= 1/255 moves the sums (S0, S1, S2) by up to (1, t, t^2) / 255
+    tmax = float(np.abs(ref["reg_s"][..., 1]).max() / max(float(ref["reg_s"][..., 0].max()), 1e-6)) + 1.0
+    _close(np_(out["reg_s"]), ref["reg_s"], tol_img * (1 + np.abs(ref["reg_s"])), frac, "reg_s",
+           cap=(1 + tmax + tmax * tmax) / 255 + 1e-2 * np.abs(ref["reg_s"]))
     _close(np_(out["reg"]), ref["reg"], tol_img * 10 + tol_img * np.abs(ref["reg"]), frac, "reg")
     same_depth = np_(out["depth_idx"]) == ref["depth_idx"]
     assert same_depth.mean() > 0.999
@@ -221,8 +225,17 @@ def test_raster_tiny_matches_reference_golden():
         assert err < 2e-4, (k, err)
 
 
-@pytest.mark.parametrize("w,h,bw", [(64, 64, 16), (48, 32, 16), (70, 45, 8), (33, 29, 5)])
-def test_raster_small_matches_oracle(w, h, bw):
+@pytest.fixture(params=[1, 2], ids=["1px", "2px"])
+def pixels_per_thread(request):
+    import gstex_cuda_gb300.cuda as C
+    old = C.PIXELS_PER_THREAD
+    C.PIXELS_PER_THREAD = request.param
+    yield request.param
+    C.PIXELS_PER_THREAD = old
+
+
+@pytest.mark.parametrize("w,h,bw", [(64, 64, 16), (48, 32, 16), (70, 45, 8), (33, 29, 5), (40, 30, 10)])
+def test_raster_small_matches_oracle(w, h, bw, pixels_per_thread):
     case = Case(small_scene(n=200, width=w, height=h, seed=w + h))
     bg = np.array([1.0, 1.0, 1.0])
     b, out, bgt, ref = _compare_forward(case, bw, 1 << 8, bg, 5e-5)
@@ -241,7 +254,7 @@ def test_raster_generic_channels(C):
     _compare_backward(case, b, out, bgt, ref, 16, 1 << 8, bg, 5e-4)
 
 
-def test_raster_bf16_texels():
+def test_raster_bf16_texels(pixels_per_thread):
     """bf16 [T,4] texel storage: compared with the oracle run on the same
     bf16-rounded texel values (all blending in fp32)."""
     case = Case(small_scene(n=300, width=64, height=64, seed=21))
