@@ -56,7 +56,7 @@ def _stale() -> bool:
 
 def _compile(src: str, verbose: bool) -> str:
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
-    flags = PER_FILE.get(os.path.basename(src), [])
+    flags = PER_FILE.get(os.path.basename(src), []) + os.environ.get("GSTEX_NVCC_EXTRA", "").split()
     cmd = [nvcc()] + ARCH + COMMON + flags + (["-Xptxas", "-v"] if verbose else []) + ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

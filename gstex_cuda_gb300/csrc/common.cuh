@@ -140,13 +140,9 @@ struct RecWarm {  // pairs that pass the alpha test
     float4 nrm;   // world normal (axis 3), 1 / (scale_y * glob_scale)
     int4 tex;     // chart h, w, start, Gaussian id
 };
-struct RecCold {  // direct form and the backward's ray terms
-    float4 mu;    // camera-space mean
-    float4 a1;    // camera-space axis 1
-    float4 a2;    // camera-space axis 2
-    float4 n;     // camera-space normal
-    float4 um;    // camera-space umap
-    float4 vm;    // camera-space vmap
+struct RecCold {  // the backward's ray terms and the blur adjoint
+    float4 mu;    // camera-space mean, a1 . mean
+    float4 dt;    // a2 . mean, umap . mean, vmap . mean (camera space), unused
 };
 constexpr int kRecBytes = sizeof(RecHot) + sizeof(RecWarm) + sizeof(RecCold);
 
@@ -179,12 +175,8 @@ __device__ __forceinline__ void make_record(RecHot& H, RecWarm& Wm, RecCold& Cd,
     // blur centre exactly as the reference projects it (helpers.cuh:145-152)
     const float rwb = 1.f / (mc.z + 1e-6f);
     const float bx = mc.x * rwb * V.fx + V.cx, by = mc.y * rwb * V.fy + V.cy;
-    Cd.mu = f4(mc, 0.f);
-    Cd.a1 = f4(a1c, is1);
-    Cd.a2 = f4(a2c, is2);
-    Cd.n = f4(nc, 0.f);
-    Cd.um = f4(umc, 0.f);
-    Cd.vm = f4(vmc, 0.f);
+    Cd.mu = f4(mc, dot3(a1c, mc));
+    Cd.dt = make_float4(dot3(a2c, mc), dot3(umc, mc), dot3(vmc, mc), 0.f);
     Wm.uvs = make_float4(uv0.x, uv0.y, bx, by);
     Wm.col = f4(color, is1);
     Wm.nrm = f4(A.a3, is2);
@@ -297,6 +289,8 @@ struct Hit {
     float l1s, l2s;  // plane coordinates divided by the scales
     float du, dv;    // pixel offset from the projected centre (fast form)
     float inv;       // d t_cam / d tvn: 1 / den (fast form), idn / den_ref (direct form)
+    float nd;        // n_c . d, the sign of ray . normal
+    float tu, tv;    // texture uv before clamping (direct form only)
     bool direct;
 };
 
@@ -306,44 +300,49 @@ __device__ __forceinline__ float clamp_denom(float d) {
     return d;
 }
 
-__device__ __forceinline__ Hit intersect(const RecHot& Hr, const RecCold* Cd, const PixelRay& P) {
+// Fast form of the intersection; sets H.direct when the pixel needs the
+// direct form (computed by the caller from the Gaussian's parameters).
+__device__ __forceinline__ Hit intersect(const RecHot& Hr, const PixelRay& P) {
     Hit H;
     H.du = P.px - Hr.a.x;
     H.dv = P.py - Hr.a.y;
     const float den = Hr.a.z + Hr.b.x * H.du + Hr.b.y * H.dv;
+    H.nd = den;
     H.direct = __float_as_int(Hr.d.w) != 0 || !(fabsf(den) >= kDenomEps * P.dn);
-    if (!H.direct) {
-        const float inv = __fdividef(1.f, den);
-        H.inv = inv;
-        H.tcam = Hr.a.w * inv;
-        H.t = H.tcam * P.dn;
-        H.l1s = (Hr.c.x * H.du + Hr.c.y * H.dv) * inv;
-        H.l2s = (Hr.c.z * H.du + Hr.c.w * H.dv) * inv;
-        return H;
-    }
-    // direct camera-space form with the reference's denominator clamp
-    const RecCold& C = *Cd;
-    const float3 d = make_float3(P.u, P.v, 1.f);
-    const float dref = clamp_denom(dot3(f3(C.n), d) * P.idn);
-    const float t = Hr.a.w / dref;
-    const float3 delta = t * (P.idn * d) - f3(C.mu);
-    H.inv = P.idn / dref;
-    H.t = t;
-    H.tcam = t * P.idn;
-    H.l1s = dot3(f3(C.a1), delta) * C.a1.w;
-    H.l2s = dot3(f3(C.a2), delta) * C.a2.w;
+    const float inv = __fdividef(1.f, den);
+    H.inv = inv;
+    H.tcam = Hr.a.w * inv;
+    H.t = H.tcam * P.dn;
+    H.l1s = (Hr.c.x * H.du + Hr.c.y * H.dv) * inv;
+    H.l2s = (Hr.c.z * H.du + Hr.c.w * H.dv) * inv;
     return H;
 }
 
+// Direct camera-space form with the reference's denominator clamp, from the
+// camera-space frame of the Gaussian.
+__device__ __forceinline__ void intersect_direct(Hit& H, const PixelRay& P, float tvn, float3 mc, float3 a1c,
+                                                 float3 a2c, float3 nc, float3 umc, float3 vmc, float is1, float is2,
+                                                 float uv0x, float uv0y) {
+    const float3 d = make_float3(P.u, P.v, 1.f);
+    H.nd = dot3(nc, d);
+    const float dref = clamp_denom(H.nd * P.idn);
+    const float t = tvn / dref;
+    const float3 delta = t * (P.idn * d) - mc;
+    H.inv = P.idn / dref;
+    H.t = t;
+    H.tcam = t * P.idn;
+    H.l1s = dot3(a1c, delta) * is1;
+    H.l2s = dot3(a2c, delta) * is2;
+    H.tu = uv0x + dot3(umc, delta);
+    H.tv = uv0y + dot3(vmc, delta);
+}
+
 // Texture coordinates of the hit (before clamping).
-__device__ __forceinline__ float2 hit_uv(const Hit& H, const RecWarm& Wm, const RecCold* Cd, const PixelRay& P) {
+__device__ __forceinline__ float2 hit_uv(const Hit& H, const RecWarm& Wm) {
     if (!H.direct)
         return make_float2(Wm.uvs.x + (Wm.uvm.x * H.du + Wm.uvm.y * H.dv) * H.inv,
                            Wm.uvs.y + (Wm.uvm.z * H.du + Wm.uvm.w * H.dv) * H.inv);
-    const RecCold& C = *Cd;
-    const float3 d = make_float3(P.u, P.v, 1.f);
-    const float3 delta = H.t * (P.idn * d) - f3(C.mu);
-    return make_float2(Wm.uvs.x + dot3(f3(C.um), delta), Wm.uvs.y + dot3(f3(C.vm), delta));
+    return make_float2(H.tu, H.tv);
 }
 
 __device__ __forceinline__ float clamp01(float x) {

@@ -30,6 +30,29 @@ __device__ __forceinline__ void stage(const Recs& R, int slot, const SceneArgs& 
                 a.umap[gid], a.vmap[gid], a.dims[gid], use_blur);
 }
 
+// Completes a Hit in the direct form, rebuilding the Gaussian's camera-space
+// frame from its parameters (rare: splats at the camera plane and pixels within
+// the reference's denominator clamp).
+__device__ __forceinline__ void direct_hit(Hit& H, const float4* __restrict__ quats, const float3* __restrict__ means,
+                                           const float* __restrict__ scales, float glob, const float2* __restrict__ uv0s,
+                                           const float3* __restrict__ umaps, const float3* __restrict__ vmaps,
+                                           const View& V, int gid, const PixelRay& P, float tvn) {
+    const Axes A = quat_axes(quats[gid]);
+    const float3 mc = V.xform(means[gid]);
+    const float is1 = 1.f / (scales[3 * gid] * glob), is2 = 1.f / (scales[3 * gid + 1] * glob);
+    const float2 uv0 = uv0s[gid];
+    intersect_direct(H, P, tvn, mc, V.rot(A.a1), V.rot(A.a2), V.rot(A.a3), V.rot(umaps[gid]), V.rot(vmaps[gid]), is1,
+                     is2, uv0.x, uv0.y);
+}
+
+__device__ __forceinline__ Hit hit_pixel(const RecHot& Hr, const Recs& R, int k, const SceneArgs& a, const View& V,
+                                         const PixelRay& P) {
+    Hit H = intersect(Hr, P);
+    if (H.direct)
+        direct_hit(H, a.quats, a.means, a.scales, a.glob, a.uv0, a.umap, a.vmap, V, R.warm[k].tex.w, P, Hr.a.w);
+    return H;
+}
+
 // All channels of the 4 bilinear corners (C == 3 fast path).
 template <int TEXMODE>
 __device__ __forceinline__ void fetch3(const void* tex, const Bilerp& B, float c[4][3]) {
@@ -125,7 +148,7 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
             for (int p = 0; p < PPT; p++) {
                 if (done[p]) continue;
                 if (outside_box(Hr, P[p]) && T[p] > 1.01e-4f) continue;
-                const Hit H = intersect(Hr, R.cold + k, P[p]);
+                const Hit H = hit_pixel(Hr, R, k, a, V, P[p]);
                 const float sigma = 0.5f * (H.l1s * H.l1s + H.l2s * H.l2s);
                 float nbf = 1.f, bf = 0.f, sigma_blur = 0.f;
                 if (use_blur) {
@@ -146,11 +169,10 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
                 out[p].y = out[p].y + col.y * vis;
                 out[p].z = out[p].z + col.z * vis;
                 float3 hn = f3(Wm.nrm);
-                if (flip && dot3(make_float3(P[p].u, P[p].v, 1.f), f3(R.cold[k].n)) > 0.f)
-                    hn = make_float3(-hn.x, -hn.y, -hn.z);
+                if (flip && H.nd > 0.f) hn = make_float3(-hn.x, -hn.y, -hn.z);
                 nrm[p].x += vis * hn.x; nrm[p].y += vis * hn.y; nrm[p].z += vis * hn.z;
                 if (C > 0) {
-                    const float2 uv = hit_uv(H, Wm, R.cold + k, P[p]);
+                    const float2 uv = hit_uv(H, Wm);
                     const int4 tx = Wm.tex;
                     const Bilerp B = bilerp(tx.x, tx.y, tx.z, clamp01(uv.x), clamp01(uv.y), bilinear);
                     if (CT == 3) {
@@ -255,7 +277,7 @@ __device__ __forceinline__ void bwd_pair(const SceneArgs& a, const BwdArgs& g, c
     float v_vis = col.x * vout.x + col.y * vout.y + col.z * vout.z + nw.x * vnorm.x + nw.y * vnorm.y + nw.z * vnorm.z;
     float v_u = 0.f, v_v = 0.f;
     if (C > 0) {
-        const float2 uv = hit_uv(H, Wm, R.cold + k, P);
+        const float2 uv = hit_uv(H, Wm);
         const int4 tx = Wm.tex;
         const Bilerp B = bilerp(tx.x, tx.y, tx.z, clamp01(uv.x), clamp01(uv.y), bilinear);
         const float fh = (float)tx.x, fw = (float)tx.y;
@@ -334,13 +356,16 @@ __device__ __forceinline__ void bwd_pair(const SceneArgs& a, const BwdArgs& g, c
     const float l1 = __fdividef(H.l1s, is1), l2 = __fdividef(H.l2s, is2);
     const float v_l1 = H.l1s * is1 * v_sigma;
     const float v_l2 = H.l2s * is2 * v_sigma;
+    // ray . axis from the hit: l = a . (t r - mu) gives a . r = (l + a . mu) / t
     const RecCold& Cd = R.cold[k];
-    const float ra1 = (Cd.a1.x * P.u + Cd.a1.y * P.v + Cd.a1.z) * P.idn;
-    const float ra2 = (Cd.a2.x * P.u + Cd.a2.y * P.v + Cd.a2.z) * P.idn;
+    const float it = __fdividef(1.f, H.t);
+    const float ra1 = (l1 + Cd.mu.w) * it;
+    const float ra2 = (l2 + Cd.dt.x) * it;
     v_t += v_l1 * ra1 + v_l2 * ra2;
     if (prop_uv) {
-        const float rum = (Cd.um.x * P.u + Cd.um.y * P.v + Cd.um.z) * P.idn;
-        const float rvm = (Cd.vm.x * P.u + Cd.vm.y * P.v + Cd.vm.z) * P.idn;
+        const float2 uvr = hit_uv(H, Wm);
+        const float rum = (uvr.x - Wm.uvs.x + Cd.dt.y) * it;
+        const float rvm = (uvr.y - Wm.uvs.y + Cd.dt.z) * it;
         v_t += v_u * rum + v_v * rvm;
     }
     float v_t_view = 0.f;
@@ -451,7 +476,7 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
                 e[p] = eb[p] = alpha[p] = bf[p] = 0.f;
                 nbf[p] = 1.f;
                 if (valid[p]) {
-                    H[p] = intersect(Hr, R.cold + k, S[p].P);
+                    H[p] = hit_pixel(Hr, R, k, a, V, S[p].P);
                     const float sigma = 0.5f * (H[p].l1s * H[p].l1s + H[p].l2s * H[p].l2s);
                     float sigma_blur = 0.f;
                     if (use_blur) {
@@ -526,8 +551,14 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
 #ifndef GSTEX_BWD_MINB
 #define GSTEX_BWD_MINB 4
 #endif
-#define FWD_BOUNDS(PPT) __launch_bounds__((PPT) == 2 ? 128 : 256, (PPT) == 2 ? GSTEX_FWD_MINB : 3)
-#define BWD_BOUNDS(PPT) __launch_bounds__((PPT) == 2 ? 128 : 256, (PPT) == 2 ? GSTEX_BWD_MINB : 2)
+#ifndef GSTEX_FWD_MINB1
+#define GSTEX_FWD_MINB1 4
+#endif
+#ifndef GSTEX_BWD_MINB1
+#define GSTEX_BWD_MINB1 2
+#endif
+#define FWD_BOUNDS(PPT) __launch_bounds__((PPT) == 2 ? 128 : 256, (PPT) == 2 ? GSTEX_FWD_MINB : GSTEX_FWD_MINB1)
+#define BWD_BOUNDS(PPT) __launch_bounds__((PPT) == 2 ? 128 : 256, (PPT) == 2 ? GSTEX_BWD_MINB : GSTEX_BWD_MINB1)
 
 template <int TEXMODE, int CT, int PPT>
 __global__ void FWD_BOUNDS(PPT) fwd_view_kernel(SceneArgs a, ViewArgs va, FwdOut o) {
