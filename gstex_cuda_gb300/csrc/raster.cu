@@ -79,11 +79,30 @@ __device__ __forceinline__ void fetch3(const void* tex, const Bilerp& B, float c
     }
 }
 
+// Local (row, column) of a thread's first pixel.  When the tile width is a
+// multiple of 8, each warp covers an 8-column block of 4 thread rows
+// (8 x 4*PPT pixels): a warp's pixels stay close together, so a splat's screen
+// box splits fewer warps than with 16 x 2 strips.  Otherwise thread (x, y)
+// owns column x and rows PPT*y + p.
+#ifndef GSTEX_WARP_BLOCK
+#define GSTEX_WARP_BLOCK 1
+#endif
+template <int PPT>
+__device__ __forceinline__ int2 thread_pixel(int bw) {
+#if GSTEX_WARP_BLOCK
+    if ((bw & 7) == 0) {
+        const int tr = threadIdx.y * blockDim.x + threadIdx.x;
+        const int lane = tr & 31, w = tr >> 5, wx = bw >> 3;
+        return make_int2(((w / wx) * 4 + (lane >> 3)) * PPT, (w % wx) * 8 + (lane & 7));
+    }
+#endif
+    return make_int2(threadIdx.y * PPT, threadIdx.x);
+}
+
 // ---------------------------------------------------------------------------
 // Forward body: one tile.  A block of bw x (bw / PPT) threads covers the
-// bw x bw tile; thread (x, y) owns pixels (x, PPT*y + p), p < PPT, so a warp
-// covers a compact 16 x (2*PPT) strip and every staged record read from
-// shared memory is used for PPT pixels.
+// bw x bw tile; each thread owns PPT vertically adjacent pixels, so every
+// staged record read from shared memory is used for PPT pixels.
 // ---------------------------------------------------------------------------
 template <int TEXMODE, int CT, int PPT>
 __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, const FwdOut& o, const Recs& R) {
@@ -97,7 +116,8 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
     const bool bilinear = !(a.settings & (1 << 2));
     const int C = CT >= 0 ? CT : a.C;
     constexpr int CA = CT > 0 ? CT : (CT == 0 ? 1 : kMaxChannels);
-    const int pj = J.tx * bw + threadIdx.x;
+    const int2 lp = thread_pixel<PPT>(bw);
+    const int pj = J.tx * bw + lp.y;
     PixelRay P[PPT];
     bool inside[PPT], done[PPT];
     float T[PPT], depth[PPT], reg[PPT];
@@ -107,7 +127,7 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
     bool all_done = true;
 #pragma unroll
     for (int p = 0; p < PPT; p++) {
-        const int pi = J.ty * bw + threadIdx.y * PPT + p;
+        const int pi = J.ty * bw + lp.x + p;
         P[p] = make_pixel(V, pi, pj);
         inside[p] = pi < J.H && pj < J.W;
         done[p] = !inside[p];
@@ -210,7 +230,7 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
 #pragma unroll
     for (int p = 0; p < PPT; p++) {
         if (!inside[p]) continue;
-        const int pi = J.ty * bw + threadIdx.y * PPT + p;
+        const int pi = J.ty * bw + lp.x + p;
         const size_t pix = J.pix_base + (size_t)pi * J.W + pj;
         o.final_T[pix] = T[p];
         o.final_idx[pix] = cur[p];
@@ -419,12 +439,13 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
     const int C = CT >= 0 ? CT : a.C;
     constexpr int CA = CT > 0 ? CT : (CT == 0 ? 1 : kMaxChannels);
     const float3 z3 = make_float3(0.f, 0.f, 0.f);
-    const int pj = J.tx * bw + threadIdx.x;
+    const int2 lp = thread_pixel<PPT>(bw);
+    const int pj = J.tx * bw + lp.y;
     BwdPix<CA> S[PPT];
     int my_bfin = -1;
 #pragma unroll
     for (int p = 0; p < PPT; p++) {
-        const int pi = J.ty * bw + threadIdx.y * PPT + p;
+        const int pi = J.ty * bw + lp.x + p;
         BwdPix<CA>& s = S[p];
         s.P = make_pixel(V, pi, pj);
         s.inside = pi < J.H && pj < J.W;
