@@ -123,6 +123,20 @@ class Case:
         return dict(zip(names, grads))
 
 
+def close_frac(got, ref, tol, frac, name, cap=None):
+    """|got - ref| <= tol everywhere, except for at most a fraction ``frac`` of
+    elements (pixels where a float rounding difference flips one of the
+    reference's hard thresholds: alpha >= 1/255, T <= 1e-4, T > 0.5), which
+    must still stay below 1e-2 (relative to the value's size)."""
+    err = np.abs(np.asarray(got, np.float64) - np.asarray(ref, np.float64))
+    if err.size == 0:
+        return
+    bad = err > tol
+    assert bad.mean() <= frac, (name, float(bad.mean()), float(err.max()))
+    cap = 1e-2 * (1 + np.abs(ref)) if cap is None else cap
+    assert np.all(err < np.maximum(cap, tol)), (name, float(err.max()))
+
+
 def upstream(H, W, C, seed=7):
     g = np.random.default_rng(seed)
     return dict(img=g.standard_normal((H, W, 3)), depth=g.standard_normal((H, W)), reg=g.standard_normal((H, W)),

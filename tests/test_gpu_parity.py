@@ -11,7 +11,7 @@ import pytest
 import torch
 
 import oracle
-from gpu_helpers import Case, np_, small_scene, upstream
+from gpu_helpers import Case, close_frac as _close, np_, small_scene, upstream
 
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
@@ -133,20 +133,6 @@ def test_phantom_slots_of_clipped_gaussians():
 # --------------------------------------------------------------------------
 # compositor forward / backward vs oracle
 # --------------------------------------------------------------------------
-def _close(got, ref, tol, frac, name, cap=None):
-    """|got - ref| <= tol everywhere, except for at most a fraction ``frac`` of
-    elements (pixels where a float rounding difference flips one of the
-    reference's hard thresholds: alpha >= 1/255, T <= 1e-4, T > 0.5), which
-    must still stay below 1e-2 (relative to the value's size)."""
-    err = np.abs(np.asarray(got, np.float64) - np.asarray(ref, np.float64))
-    if err.size == 0:
-        return
-    bad = err > tol
-    assert bad.mean() <= frac, (name, float(bad.mean()), float(err.max()))
-    cap = 1e-2 * (1 + np.abs(ref)) if cap is None else cap
-    assert np.all(err < np.maximum(cap, tol)), (name, float(err.max()))
-
-
 def _compare_forward(case, bw, settings, bg, tol_img, texture=None, prec="f64", frac=0.0):
     b = case.binning_cuda(bw)
     ref = oracle.texture_forward(case.scene_np, case.cam_np, b["gaussian_ids_sorted"].cpu().numpy(),
