@@ -41,7 +41,7 @@ class BatchInputs(ctypes.Structure):
                 ("views", _P), ("tile_view", _P), ("tile_order", _P), ("gaussian_ids_sorted", _P), ("tile_bins", _P),
                 ("colors", _P), ("opacities", _P), ("means", _P), ("scales", _P), ("glob_scale", _F), ("quats", _P),
                 ("uv0", _P), ("umap", _P), ("vmap", _P), ("texture_dims", _P), ("texture", _P), ("background", _P),
-                ("queue", _P), ("grid", _I), ("pixels_per_thread", _I)]
+                ("queue", _P), ("grid", _I), ("pixels_per_thread", _I), ("records", _P)]
 
 
 _BATCH_SIGS = {
@@ -52,6 +52,8 @@ _BATCH_SIGS = {
     "gstex_batch_emit": (_I, [_I, _I, _P, _P, _P, _F, _P, _I, _P, _P, _LL, _P, _P, _P, _P, _P]),
     "gstex_sort_pairs_dyn": (_I, [_I, _P, _I, _P, _P, _P, _P, _P, ctypes.c_size_t, _P]),
     "gstex_get_tile_bin_edges_dyn": (_I, [_I, _P, _P, _I, _P, _P]),
+    "gstex_batch_records_bytes": (ctypes.c_size_t, [_I, _I]),
+    "gstex_batch_records": (_I, [ctypes.POINTER(BatchInputs), _P, _P, _P]),
     "gstex_batch_forward": (_I, [ctypes.POINTER(BatchInputs), ctypes.POINTER(_lib.ForwardOutputs), _P]),
     "gstex_batch_backward_workspace_bytes": (ctypes.c_size_t, [_I]),
     "gstex_batch_backward": (_I, [ctypes.POINTER(BatchInputs), ctypes.POINTER(_lib.BackwardIO), _P]),
@@ -111,7 +113,7 @@ class BatchRenderer:
     def __init__(self, cameras: Sequence[Camera], num_points: int, *, channels: int = 3, texture_dtype=torch.float32,
                  block_width: int = 16, settings: int = 1 << 8, background=(0.0, 0.0, 0.0), capacity: int = 0,
                  device="cuda:0", grid: int = 0, loss_weights: Optional[dict] = None, fwd_ppt: int = 1,
-                 bwd_ppt: int = 1):
+                 bwd_ppt: int = 1, prebuilt_records: bool = True):
         self.dev = torch.device(device)
         self.N = int(num_points)
         self.V = len(cameras)
@@ -154,6 +156,9 @@ class BatchRenderer:
         self.cum = torch.empty(VN, **i32)
         self.total = torch.zeros(1, **i64)
         self.scan_ws = torch.empty(L.gstex_scan_workspace_bytes(VN), **u8)
+        # splat records of every (view, Gaussian), built once per step by bin()
+        self.records = (torch.empty(L.gstex_batch_records_bytes(self.N, self.V), **u8) if prebuilt_records
+                        else None)
         # intersections (capacity-sized)
         self.capacity = int(capacity) if capacity else max(1 << 20, 4 * VN)
         self._alloc_isect()
@@ -203,10 +208,12 @@ class BatchRenderer:
         bi.texture_dims, bi.texture, bi.background = ptr(s.texture_dims), ptr(s.texture), ptr(self.bg)
         bi.queue, bi.grid = ptr(self.queue), self.grid
         bi.pixels_per_thread = self.bwd_ppt if backward else self.fwd_ppt
+        bi.records = ptr(self.records) if self.records is not None else None
         return bi
 
     def bin(self, s: Scene):
-        """Projection, SH colours and binning of all views (device only)."""
+        """Projection, SH colours, splat records and binning of all views (device
+        only)."""
         L = _L()
         st = torch.cuda.current_stream(self.dev).cuda_stream
         sh_dtype = 1 if s.sh_coeffs.dtype == torch.bfloat16 else 0
@@ -214,6 +221,9 @@ class BatchRenderer:
                                     float(s.glob_scale), ptr(s.quats), ptr(s.sh_coeffs), sh_dtype, s.sh_degree,
                                     self.bw, ptr(self.colors), ptr(self.counts), st), "batch_project")
         VN = self.V * self.N
+        if self.records is not None:
+            check(L.gstex_batch_records(ctypes.byref(self._inputs(s)), ptr(self.counts), ptr(self.records), st),
+                  "batch_records")
         check(L.gstex_inclusive_scan_i32(VN, ptr(self.counts), ptr(self.cum), ptr(self.total), ptr(self.scan_ws),
                                          self.scan_ws.numel(), st), "scan")
         check(L.gstex_batch_emit(self.N, self.V, ptr(self.views_dev), ptr(s.means), ptr(s.scales),

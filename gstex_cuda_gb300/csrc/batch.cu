@@ -341,7 +341,23 @@ static int batch_scene(const gstex_batch_inputs* in, SceneArgs& a, BatchArgs& ba
     ba.colors = (const float3*)in->colors;
     ba.vcolors = nullptr;
     ba.queue = in->queue;
+    ba.recs = (const RecAll*)in->records;
     return GSTEX_OK;
+}
+
+extern "C" size_t gstex_batch_records_bytes(int num_points, int num_views) {
+    return (size_t)(num_points > 0 ? num_points : 0) * (num_views > 0 ? num_views : 0) * sizeof(RecAll);
+}
+
+extern "C" int gstex_batch_records(const gstex_batch_inputs* in, const int32_t* counts, void* records,
+                                   gstex_stream_t s) {
+    SceneArgs a;
+    BatchArgs ba;
+    int rc = batch_scene(in, a, ba);
+    if (rc) return rc;
+    GSTEX_REQUIRE(records && ((uintptr_t)records & 15) == 0);
+    if (a.N > 0) GSTEX_REQUIRE(counts);
+    return launch_records(a, ba, in->num_views, counts, (RecAll*)records, (cudaStream_t)s);
 }
 
 static int grid_of(const gstex_batch_inputs* in, bool backward) {

@@ -146,6 +146,16 @@ struct RecCold {  // the backward's ray terms and the blur adjoint
 };
 constexpr int kRecBytes = sizeof(RecHot) + sizeof(RecWarm) + sizeof(RecCold);
 
+// One (view, Gaussian) record as the batched path stores it in device memory:
+// built once per view by the record kernel (where the near-edge-on solve runs
+// in double), then copied into shared memory by every tile the splat touches.
+struct __align__(16) RecAll {
+    RecHot h;
+    RecWarm w;
+    RecCold c;
+};
+static_assert(sizeof(RecAll) == kRecBytes, "record layout");
+
 struct Recs {
     RecHot* hot;
     RecWarm* warm;

@@ -30,6 +30,30 @@ __device__ __forceinline__ void stage(const Recs& R, int slot, const SceneArgs& 
                 a.umap[gid], a.vmap[gid], a.dims[gid], use_blur);
 }
 
+// Stages the record of Gaussian gid for one tile: a copy of the prebuilt
+// (view, Gaussian) record when the batched path built them, else built here.
+__device__ __forceinline__ void stage_job(const Recs& R, int slot, const SceneArgs& a, const TileJob& J, int gid,
+                                          bool use_blur) {
+    if (J.recs) {
+        const uint4* src = reinterpret_cast<const uint4*>(J.recs + gid);
+        uint4 v[kRecBytes / 16];
+#pragma unroll
+        for (int q = 0; q < kRecBytes / 16; q++) v[q] = __ldg(src + q);
+        uint4* hot = reinterpret_cast<uint4*>(R.hot + slot);
+        uint4* warm = reinterpret_cast<uint4*>(R.warm + slot);
+        uint4* cold = reinterpret_cast<uint4*>(R.cold + slot);
+        constexpr int nh = sizeof(RecHot) / 16, nw = sizeof(RecWarm) / 16, nc = sizeof(RecCold) / 16;
+#pragma unroll
+        for (int q = 0; q < nh; q++) hot[q] = v[q];
+#pragma unroll
+        for (int q = 0; q < nw; q++) warm[q] = v[nh + q];
+#pragma unroll
+        for (int q = 0; q < nc; q++) cold[q] = v[nh + nw + q];
+    } else {
+        stage(R, slot, a, J.V, J.colors, gid, use_blur);
+    }
+}
+
 // Completes a Hit in the direct form, rebuilding the Gaussian's camera-space
 // frame from its parameters (rare: splats at the camera plane and pixels within
 // the reference's denominator clamp).
@@ -148,7 +172,7 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
         if (__syncthreads_count(all_done) >= nthr) break;
         const int bstart = range.x + nthr * b;
         const int idx = bstart + tr;
-        if (idx < range.y) stage(R, tr, a, V, J.colors, a.gids[idx], use_blur);
+        if (idx < range.y) stage_job(R, tr, a, J, a.gids[idx], use_blur);
         __syncthreads();
         const int bsize = min(nthr, range.y - bstart);
         if (all_done) continue;
@@ -472,7 +496,7 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
         const int bend = range.y - 1 - nthr * b;
         const int bsize = min(nthr, bend + 1 - range.x);
         const int idx = bend - tr;
-        if (idx >= range.x) stage(R, tr, a, V, J.colors, a.gids[idx], use_blur);
+        if (idx >= range.x) stage_job(R, tr, a, J, a.gids[idx], use_blur);
         for (int q = tr; q < nthr * kMoments; q += nthr) smom[q] = 0.f;
         __syncthreads();
         for (int k = max(0, bend - warp_bfin); k < bsize; ++k) {
@@ -592,6 +616,7 @@ __global__ void FWD_BOUNDS(PPT) fwd_view_kernel(SceneArgs a, ViewArgs va, FwdOut
     J.pix_base = 0;
     J.colors = va.colors;
     J.vcolors = nullptr;
+    J.recs = nullptr;
     fwd_tile<TEXMODE, CT, PPT>(a, J, o, Recs::carve(smem, blockDim.x * blockDim.y));
 }
 
@@ -607,6 +632,7 @@ __global__ void BWD_BOUNDS(PPT) bwd_view_kernel(SceneArgs a, ViewArgs va, BwdArg
     J.pix_base = 0;
     J.colors = va.colors;
     J.vcolors = va.vcolors;
+    J.recs = nullptr;
     bwd_tile<TEXMODE, CT, PPT>(a, J, g, Recs::carve(smem, nthr), reinterpret_cast<float*>(smem + (size_t)kRecBytes * nthr));
 }
 
@@ -628,6 +654,7 @@ __device__ __forceinline__ bool next_job(const BatchArgs& ba, int* s_tile, TileJ
     J.pix_base = bv.pix_offset;
     J.colors = ba.colors + (size_t)v * ba.num_points;
     J.vcolors = ba.vcolors ? ba.vcolors + (size_t)v * ba.num_points * 3 : nullptr;
+    J.recs = ba.recs ? ba.recs + (size_t)v * ba.num_points : nullptr;
     return true;
 }
 
@@ -649,6 +676,29 @@ __global__ void BWD_BOUNDS(PPT) bwd_batch_kernel(SceneArgs a, BatchArgs ba, BwdA
     const Recs R = Recs::carve(smem, nthr);
     float* smom = reinterpret_cast<float*>(smem + (size_t)kRecBytes * nthr);
     while (next_job(ba, &s_tile, J)) bwd_tile<TEXMODE, CT, PPT>(a, J, g, R, smom);
+}
+
+// Records of every (view, Gaussian) pair with tiles in the view, and of
+// Gaussian 0 in every view (the reference's zero-slot entries name it).
+// grid.y = view.
+__global__ void records_kernel(SceneArgs a, BatchArgs ba, const int32_t* __restrict__ counts,
+                               RecAll* __restrict__ recs) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ba.num_points) return;
+    const size_t j = (size_t)blockIdx.y * ba.num_points + i;
+    if (counts[j] <= 0 && i != 0) return;
+    const View V = ba.views[blockIdx.y].V;
+    RecAll r;
+    make_record(r.h, r.w, r.c, i, V, a.means[i], a.quats[i], make_float2(a.scales[3 * i], a.scales[3 * i + 1]), a.glob,
+                a.opac[i], ba.colors[j], a.uv0[i], a.umap[i], a.vmap[i], a.dims[i], a.settings & (1 << 9));
+    recs[j] = r;
+}
+
+int launch_records(const SceneArgs& a, const BatchArgs& ba, int num_views, const int32_t* counts, RecAll* recs,
+                   cudaStream_t stream) {
+    if (a.N == 0) return GSTEX_OK;
+    records_kernel<<<dim3(ceil_div(a.N, 128), num_views), 128, 0, stream>>>(a, ba, counts, recs);
+    return check_launch("batch_records");
 }
 
 // Moments -> parameter gradients (one thread per Gaussian).  Colour gradients

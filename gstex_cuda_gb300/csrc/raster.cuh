@@ -55,6 +55,7 @@ struct BatchArgs {
     const float3* colors;      // [V, N, 3]
     float* vcolors;            // [V, N, 3]
     int* queue;                // tile counter, zero before each launch
+    const RecAll* recs;        // optional [V, N] prebuilt records; null: built per tile
 };
 
 // What one CTA needs to render one tile.
@@ -65,6 +66,7 @@ struct TileJob {
     size_t pix_base;
     const float3* colors;
     float* vcolors;
+    const RecAll* recs;   // the view's prebuilt records, or null
 };
 
 struct FwdOut {
@@ -105,5 +107,7 @@ int launch_bwd_batch(const SceneArgs& a, const BatchArgs& ba, const BwdArgs& g, 
 int launch_finalize(const SceneArgs& a, const float* moments, float* v_opac, float* v_means, float* v_scales,
                     float* v_quats, float* v_uv0, float* v_umap, float* v_vmap, cudaStream_t stream);
 int resident_ctas(int bw, bool backward, int texmode, int C, int ppt);
+int launch_records(const SceneArgs& a, const BatchArgs& ba, int num_views, const int32_t* counts, RecAll* recs,
+                   cudaStream_t stream);
 
 }  // namespace gstex

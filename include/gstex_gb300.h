@@ -294,7 +294,24 @@ typedef struct gstex_batch_inputs {
     int* queue;                         /* device int (tile queue counter) */
     int grid;                           /* persistent CTAs; 0 = all resident */
     int pixels_per_thread;              /* 0 = default (1); 2 needs an even block width */
+    const void* records;                /* optional: gstex_batch_records output (16-byte aligned);
+                                           null = each tile derives the records it stages */
 } gstex_batch_inputs;
+
+/* Bytes of the per-(view, Gaussian) splat records of gstex_batch_records
+ * (176 bytes per pair). */
+size_t gstex_batch_records_bytes(int num_points, int num_views);
+
+/* Builds the splat record (camera-space plane coefficients, alpha >= 1/255
+ * screen box, colour, chart) of every (view, Gaussian) pair whose tile count
+ * in `counts` ([V, N], from gstex_batch_project) is positive, and of
+ * Gaussian 0 in every view, once per step; near-edge-on splats are solved in
+ * double here.  Pass the buffer as in->records to the forward and backward,
+ * which then copy records instead of deriving them per tile.  Reads
+ * in->colors, the Gaussian parameters and in->views.  No reference
+ * counterpart (the reference derives the same quantities per pixel,
+ * csrc/texture.cu:160-181). */
+int gstex_batch_records(const gstex_batch_inputs* in, const int32_t* counts, void* records, gstex_stream_t stream);
 
 /* Forward of all views: outputs are the concatenated per-view buffers
  * (pixel p of view v at pix_offsets[v] + p).  Batched texture_forward. */
