@@ -111,6 +111,11 @@ __device__ __forceinline__ void fetch3(const void* tex, const Bilerp& B, float c
 #ifndef GSTEX_WARP_BLOCK
 #define GSTEX_WARP_BLOCK 1
 #endif
+// Candidate lists in the forward (off: forward pixels saturate early, and
+// walking every staged slot with a per-thread box test measured faster).
+#ifndef GSTEX_FWD_LIST
+#define GSTEX_FWD_LIST 0
+#endif
 template <int PPT>
 __device__ __forceinline__ int2 thread_pixel(int bw) {
 #if GSTEX_WARP_BLOCK
@@ -123,16 +128,44 @@ __device__ __forceinline__ int2 thread_pixel(int bw) {
     return make_int2(threadIdx.y * PPT, threadIdx.x);
 }
 
+// Candidate list of one warp: the staged slots k in [k0, bsize), in order,
+// whose screen box overlaps the rectangle of the warp's pixel centres.  A
+// splat left out is outside its alpha >= 1/255 box for every pixel of the
+// warp.  Returns the count; the entries are in wl[0, count).  The lanes of a
+// partial warp (tile widths that are not a multiple of 8) are its low lanes.
+__device__ __forceinline__ int build_list(uint8_t* wl, const Recs& R, int k0, int bsize, float rx0, float rx1,
+                                          float ry0, float ry1, unsigned wmask, unsigned lane) {
+    const int nl = __popc(wmask);
+    int cnt = 0;
+    for (int base = k0; base < bsize; base += nl) {
+        const int kk = base + (int)lane;
+        bool hit = false;
+        if (kk < bsize) {
+            const float4 hb = R.hot[kk].b, hd = R.hot[kk].d;
+            hit = !(hb.w < rx0 || hb.z > rx1 || hd.y < ry0 || hd.x > ry1);
+        }
+        const unsigned m = __ballot_sync(wmask, hit);
+        if (hit) wl[cnt + __popc(m & ((1u << lane) - 1u))] = (uint8_t)kk;
+        cnt += __popc(m);
+    }
+    __syncwarp(wmask);
+    return cnt;
+}
+
 // ---------------------------------------------------------------------------
 // Forward body: one tile.  A block of bw x (bw / PPT) threads covers the
 // bw x bw tile; each thread owns PPT vertically adjacent pixels, so every
 // staged record read from shared memory is used for PPT pixels.
 // ---------------------------------------------------------------------------
 template <int TEXMODE, int CT, int PPT>
-__device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, const FwdOut& o, const Recs& R) {
+__device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, const FwdOut& o, const Recs& R,
+                                         uint8_t* lists) {
     const int nthr = blockDim.x * blockDim.y;
     const int tr = threadIdx.y * blockDim.x + threadIdx.x;
     const int bw = blockDim.x;
+    const unsigned wmask = __activemask();
+    const unsigned lane = tr & 31;
+    uint8_t* wl = lists + (tr >> 5) * nthr;
     const View& V = J.V;
     const bool use_blur = a.settings & (1 << 9);
     const bool use_ndc = a.settings & (1 << 10);
@@ -175,18 +208,47 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
         if (idx < range.y) stage_job(R, tr, a, J, a.gids[idx], use_blur);
         __syncthreads();
         const int bsize = min(nthr, range.y - bstart);
-        if (all_done) continue;
-        for (int k = 0; k < bsize; ++k) {
+        if (__all_sync(wmask, all_done)) continue;
+        // Outside its alpha >= 1/255 box the reference skips a splat, and can
+        // end a pixel there only when T <= 1e-4 * 255/254.  While every live
+        // pixel of the warp has T > 1.01e-4 the warp walks its candidate list;
+        // once one has not, it walks every remaining slot in order.
+        int cnt = 0;
+        bool low = false;
+#pragma unroll
+        for (int p = 0; p < PPT; p++) low = low || (!done[p] && T[p] <= 1.01e-4f);
+#if GSTEX_FWD_LIST
+        bool slow = __any_sync(wmask, low);
+        if (!slow) {
+            // rectangle of the warp's pixel centres (pixel centres are positive,
+            // so their float bits order like integers)
+            const float rx0 = __int_as_float(__reduce_min_sync(wmask, __float_as_int(P[0].px)));
+            const float rx1 = __int_as_float(__reduce_max_sync(wmask, __float_as_int(P[0].px)));
+            const float ry0 = __int_as_float(__reduce_min_sync(wmask, __float_as_int(P[0].py)));
+            const float ry1 = __int_as_float(__reduce_max_sync(wmask, __float_as_int(P[PPT - 1].py)));
+            cnt = build_list(wl, R, 0, bsize, rx0, rx1, ry0, ry1, wmask, lane);
+        }
+#else
+        bool slow = true;
+#endif
+        int j = 0, k = -1;
+        int kn = (!slow && cnt > 0) ? wl[0] : 0;
+        while (true) {
+            if (!slow) {
+                if (j >= cnt) break;
+                k = kn;
+                if (++j < cnt) kn = wl[j];
+            } else if (++k >= bsize) {
+                break;
+            }
             const float4 hb = R.hot[k].b, hd = R.hot[k].d;
             bool need = false;
 #pragma unroll
             for (int p = 0; p < PPT; p++) {
-                // outside the splat's alpha >= 1/255 box the reference skips the pair; it
-                // can only end the pixel there when T <= 1e-4 * 255/254
                 const bool out_box = P[p].px < hb.z || P[p].px > hb.w || P[p].py < hd.x || P[p].py > hd.y;
                 need = need || (!done[p] && !(out_box && T[p] > 1.01e-4f));
             }
-            if (!need) continue;
+            if (need) {
             const RecHot Hr = R.hot[k];
 #pragma unroll
             for (int p = 0; p < PPT; p++) {
@@ -244,11 +306,17 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
                 T[p] = next_T;
                 cur[p] = bstart + k;
             }
+            }
             bool ad = true;
+            low = false;
 #pragma unroll
-            for (int p = 0; p < PPT; p++) ad = ad && done[p];
+            for (int p = 0; p < PPT; p++) {
+                ad = ad && done[p];
+                low = low || (!done[p] && T[p] <= 1.01e-4f);
+            }
             all_done = ad;
-            if (all_done) break;
+            if (__all_sync(wmask, all_done)) break;
+            if (!slow) slow = __any_sync(wmask, low);
         }
     }
 #pragma unroll
@@ -448,12 +516,13 @@ __device__ __forceinline__ void bwd_pair(const SceneArgs& a, const BwdArgs& g, c
 
 template <int TEXMODE, int CT, int PPT>
 __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, const BwdArgs& g, const Recs& R,
-                                         float* smom) {
+                                         float* smom, uint8_t* lists) {
     const int nthr = blockDim.x * blockDim.y;
     const int tr = threadIdx.y * blockDim.x + threadIdx.x;
     const int bw = blockDim.x;
     const unsigned lane = tr & 31;
     const unsigned wmask = __activemask();
+    uint8_t* wl = lists + (tr >> 5) * nthr;
     const bool full_warp = wmask == 0xffffffffu;
     const View& V = J.V;
     const bool use_blur = a.settings & (1 << 9);
@@ -488,6 +557,11 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
         if (s.inside) my_bfin = max(my_bfin, s.bfin);
     }
     const int warp_bfin = __reduce_max_sync(wmask, my_bfin);
+    // rectangle of the warp's pixel centres
+    const float rx0 = (float)__reduce_min_sync(wmask, pj) + 0.5f, rx1 = (float)__reduce_max_sync(wmask, pj) + 0.5f;
+    const int pi0 = J.ty * bw + lp.x;
+    const float ry0 = (float)__reduce_min_sync(wmask, pi0) + 0.5f;
+    const float ry1 = (float)__reduce_max_sync(wmask, pi0 + PPT - 1) + 0.5f;
 
     const int2 range = J.range;
     const int nb = ceil_div(range.y - range.x, nthr);
@@ -499,7 +573,11 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
         if (idx >= range.x) stage_job(R, tr, a, J, a.gids[idx], use_blur);
         for (int q = tr; q < nthr * kMoments; q += nthr) smom[q] = 0.f;
         __syncthreads();
-        for (int k = max(0, bend - warp_bfin); k < bsize; ++k) {
+        // splats outside their alpha >= 1/255 box contribute nothing here:
+        // walk the warp's candidates, back to front
+        const int cnt = build_list(wl, R, max(0, bend - warp_bfin), bsize, rx0, rx1, ry0, ry1, wmask, lane);
+        for (int j = 0; j < cnt; ++j) {
+            const int k = wl[j];
             const int gidx = bend - k;
             {
                 const float4 hb = R.hot[k].b, hd = R.hot[k].d;
@@ -617,7 +695,8 @@ __global__ void FWD_BOUNDS(PPT) fwd_view_kernel(SceneArgs a, ViewArgs va, FwdOut
     J.colors = va.colors;
     J.vcolors = nullptr;
     J.recs = nullptr;
-    fwd_tile<TEXMODE, CT, PPT>(a, J, o, Recs::carve(smem, blockDim.x * blockDim.y));
+    const int nthr = blockDim.x * blockDim.y;
+    fwd_tile<TEXMODE, CT, PPT>(a, J, o, Recs::carve(smem, nthr), smem + (size_t)kRecBytes * nthr);
 }
 
 template <int TEXMODE, int CT, int PPT>
@@ -633,7 +712,8 @@ __global__ void BWD_BOUNDS(PPT) bwd_view_kernel(SceneArgs a, ViewArgs va, BwdArg
     J.colors = va.colors;
     J.vcolors = va.vcolors;
     J.recs = nullptr;
-    bwd_tile<TEXMODE, CT, PPT>(a, J, g, Recs::carve(smem, nthr), reinterpret_cast<float*>(smem + (size_t)kRecBytes * nthr));
+    bwd_tile<TEXMODE, CT, PPT>(a, J, g, Recs::carve(smem, nthr), reinterpret_cast<float*>(smem + (size_t)kRecBytes * nthr),
+                               smem + (size_t)(kRecBytes + kMoments * sizeof(float)) * nthr);
 }
 
 __device__ __forceinline__ bool next_job(const BatchArgs& ba, int* s_tile, TileJob& J) {
@@ -663,8 +743,10 @@ __global__ void FWD_BOUNDS(PPT) fwd_batch_kernel(SceneArgs a, BatchArgs ba, FwdO
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_tile;
     TileJob J;
-    const Recs R = Recs::carve(smem, blockDim.x * blockDim.y);
-    while (next_job(ba, &s_tile, J)) fwd_tile<TEXMODE, CT, PPT>(a, J, o, R);
+    const int nthr = blockDim.x * blockDim.y;
+    const Recs R = Recs::carve(smem, nthr);
+    uint8_t* lists = smem + (size_t)kRecBytes * nthr;
+    while (next_job(ba, &s_tile, J)) fwd_tile<TEXMODE, CT, PPT>(a, J, o, R, lists);
 }
 
 template <int TEXMODE, int CT, int PPT>
@@ -675,7 +757,8 @@ __global__ void BWD_BOUNDS(PPT) bwd_batch_kernel(SceneArgs a, BatchArgs ba, BwdA
     TileJob J;
     const Recs R = Recs::carve(smem, nthr);
     float* smom = reinterpret_cast<float*>(smem + (size_t)kRecBytes * nthr);
-    while (next_job(ba, &s_tile, J)) bwd_tile<TEXMODE, CT, PPT>(a, J, g, R, smom);
+    uint8_t* lists = smem + (size_t)(kRecBytes + kMoments * sizeof(float)) * nthr;
+    while (next_job(ba, &s_tile, J)) bwd_tile<TEXMODE, CT, PPT>(a, J, g, R, smom, lists);
 }
 
 // Records of every (view, Gaussian) pair with tiles in the view, and of
@@ -797,8 +880,15 @@ template <int M, int C, int P> struct BwdBatch { typedef void (*type)(SceneArgs,
 
 static dim3 block_of(int bw, int ppt) { return dim3(bw, bw / ppt); }
 static int threads_of(int bw, int ppt) { return bw * (bw / ppt); }
-size_t fwd_smem(int bw, int ppt) { return (size_t)kRecBytes * threads_of(bw, ppt); }
-size_t bwd_smem(int bw, int ppt) { return ((size_t)kRecBytes + kMoments * sizeof(float)) * threads_of(bw, ppt); }
+// records, then (backward) the moment slots, then one candidate list per warp
+static size_t list_bytes(int bw, int ppt) {
+    const int n = threads_of(bw, ppt);
+    return (size_t)ceil_div(n, 32) * n;
+}
+size_t fwd_smem(int bw, int ppt) { return (size_t)kRecBytes * threads_of(bw, ppt) + list_bytes(bw, ppt); }
+size_t bwd_smem(int bw, int ppt) {
+    return ((size_t)kRecBytes + kMoments * sizeof(float)) * threads_of(bw, ppt) + list_bytes(bw, ppt);
+}
 
 int launch_finalize(const SceneArgs& a, const float* moments, float* v_opac, float* v_means, float* v_scales,
                     float* v_quats, float* v_uv0, float* v_umap, float* v_vmap, cudaStream_t stream) {
