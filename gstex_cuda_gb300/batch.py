@@ -53,7 +53,8 @@ _BATCH_SIGS = {
     "gstex_sort_pairs_dyn": (_I, [_I, _P, _I, _P, _P, _P, _P, _P, ctypes.c_size_t, _P]),
     "gstex_get_tile_bin_edges_dyn": (_I, [_I, _P, _P, _I, _P, _P]),
     "gstex_batch_records_bytes": (ctypes.c_size_t, [_I, _I]),
-    "gstex_batch_records": (_I, [ctypes.POINTER(BatchInputs), _P, _P, _P]),
+    "gstex_batch_records_workspace_bytes": (ctypes.c_size_t, [_I, _I]),
+    "gstex_batch_records": (_I, [ctypes.POINTER(BatchInputs), _P, _P, _P, ctypes.c_size_t, _P]),
     "gstex_batch_forward": (_I, [ctypes.POINTER(BatchInputs), ctypes.POINTER(_lib.ForwardOutputs), _P]),
     "gstex_batch_backward_workspace_bytes": (ctypes.c_size_t, [_I]),
     "gstex_batch_backward": (_I, [ctypes.POINTER(BatchInputs), ctypes.POINTER(_lib.BackwardIO), _P]),
@@ -159,6 +160,8 @@ class BatchRenderer:
         # splat records of every (view, Gaussian), built once per step by bin()
         self.records = (torch.empty(L.gstex_batch_records_bytes(self.N, self.V), **u8) if prebuilt_records
                         else None)
+        self.records_ws = (torch.empty(L.gstex_batch_records_workspace_bytes(self.N, self.V), **u8)
+                           if prebuilt_records else None)
         # intersections (capacity-sized)
         self.capacity = int(capacity) if capacity else max(1 << 20, 4 * VN)
         self._alloc_isect()
@@ -222,8 +225,8 @@ class BatchRenderer:
                                     self.bw, ptr(self.colors), ptr(self.counts), st), "batch_project")
         VN = self.V * self.N
         if self.records is not None:
-            check(L.gstex_batch_records(ctypes.byref(self._inputs(s)), ptr(self.counts), ptr(self.records), st),
-                  "batch_records")
+            check(L.gstex_batch_records(ctypes.byref(self._inputs(s)), ptr(self.counts), ptr(self.records),
+                                        ptr(self.records_ws), self.records_ws.numel(), st), "batch_records")
         check(L.gstex_inclusive_scan_i32(VN, ptr(self.counts), ptr(self.cum), ptr(self.total), ptr(self.scan_ws),
                                          self.scan_ws.numel(), st), "scan")
         check(L.gstex_batch_emit(self.N, self.V, ptr(self.views_dev), ptr(s.means), ptr(s.scales),

@@ -349,15 +349,23 @@ extern "C" size_t gstex_batch_records_bytes(int num_points, int num_views) {
     return (size_t)(num_points > 0 ? num_points : 0) * (num_views > 0 ? num_views : 0) * sizeof(RecAll);
 }
 
+extern "C" size_t gstex_batch_records_workspace_bytes(int num_points, int num_views) {
+    return 16 + (size_t)(num_points > 0 ? num_points : 0) * (num_views > 0 ? num_views : 0) * sizeof(uint32_t);
+}
+
 extern "C" int gstex_batch_records(const gstex_batch_inputs* in, const int32_t* counts, void* records,
-                                   gstex_stream_t s) {
+                                   void* workspace, size_t workspace_bytes, gstex_stream_t s) {
     SceneArgs a;
     BatchArgs ba;
     int rc = batch_scene(in, a, ba);
     if (rc) return rc;
-    GSTEX_REQUIRE(records && ((uintptr_t)records & 15) == 0);
+    GSTEX_REQUIRE(records && ((uintptr_t)records & 15) == 0 && workspace && ((uintptr_t)workspace & 15) == 0);
+    if ((unsigned long long)a.N * (unsigned long long)in->num_views > 0xffffffffull) return GSTEX_ERR_UNSUPPORTED;
+    if (workspace_bytes < gstex_batch_records_workspace_bytes(a.N, in->num_views)) return GSTEX_ERR_CAPACITY;
     if (a.N > 0) GSTEX_REQUIRE(counts);
-    return launch_records(a, ba, in->num_views, counts, (RecAll*)records, (cudaStream_t)s);
+    unsigned char* ws = (unsigned char*)workspace;
+    return launch_records(a, ba, in->num_views, counts, (RecAll*)records, (int*)ws, (uint32_t*)(ws + 16),
+                          (cudaStream_t)s);
 }
 
 static int grid_of(const gstex_batch_inputs* in, bool backward) {

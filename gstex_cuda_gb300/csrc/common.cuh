@@ -172,10 +172,33 @@ struct Recs {
 __device__ __forceinline__ float4 f4(float3 v, float w) { return make_float4(v.x, v.y, v.z, w); }
 __device__ __forceinline__ float3 f3(float4 v) { return make_float3(v.x, v.y, v.z); }
 
-__device__ __forceinline__ void make_record(RecHot& H, RecWarm& Wm, RecCold& Cd, int gid, const View& V,
+// Near-edge-on splats (|n_c . d0| < kEdgeOn): the plane coefficients in
+// double.  Writes H.a, H.b.x/.y, H.c and Wm.uvm.
+constexpr float kEdgeOn = 0.05f;
+__device__ __forceinline__ void edge_on_solve(RecHot& H, RecWarm& Wm, const View& V, float3 mc, float3 a1c,
+                                              float3 a2c, float3 nc, float3 umc, float3 vmc, float is1, float is2,
+                                              float tvn) {
+    const double mz = mc.z, imz = 1.0 / mz;
+    const double u0 = (double)mc.x * imz, v0 = (double)mc.y * imz;
+    const double g = (double)nc.x * u0 + (double)nc.y * v0 + nc.z;
+    const double ifx = 1.0 / V.fx, ify = 1.0 / V.fy;
+    const double a1d = a1c.x * u0 + a1c.y * v0 + a1c.z, a2d = a2c.x * u0 + a2c.y * v0 + a2c.z;
+    const double umd = umc.x * u0 + umc.y * v0 + umc.z, vmd = vmc.x * u0 + vmc.y * v0 + vmc.z;
+    H.a = make_float4((float)(V.fx * u0 + V.cx), (float)(V.fy * v0 + V.cy), (float)g, tvn);
+    H.b.x = (float)(nc.x * ifx);
+    H.b.y = (float)(nc.y * ify);
+    H.c = make_float4((float)(mz * (g * a1c.x - a1d * nc.x) * ifx * is1),
+                      (float)(mz * (g * a1c.y - a1d * nc.y) * ify * is1),
+                      (float)(mz * (g * a2c.x - a2d * nc.x) * ifx * is2),
+                      (float)(mz * (g * a2c.y - a2d * nc.y) * ify * is2));
+    Wm.uvm = make_float4((float)(mz * (g * umc.x - umd * nc.x) * ifx), (float)(mz * (g * umc.y - umd * nc.y) * ify),
+                         (float)(mz * (g * vmc.x - vmd * nc.x) * ifx), (float)(mz * (g * vmc.y - vmd * nc.y) * ify));
+}
+
+__device__ __forceinline__ bool make_record(RecHot& H, RecWarm& Wm, RecCold& Cd, int gid, const View& V,
                                             const float3 mean, const float4 quat, const float2 scale,
                                             float glob_scale, float opac, float3 color, float2 uv0, float3 umap,
-                                            float3 vmap, int3 dims, bool use_blur) {
+                                            float3 vmap, int3 dims, bool use_blur, bool allow_double = true) {
     const Axes A = quat_axes(quat);
     const float3 mc = V.xform(mean);
     const float3 a1c = V.rot(A.a1), a2c = V.rot(A.a2), nc = V.rot(A.a3);
@@ -236,37 +259,29 @@ __device__ __forceinline__ void make_record(RecHot& H, RecWarm& Wm, RecCold& Cd,
         H.c = make_float4(0.f, 0.f, 0.f, 0.f);
         H.d = make_float4(y0, y1, opac, __int_as_float(flags));
         Wm.uvm = make_float4(0.f, 0.f, 0.f, 0.f);
-        return;
+        return false;
     }
+    H.b.z = x0;
+    H.b.w = x1;
     const float u0f = mc.x / mc.z, v0f = mc.y / mc.z;
     const float gf = nc.x * u0f + nc.y * v0f + nc.z;
-    if (fabsf(gf) < 0.05f) {
-        // near edge-on splat: the coefficient algebra runs in double
-        const double mz = mc.z, u0 = (double)mc.x / mz, v0 = (double)mc.y / mz;
-        const double g = (double)nc.x * u0 + (double)nc.y * v0 + nc.z;
-        const double ifx = 1.0 / V.fx, ify = 1.0 / V.fy;
-        const double a1d = a1c.x * u0 + a1c.y * v0 + a1c.z, a2d = a2c.x * u0 + a2c.y * v0 + a2c.z;
-        const double umd = umc.x * u0 + umc.y * v0 + umc.z, vmd = vmc.x * u0 + vmc.y * v0 + vmc.z;
-        H.a = make_float4((float)(V.fx * u0 + V.cx), (float)(V.fy * v0 + V.cy), (float)g, tvn);
-        H.b = make_float4((float)(nc.x * ifx), (float)(nc.y * ify), x0, x1);
-        H.c = make_float4((float)(mz * (g * a1c.x - a1d * nc.x) * ifx * is1),
-                          (float)(mz * (g * a1c.y - a1d * nc.y) * ify * is1),
-                          (float)(mz * (g * a2c.x - a2d * nc.x) * ifx * is2),
-                          (float)(mz * (g * a2c.y - a2d * nc.y) * ify * is2));
-        Wm.uvm = make_float4((float)(mz * (g * umc.x - umd * nc.x) * ifx), (float)(mz * (g * umc.y - umd * nc.y) * ify),
-                             (float)(mz * (g * vmc.x - vmd * nc.x) * ifx), (float)(mz * (g * vmc.y - vmd * nc.y) * ify));
+    const bool edge_on = fabsf(gf) < kEdgeOn;
+    if (edge_on && allow_double) {
+        edge_on_solve(H, Wm, V, mc, a1c, a2c, nc, umc, vmc, is1, is2, tvn);
     } else {
         const float mz = mc.z, ifx = 1.f / V.fx, ify = 1.f / V.fy;
         const float a1d = a1c.x * u0f + a1c.y * v0f + a1c.z, a2d = a2c.x * u0f + a2c.y * v0f + a2c.z;
         const float umd = umc.x * u0f + umc.y * v0f + umc.z, vmd = vmc.x * u0f + vmc.y * v0f + vmc.z;
         H.a = make_float4(V.fx * u0f + V.cx, V.fy * v0f + V.cy, gf, tvn);
-        H.b = make_float4(nc.x * ifx, nc.y * ify, x0, x1);
+        H.b.x = nc.x * ifx;
+        H.b.y = nc.y * ify;
         H.c = make_float4(mz * (gf * a1c.x - a1d * nc.x) * ifx * is1, mz * (gf * a1c.y - a1d * nc.y) * ify * is1,
                           mz * (gf * a2c.x - a2d * nc.x) * ifx * is2, mz * (gf * a2c.y - a2d * nc.y) * ify * is2);
         Wm.uvm = make_float4(mz * (gf * umc.x - umd * nc.x) * ifx, mz * (gf * umc.y - umd * nc.y) * ify,
                              mz * (gf * vmc.x - vmd * nc.x) * ifx, mz * (gf * vmc.y - vmd * nc.y) * ify);
     }
     H.d = make_float4(y0, y1, opac, __int_as_float(flags));
+    return edge_on && !allow_double;
 }
 
 // Per-pixel constants: pixel centre, camera direction d = (u, v, 1), |d|.

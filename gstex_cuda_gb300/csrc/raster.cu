@@ -763,25 +763,54 @@ __global__ void BWD_BOUNDS(PPT) bwd_batch_kernel(SceneArgs a, BatchArgs ba, BwdA
 
 // Records of every (view, Gaussian) pair with tiles in the view, and of
 // Gaussian 0 in every view (the reference's zero-slot entries name it).
-// grid.y = view.
+// grid.y = view.  Near-edge-on pairs get fp32 coefficients here and are
+// appended to `fix` for records_fixup_kernel: on this GPU one lane in the
+// double branch would hold its whole warp at the fp64 rate.
 __global__ void records_kernel(SceneArgs a, BatchArgs ba, const int32_t* __restrict__ counts,
-                               RecAll* __restrict__ recs) {
+                               RecAll* __restrict__ recs, int* __restrict__ fix_count, uint32_t* __restrict__ fix) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ba.num_points) return;
     const size_t j = (size_t)blockIdx.y * ba.num_points + i;
     if (counts[j] <= 0 && i != 0) return;
     const View V = ba.views[blockIdx.y].V;
     RecAll r;
-    make_record(r.h, r.w, r.c, i, V, a.means[i], a.quats[i], make_float2(a.scales[3 * i], a.scales[3 * i + 1]), a.glob,
-                a.opac[i], ba.colors[j], a.uv0[i], a.umap[i], a.vmap[i], a.dims[i], a.settings & (1 << 9));
+    const bool defer = make_record(r.h, r.w, r.c, i, V, a.means[i], a.quats[i],
+                                   make_float2(a.scales[3 * i], a.scales[3 * i + 1]), a.glob, a.opac[i], ba.colors[j],
+                                   a.uv0[i], a.umap[i], a.vmap[i], a.dims[i], a.settings & (1 << 9), false);
     recs[j] = r;
+    if (defer) fix[atomicAdd(fix_count, 1)] = (uint32_t)j;
+}
+
+// The double solve of the deferred near-edge-on records, densely.
+__global__ void records_fixup_kernel(SceneArgs a, BatchArgs ba, const int* __restrict__ fix_count,
+                                     const uint32_t* __restrict__ fix, RecAll* __restrict__ recs) {
+    const int n = *fix_count;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const uint32_t j = fix[t];
+        const int v = (int)(j / (uint32_t)ba.num_points);
+        const int i = (int)(j - (uint32_t)v * (uint32_t)ba.num_points);
+        const View V = ba.views[v].V;
+        const Axes A = quat_axes(a.quats[i]);
+        const float3 mc = V.xform(a.means[i]);
+        const float3 a1c = V.rot(A.a1), a2c = V.rot(A.a2), nc = V.rot(A.a3);
+        const float3 umc = V.rot(a.umap[i]), vmc = V.rot(a.vmap[i]);
+        const float is1 = 1.f / (a.scales[3 * i] * a.glob), is2 = 1.f / (a.scales[3 * i + 1] * a.glob);
+        RecHot h = recs[j].h;
+        RecWarm w = recs[j].w;
+        edge_on_solve(h, w, V, mc, a1c, a2c, nc, umc, vmc, is1, is2, dot3(nc, mc));
+        recs[j].h = h;
+        recs[j].w.uvm = w.uvm;
+    }
 }
 
 int launch_records(const SceneArgs& a, const BatchArgs& ba, int num_views, const int32_t* counts, RecAll* recs,
-                   cudaStream_t stream) {
+                   int* fix_count, uint32_t* fix, cudaStream_t stream) {
     if (a.N == 0) return GSTEX_OK;
-    records_kernel<<<dim3(ceil_div(a.N, 128), num_views), 128, 0, stream>>>(a, ba, counts, recs);
-    return check_launch("batch_records");
+    cudaError_t e = cudaMemsetAsync(fix_count, 0, sizeof(int), stream);
+    if (e != cudaSuccess) { set_cuda_error(e, "batch_records"); return GSTEX_ERR_CUDA; }
+    records_kernel<<<dim3(ceil_div(a.N, 128), num_views), 128, 0, stream>>>(a, ba, counts, recs, fix_count, fix);
+    records_fixup_kernel<<<152 * 4, 128, 0, stream>>>(a, ba, fix_count, fix, recs);
+    return check_launch("batch_records", 2);
 }
 
 // Moments -> parameter gradients (one thread per Gaussian).  Colour gradients

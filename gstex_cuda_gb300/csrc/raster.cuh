@@ -108,6 +108,6 @@ int launch_finalize(const SceneArgs& a, const float* moments, float* v_opac, flo
                     float* v_quats, float* v_uv0, float* v_umap, float* v_vmap, cudaStream_t stream);
 int resident_ctas(int bw, bool backward, int texmode, int C, int ppt);
 int launch_records(const SceneArgs& a, const BatchArgs& ba, int num_views, const int32_t* counts, RecAll* recs,
-                   cudaStream_t stream);
+                   int* fix_count, uint32_t* fix, cudaStream_t stream);
 
 }  // namespace gstex

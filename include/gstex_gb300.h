@@ -302,16 +302,21 @@ typedef struct gstex_batch_inputs {
  * (176 bytes per pair). */
 size_t gstex_batch_records_bytes(int num_points, int num_views);
 
+/* Workspace of gstex_batch_records: a counter and one index per pair. */
+size_t gstex_batch_records_workspace_bytes(int num_points, int num_views);
+
 /* Builds the splat record (camera-space plane coefficients, alpha >= 1/255
  * screen box, colour, chart) of every (view, Gaussian) pair whose tile count
  * in `counts` ([V, N], from gstex_batch_project) is positive, and of
  * Gaussian 0 in every view, once per step; near-edge-on splats are solved in
- * double here.  Pass the buffer as in->records to the forward and backward,
- * which then copy records instead of deriving them per tile.  Reads
- * in->colors, the Gaussian parameters and in->views.  No reference
- * counterpart (the reference derives the same quantities per pixel,
+ * double here (gathered first, then solved by a second kernel).  Pass the
+ * buffer as in->records to the forward and backward, which then copy records
+ * instead of deriving them per tile.  Reads in->colors, the Gaussian
+ * parameters and in->views; needs N * V < 2^32.  No reference counterpart
+ * (the reference derives the same quantities per pixel,
  * csrc/texture.cu:160-181). */
-int gstex_batch_records(const gstex_batch_inputs* in, const int32_t* counts, void* records, gstex_stream_t stream);
+int gstex_batch_records(const gstex_batch_inputs* in, const int32_t* counts, void* records, void* workspace,
+                        size_t workspace_bytes, gstex_stream_t stream);
 
 /* Forward of all views: outputs are the concatenated per-view buffers
  * (pixel p of view v at pix_offsets[v] + p).  Batched texture_forward. */
