@@ -146,42 +146,75 @@ __global__ void __launch_bounds__(kSortThreads) radix_hist_kernel(const uint64_t
     for (int d = threadIdx.x; d < kRadix; d += blockDim.x) hist[(size_t)d * gridDim.x + blockIdx.x] = h[d];
 }
 
-// Exclusive scan of total = kRadix * blocks counters by one block.
-__global__ void __launch_bounds__(1024) radix_scan_kernel(uint32_t* __restrict__ data, int total) {
-    __shared__ uint32_t partial[1024];
-    const int per = ceil_div(total, (int)blockDim.x);
-    const int s = threadIdx.x * per;
-    const int e = min(s + per, total);
-    uint32_t sum = 0;
-    for (int i = s; i < e; i++) sum += data[i];
-    partial[threadIdx.x] = sum;
+// Block-wide exclusive scan of one value per thread (blockDim.x == kSortThreads);
+// *total receives the sum.  Ends with a barrier.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* wsum, uint32_t* total) {
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (unsigned)o) x += y;
+    }
+    if (lane == 31) wsum[warp] = x;
     __syncthreads();
-    for (int o = 1; o < (int)blockDim.x; o <<= 1) {
-        uint32_t y = threadIdx.x >= (unsigned)o ? partial[threadIdx.x - o] : 0u;
-        __syncthreads();
-        partial[threadIdx.x] += y;
-        __syncthreads();
+    if (warp == 0) {
+        uint32_t t = lane < (unsigned)kSortWarps ? wsum[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < kSortWarps; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= (unsigned)o) t += y;
+        }
+        if (lane < (unsigned)kSortWarps) wsum[lane] = t;
     }
-    uint32_t run = partial[threadIdx.x] - sum;
-    for (int i = s; i < e; i++) {
-        const uint32_t v = data[i];
-        data[i] = run;
-        run += v;
-    }
+    __syncthreads();
+    const uint32_t before = (warp ? wsum[warp - 1] : 0u) + x - v;
+    if (total) *total = wsum[kSortWarps - 1];
+    __syncthreads();
+    return before;
 }
 
+// Exclusive scan of each digit's row of per-block counts, one block per
+// digit; the row total goes to totals[digit].
+__global__ void __launch_bounds__(kSortThreads) radix_scan_rows_kernel(uint32_t* __restrict__ hist, int blocks,
+                                                                       uint32_t* __restrict__ totals) {
+    __shared__ uint32_t wsum[kSortWarps];
+    uint32_t* row = hist + (size_t)blockIdx.x * blocks;
+    uint32_t carry = 0;
+    for (int base = 0; base < blocks; base += kSortThreads) {
+        const int i = base + threadIdx.x;
+        const uint32_t v = i < blocks ? row[i] : 0u;
+        uint32_t sum;
+        const uint32_t before = block_exclusive_scan(v, wsum, &sum);
+        if (i < blocks) row[i] = carry + before;
+        carry += sum;
+    }
+    if (threadIdx.x == 0) totals[blockIdx.x] = carry;
+}
+
+// Stable scatter of one block's chunk, 2048 items at a time: items are ranked
+// by digit (warp match + per-warp counters, so equal digits keep their input
+// order), regrouped by digit in shared memory, and written out as runs of
+// consecutive positions.
 __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
     const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
     uint32_t* __restrict__ vout, int n, int chunk, const int64_t* __restrict__ n_dev, int shift,
-    const uint32_t* __restrict__ offsets) {
+    const uint32_t* __restrict__ offsets, const uint32_t* __restrict__ totals) {
     __shared__ uint32_t run_off[kRadix];
-    resolve_count(n_dev, n, chunk);
-    __shared__ uint32_t tile_tot[kRadix];
+    __shared__ uint32_t tile_base[kRadix];
+    __shared__ uint32_t wsum[kSortWarps];
     __shared__ uint32_t wcnt[kSortWarps][kRadix];
+    __shared__ uint64_t skey[kSortTile];
+    __shared__ uint32_t sval[kSortTile];
+    resolve_count(n_dev, n, chunk);
     const int tid = threadIdx.x, warp = tid >> 5;
     const unsigned lane = tid & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
-    for (int d = tid; d < kRadix; d += blockDim.x) run_off[d] = offsets[(size_t)d * gridDim.x + blockIdx.x];
+    // digit d starts at (sum of the totals of smaller digits) + (this block's row prefix)
+    {
+        const uint32_t base = block_exclusive_scan(totals[tid], wsum, nullptr);
+        run_off[tid] = base + offsets[(size_t)tid * gridDim.x + blockIdx.x];
+    }
     const int start = blockIdx.x * chunk;
     const int end = min(start + chunk, n);
     for (int tbase = start; tbase < end; tbase += kSortTile) {
@@ -209,29 +242,42 @@ __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
             __syncwarp();
         }
         __syncthreads();
-        for (int d = tid; d < kRadix; d += blockDim.x) {
-            uint32_t tot = 0;
+        // per-warp offsets within each digit, then the digit's start in the tile
+        uint32_t tot = 0;
 #pragma unroll
-            for (int w = 0; w < kSortWarps; w++) {
-                const uint32_t c = wcnt[w][d];
-                wcnt[w][d] = tot;
-                tot += c;
-            }
-            tile_tot[d] = tot;
+        for (int w = 0; w < kSortWarps; w++) {
+            const uint32_t c = wcnt[w][tid];
+            wcnt[w][tid] = tot;
+            tot += c;
         }
+        const uint32_t tb = block_exclusive_scan(tot, wsum, nullptr);
+        tile_base[tid] = tb;
         __syncthreads();
 #pragma unroll
         for (int k = 0; k < kSortItems; k++) {
             const int i = tbase + warp * (32 * kSortItems) + k * 32 + (int)lane;
             if (i < end) {
                 const uint32_t d = (uint32_t)(key[k] >> shift) & (kRadix - 1);
-                const uint32_t pos = run_off[d] + wcnt[warp][d] + rank[k];
-                kout[pos] = key[k];
-                vout[pos] = val[k];
+                const uint32_t local = tile_base[d] + wcnt[warp][d] + rank[k];
+                skey[local] = key[k];
+                sval[local] = val[k];
             }
         }
         __syncthreads();
-        for (int d = tid; d < kRadix; d += blockDim.x) run_off[d] += tile_tot[d];
+        const int tile_n = min(kSortTile, end - tbase);
+        for (int l = tid; l < tile_n; l += kSortThreads) {
+            const uint64_t kk = skey[l];
+            const uint32_t d = (uint32_t)(kk >> shift) & (kRadix - 1);
+            const uint32_t pos = run_off[d] + (uint32_t)l - tile_base[d];
+            kout[pos] = kk;
+            vout[pos] = sval[l];
+        }
+        __syncthreads();
+        // advance each digit's cursor by the tile's count of that digit
+        {
+            const uint32_t next = (tid + 1 < kRadix) ? tile_base[tid + 1] : (uint32_t)tile_n;
+            run_off[tid] += next - tile_base[tid];
+        }
         __syncthreads();
     }
 }
@@ -258,7 +304,8 @@ extern "C" int gstex_map_gaussian_to_intersects(int n, int num_isect, const floa
 extern "C" size_t gstex_sort_workspace_bytes(int n) {
     if (n < 1) n = 1;
     const SortPlan p = sort_plan(n);
-    return align_up((size_t)n * 8, 256) + align_up((size_t)n * 4, 256) + (size_t)kRadix * p.blocks * 4;
+    return align_up((size_t)n * 8, 256) + align_up((size_t)n * 4, 256) + (size_t)kRadix * p.blocks * 4 +
+           (size_t)kRadix * 4;
 }
 
 static int sort_impl(int n, const int64_t* n_dev, int end_bit, const int64_t* keys_in, const int32_t* vals_in,
@@ -282,6 +329,7 @@ static int sort_impl(int n, const int64_t* n_dev, int end_bit, const int64_t* ke
     uint32_t* valt = (uint32_t*)w;
     w += align_up((size_t)n * 4, 256);
     uint32_t* hist = (uint32_t*)w;
+    uint32_t* totals = hist + (size_t)kRadix * p.blocks;
     // Ping-pong so that the last pass lands in the output buffers.
     const uint64_t* ksrc = (const uint64_t*)keys_in;
     const uint32_t* vsrc = (const uint32_t*)vals_in;
@@ -291,9 +339,9 @@ static int sort_impl(int n, const int64_t* n_dev, int end_bit, const int64_t* ke
         uint32_t* vdst = to_out ? (uint32_t*)vals_out : valt;
         const int shift = pass * 8;
         radix_hist_kernel<<<p.blocks, kSortThreads, 0, stream>>>(ksrc, n, p.chunk, n_dev, shift, hist);
-        radix_scan_kernel<<<1, 1024, 0, stream>>>(hist, kRadix * p.blocks);
+        radix_scan_rows_kernel<<<kRadix, kSortThreads, 0, stream>>>(hist, p.blocks, totals);
         radix_scatter_kernel<<<p.blocks, kSortThreads, 0, stream>>>(ksrc, vsrc, kdst, vdst, n, p.chunk, n_dev, shift,
-                                                                    hist);
+                                                                    hist, totals);
         ksrc = kdst;
         vsrc = vdst;
     }

@@ -23,9 +23,9 @@ namespace gstex {
 
 // Scratch of gstex_sort_pairs at GSTEX_SORT_STATIC_MAX_ITEMS pairs: alternate
 // keys (8 B/pair) + alternate values (4 B/pair) + 256 digit counters for each
-// of 512 blocks.
+// of 512 blocks + 256 digit totals.
 constexpr size_t kStaticScratchBytes = (size_t)GSTEX_SORT_STATIC_MAX_ITEMS * 8 +
-                                       (size_t)GSTEX_SORT_STATIC_MAX_ITEMS * 4 + 256 * 512 * 4;
+                                       (size_t)GSTEX_SORT_STATIC_MAX_ITEMS * 4 + 256 * 512 * 4 + 256 * 4;
 
 static __device__ __align__(256) unsigned char g_sort_scratch[kStaticScratchBytes];
 
