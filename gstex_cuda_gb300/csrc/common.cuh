@@ -146,6 +146,16 @@ struct RecCold {  // the backward's ray terms and the blur adjoint
 };
 constexpr int kRecBytes = sizeof(RecHot) + sizeof(RecWarm) + sizeof(RecCold);
 
+// The four edges of the projected alpha >= 1/255 rectangle (a convex quad
+// inside the screen box): a pixel centre (x, y) can only meet the splat where
+// A.k x + B.k y + C.k >= 0 for every edge k (pixel units, with a margin).
+// Used by the backward's candidate lists; all-pass (A = B = 0, C = 1) where
+// the box is infinite, with blur, or for a degenerate edge.
+struct RecEdge {
+    float4 A, B, C;
+};
+constexpr int kEdgeBytes = sizeof(RecEdge);
+
 // One (view, Gaussian) record as the batched path stores it in device memory:
 // built once per view by the record kernel (where the near-edge-on solve runs
 // in double), then copied into shared memory by every tile the splat touches.
@@ -153,18 +163,21 @@ struct __align__(16) RecAll {
     RecHot h;
     RecWarm w;
     RecCold c;
+    RecEdge e;
 };
-static_assert(sizeof(RecAll) == kRecBytes, "record layout");
+static_assert(sizeof(RecAll) == kRecBytes + kEdgeBytes, "record layout");
 
 struct Recs {
     RecHot* hot;
     RecWarm* warm;
     RecCold* cold;
-    __device__ __forceinline__ static Recs carve(unsigned char* smem, int n) {
+    RecEdge* edge;  // null when the kernel does not stage edges
+    __device__ __forceinline__ static Recs carve(unsigned char* smem, int n, bool with_edges) {
         Recs r;
         r.hot = reinterpret_cast<RecHot*>(smem);
         r.warm = reinterpret_cast<RecWarm*>(smem + sizeof(RecHot) * n);
         r.cold = reinterpret_cast<RecCold*>(smem + (sizeof(RecHot) + sizeof(RecWarm)) * n);
+        r.edge = with_edges ? reinterpret_cast<RecEdge*>(smem + (size_t)kRecBytes * n) : nullptr;
         return r;
     }
 };
@@ -195,10 +208,56 @@ __device__ __forceinline__ void edge_on_solve(RecHot& H, RecWarm& Wm, const View
                          (float)(mz * (g * vmc.x - vmd * nc.x) * ifx), (float)(mz * (g * vmc.y - vmd * nc.y) * ify));
 }
 
+// Edges of the convex quad with corners k = 0 (+,+), 1 (-,+), 3 (-,-), 2 (+,-)
+// in cyclic order, oriented so that the quad's centroid is inside, normalised
+// to pixel distances and widened by a margin; a degenerate edge passes all.
+__device__ __forceinline__ void quad_edges(const float (&qx)[4], const float (&qy)[4], RecEdge& E) {
+    const int cyc[5] = { 0, 1, 3, 2, 0 };
+    const float gx = 0.25f * (qx[0] + qx[1] + qx[2] + qx[3]), gy = 0.25f * (qy[0] + qy[1] + qy[2] + qy[3]);
+    const float margin = 0.05f + 1e-5f * (fabsf(gx) + fabsf(gy));
+    float A[4], B[4], C[4];
+    float side = 0.f;
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+        const int i = cyc[e], j = cyc[e + 1];
+        const float ax = -(qy[j] - qy[i]), by = qx[j] - qx[i];
+        const float len = sqrtf(ax * ax + by * by);
+        if (len > 1e-3f) {
+            const float il = 1.f / len;
+            A[e] = ax * il;
+            B[e] = by * il;
+            C[e] = -(A[e] * qx[i] + B[e] * qy[i]);
+            side += A[e] * gx + B[e] * gy + C[e];
+        } else {
+            A[e] = B[e] = 0.f;
+            C[e] = 1.f;
+        }
+    }
+    if (fabsf(side) < 1e-3f) {  // a quad of (near) zero width: no usable orientation
+        E.A = E.B = make_float4(0.f, 0.f, 0.f, 0.f);
+        E.C = make_float4(1.f, 1.f, 1.f, 1.f);
+        return;
+    }
+    const float sg = side < 0.f ? -1.f : 1.f;
+    // a flipped edge keeps C = 1 for the degenerate (all-pass) case
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+        if (A[e] != 0.f || B[e] != 0.f) {
+            A[e] *= sg;
+            B[e] *= sg;
+            C[e] = C[e] * sg + margin;
+        }
+    }
+    E.A = make_float4(A[0], A[1], A[2], A[3]);
+    E.B = make_float4(B[0], B[1], B[2], B[3]);
+    E.C = make_float4(C[0], C[1], C[2], C[3]);
+}
+
 __device__ __forceinline__ bool make_record(RecHot& H, RecWarm& Wm, RecCold& Cd, int gid, const View& V,
                                             const float3 mean, const float4 quat, const float2 scale,
                                             float glob_scale, float opac, float3 color, float2 uv0, float3 umap,
-                                            float3 vmap, int3 dims, bool use_blur, bool allow_double = true) {
+                                            float3 vmap, int3 dims, bool use_blur, bool allow_double = true,
+                                            RecEdge* E = nullptr) {
     const Axes A = quat_axes(quat);
     const float3 mc = V.xform(mean);
     const float3 a1c = V.rot(A.a1), a2c = V.rot(A.a2), nc = V.rot(A.a3);
@@ -220,10 +279,15 @@ __device__ __forceinline__ bool make_record(RecHot& H, RecWarm& Wm, RecCold& Cd,
     const float smax = __logf(255.f * opac);
     int flags = 0;
     if (!(mc.z > kTNear)) flags = 1;
+    if (E) {
+        E->A = E->B = make_float4(0.f, 0.f, 0.f, 0.f);
+        E->C = make_float4(1.f, 1.f, 1.f, 1.f);
+    }
     if (smax > 0.f) {
         const float a = sqrtf(2.f * smax + 1e-3f) * 1.002f;
         const float e1 = a / is1, e2 = a / is2;
         bool front = !flags;
+        float qx[4], qy[4];
 #pragma unroll
         for (int k = 0; k < 4; k++) {
             const float s1 = (k & 1) ? -e1 : e1, s2 = (k & 2) ? -e2 : e2;
@@ -232,12 +296,15 @@ __device__ __forceinline__ bool make_record(RecHot& H, RecWarm& Wm, RecCold& Cd,
             front = front && c.z > 1e-3f;
             const float iz = 1.f / c.z;
             const float px = V.fx * c.x * iz + V.cx, py = V.fy * c.y * iz + V.cy;
+            qx[k] = px;
+            qy[k] = py;
             x0 = fminf(x0, px); x1 = fmaxf(x1, px);
             y0 = fminf(y0, py); y1 = fmaxf(y1, py);
         }
         if (front) {
             const float mx = 1e-2f + 1e-5f * (fabsf(x0) + fabsf(x1)), my = 1e-2f + 1e-5f * (fabsf(y0) + fabsf(y1));
             x0 -= mx; x1 += mx; y0 -= my; y1 += my;
+            if (E && !use_blur) quad_edges(qx, qy, *E);
         } else {
             x0 = y0 = -INFINITY;
             x1 = y1 = INFINITY;

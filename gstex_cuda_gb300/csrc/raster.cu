@@ -27,7 +27,7 @@ __device__ __forceinline__ void stage(const Recs& R, int slot, const SceneArgs& 
                                       int gid, bool use_blur) {
     make_record(R.hot[slot], R.warm[slot], R.cold[slot], gid, V, a.means[gid], a.quats[gid],
                 make_float2(a.scales[3 * gid], a.scales[3 * gid + 1]), a.glob, a.opac[gid], colors[gid], a.uv0[gid],
-                a.umap[gid], a.vmap[gid], a.dims[gid], use_blur);
+                a.umap[gid], a.vmap[gid], a.dims[gid], use_blur, true, R.edge ? R.edge + slot : nullptr);
 }
 
 // Stages the record of Gaussian gid for one tile: a copy of the prebuilt
@@ -49,6 +49,11 @@ __device__ __forceinline__ void stage_job(const Recs& R, int slot, const SceneAr
         for (int q = 0; q < nw; q++) warm[q] = v[nh + q];
 #pragma unroll
         for (int q = 0; q < nc; q++) cold[q] = v[nh + nw + q];
+        if (R.edge) {
+            uint4* edge = reinterpret_cast<uint4*>(R.edge + slot);
+#pragma unroll
+            for (int q = 0; q < kEdgeBytes / 16; q++) edge[q] = __ldg(src + kRecBytes / 16 + q);
+        }
     } else {
         stage(R, slot, a, J.V, J.colors, gid, use_blur);
     }
@@ -113,6 +118,10 @@ __device__ __forceinline__ void fetch3(const void* tex, const Bilerp& B, float c
 #endif
 // Candidate lists in the forward (off: forward pixels saturate early, and
 // walking every staged slot with a per-thread box test measured faster).
+// Warps with at most this many valid lanes skip the transpose reduction.
+#ifndef GSTEX_SPARSE_LANES
+#define GSTEX_SPARSE_LANES 0
+#endif
 #ifndef GSTEX_FWD_LIST
 #define GSTEX_FWD_LIST 0
 #endif
@@ -143,6 +152,16 @@ __device__ __forceinline__ int build_list(uint8_t* wl, const Recs& R, int k0, in
         if (kk < bsize) {
             const float4 hb = R.hot[kk].b, hd = R.hot[kk].d;
             hit = !(hb.w < rx0 || hb.z > rx1 || hd.y < ry0 || hd.x > ry1);
+            if (hit && R.edge) {
+                // separating axes of the splat's quad: the rectangle's corner
+                // furthest inside each edge must be inside it
+                const RecEdge e = R.edge[kk];
+                const float ea[4] = { e.A.x, e.A.y, e.A.z, e.A.w }, eb[4] = { e.B.x, e.B.y, e.B.z, e.B.w };
+                const float ec[4] = { e.C.x, e.C.y, e.C.z, e.C.w };
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    hit = hit && ea[q] * (ea[q] > 0.f ? rx1 : rx0) + eb[q] * (eb[q] > 0.f ? ry1 : ry0) + ec[q] >= 0.f;
+            }
         }
         const unsigned m = __ballot_sync(wmask, hit);
         if (hit) wl[cnt + __popc(m & ((1u << lane) - 1u))] = (uint8_t)kk;
@@ -626,7 +645,8 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
                     bwd_pair<TEXMODE, CT, CA>(a, g, R, k, gidx, Hr, H[p], alpha[p], e[p], eb[p], nbf[p], bf[p], S[p],
                                               C, use_ndc, prop_uv, bilinear, m);
             float* dst = smom + k * kMoments;
-            if (full_warp) {
+            // few valid lanes: each adds its own moments; else one transpose reduction
+            if (full_warp && __popc(vmask) > GSTEX_SPARSE_LANES) {
                 const float s = warp_transpose_reduce(m, lane);
                 if (lane < (unsigned)kMoments) atomicAdd(dst + lane, s);
             } else if (any) {
@@ -696,7 +716,7 @@ __global__ void FWD_BOUNDS(PPT) fwd_view_kernel(SceneArgs a, ViewArgs va, FwdOut
     J.vcolors = nullptr;
     J.recs = nullptr;
     const int nthr = blockDim.x * blockDim.y;
-    fwd_tile<TEXMODE, CT, PPT>(a, J, o, Recs::carve(smem, nthr), smem + (size_t)kRecBytes * nthr);
+    fwd_tile<TEXMODE, CT, PPT>(a, J, o, Recs::carve(smem, nthr, false), smem + (size_t)kRecBytes * nthr);
 }
 
 template <int TEXMODE, int CT, int PPT>
@@ -712,8 +732,9 @@ __global__ void BWD_BOUNDS(PPT) bwd_view_kernel(SceneArgs a, ViewArgs va, BwdArg
     J.colors = va.colors;
     J.vcolors = va.vcolors;
     J.recs = nullptr;
-    bwd_tile<TEXMODE, CT, PPT>(a, J, g, Recs::carve(smem, nthr), reinterpret_cast<float*>(smem + (size_t)kRecBytes * nthr),
-                               smem + (size_t)(kRecBytes + kMoments * sizeof(float)) * nthr);
+    bwd_tile<TEXMODE, CT, PPT>(a, J, g, Recs::carve(smem, nthr, true),
+                               reinterpret_cast<float*>(smem + (size_t)(kRecBytes + kEdgeBytes) * nthr),
+                               smem + (size_t)(kRecBytes + kEdgeBytes + kMoments * sizeof(float)) * nthr);
 }
 
 __device__ __forceinline__ bool next_job(const BatchArgs& ba, int* s_tile, TileJob& J) {
@@ -744,7 +765,7 @@ __global__ void FWD_BOUNDS(PPT) fwd_batch_kernel(SceneArgs a, BatchArgs ba, FwdO
     __shared__ int s_tile;
     TileJob J;
     const int nthr = blockDim.x * blockDim.y;
-    const Recs R = Recs::carve(smem, nthr);
+    const Recs R = Recs::carve(smem, nthr, false);
     uint8_t* lists = smem + (size_t)kRecBytes * nthr;
     while (next_job(ba, &s_tile, J)) fwd_tile<TEXMODE, CT, PPT>(a, J, o, R, lists);
 }
@@ -755,9 +776,9 @@ __global__ void BWD_BOUNDS(PPT) bwd_batch_kernel(SceneArgs a, BatchArgs ba, BwdA
     __shared__ int s_tile;
     const int nthr = blockDim.x * blockDim.y;
     TileJob J;
-    const Recs R = Recs::carve(smem, nthr);
-    float* smom = reinterpret_cast<float*>(smem + (size_t)kRecBytes * nthr);
-    uint8_t* lists = smem + (size_t)(kRecBytes + kMoments * sizeof(float)) * nthr;
+    const Recs R = Recs::carve(smem, nthr, true);
+    float* smom = reinterpret_cast<float*>(smem + (size_t)(kRecBytes + kEdgeBytes) * nthr);
+    uint8_t* lists = smem + (size_t)(kRecBytes + kEdgeBytes + kMoments * sizeof(float)) * nthr;
     while (next_job(ba, &s_tile, J)) bwd_tile<TEXMODE, CT, PPT>(a, J, g, R, smom, lists);
 }
 
@@ -776,7 +797,7 @@ __global__ void records_kernel(SceneArgs a, BatchArgs ba, const int32_t* __restr
     RecAll r;
     const bool defer = make_record(r.h, r.w, r.c, i, V, a.means[i], a.quats[i],
                                    make_float2(a.scales[3 * i], a.scales[3 * i + 1]), a.glob, a.opac[i], ba.colors[j],
-                                   a.uv0[i], a.umap[i], a.vmap[i], a.dims[i], a.settings & (1 << 9), false);
+                                   a.uv0[i], a.umap[i], a.vmap[i], a.dims[i], a.settings & (1 << 9), false, &r.e);
     recs[j] = r;
     if (defer) fix[atomicAdd(fix_count, 1)] = (uint32_t)j;
 }
@@ -916,7 +937,7 @@ static size_t list_bytes(int bw, int ppt) {
 }
 size_t fwd_smem(int bw, int ppt) { return (size_t)kRecBytes * threads_of(bw, ppt) + list_bytes(bw, ppt); }
 size_t bwd_smem(int bw, int ppt) {
-    return ((size_t)kRecBytes + kMoments * sizeof(float)) * threads_of(bw, ppt) + list_bytes(bw, ppt);
+    return ((size_t)kRecBytes + kEdgeBytes + kMoments * sizeof(float)) * threads_of(bw, ppt) + list_bytes(bw, ppt);
 }
 
 int launch_finalize(const SceneArgs& a, const float* moments, float* v_opac, float* v_means, float* v_scales,

@@ -299,14 +299,14 @@ typedef struct gstex_batch_inputs {
 } gstex_batch_inputs;
 
 /* Bytes of the per-(view, Gaussian) splat records of gstex_batch_records
- * (176 bytes per pair). */
+ * (224 bytes per pair). */
 size_t gstex_batch_records_bytes(int num_points, int num_views);
 
 /* Workspace of gstex_batch_records: a counter and one index per pair. */
 size_t gstex_batch_records_workspace_bytes(int num_points, int num_views);
 
 /* Builds the splat record (camera-space plane coefficients, alpha >= 1/255
- * screen box, colour, chart) of every (view, Gaussian) pair whose tile count
+ * screen box and quad, colour, chart) of every (view, Gaussian) pair whose tile count
  * in `counts` ([V, N], from gstex_batch_project) is positive, and of
  * Gaussian 0 in every view, once per step; near-edge-on splats are solved in
  * double here (gathered first, then solved by a second kernel).  Pass the
