@@ -135,6 +135,23 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
+def traffic_per_intersection():
+    """DRAM bytes per intersection of the compositor kernels, measured with ncu
+    on a smaller case of the same workload (the committed profile summary); the full
+    launch's traffic is that times its intersections."""
+    import re
+    out = {}
+    try:
+        with open(os.path.join(HERE, "profiles", "compositor_dram_traffic_4views.txt")) as f:
+            for line in f:
+                m = re.match(r"^\| (forward|backward) \|.*\| ([0-9.]+) \|$", line.strip())
+                if m:
+                    out[m.group(1)] = float(m.group(2))
+    except OSError:
+        pass
+    return out
+
+
 def algorithmic_bytes(I, tiles, T, P, C, N, tex_bytes_per_texel, grad_texel_bytes, backward):
     """Compulsory bytes of one compositor launch: per intersection a 4-byte id
     and the 96-byte fp32 Gaussian record; per tile its range; every texel once;
@@ -363,6 +380,8 @@ def main():
     peak, peak_kind = measured_peak_hbm()
     dom = ("backward", bb, bwd_ms) if bwd_ms >= fwd_ms else ("forward", fb, fwd_ms)
     achieved = dom[1] / (dom[2] / 1000.0) / 1e9
+    tpi = traffic_per_intersection().get(dom[0])
+    traffic = tpi * I if tpi else None
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -387,7 +406,8 @@ def main():
                            "autotune": tuned},
                 "e2e": e2e, "gpu_launches": int(launches),
                 "roofline": {"bound": "hbm", "kernel": dom[0], "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                             "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                             "traffic_source": "ncu dram bytes per intersection (4-view case) x intersections",
                              "algorithmic_bytes_per_launch": dom[1], "kernel_ms": dom[2]},
                 "kernels_ms": {"forward": fwd_ms, "backward": bwd_ms},
                 "graph_frames_per_s": graph_fps,
