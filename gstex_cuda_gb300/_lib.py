@@ -31,6 +31,11 @@ class RasterInputs(ctypes.Structure):
                 ("pixels_per_thread", _I)]
 
 
+class EditIO(ctypes.Structure):
+    _fields_ = [("updated_img", _P), ("updated_alpha", _P), ("depth_lower", _P), ("depth_upper", _P),
+                ("num_texels", ctypes.c_longlong), ("updated_texture", _P)]
+
+
 class ForwardOutputs(ctypes.Structure):
     _fields_ = [("img", _P), ("depth", _P), ("reg", _P), ("texture", _P), ("normal", _P), ("final_T", _P),
                 ("final_idx", _P), ("depth_idx", _P), ("reg_s", _P)]
@@ -61,6 +66,7 @@ _SIGS = {
     "gstex_sort_pairs": (_I, [_I, _I, _P, _P, _P, _P, _P, ctypes.c_size_t, _P]),
     "gstex_get_tile_bin_edges": (_I, [_I, _P, _I, _P, _P]),
     "gstex_texture_forward": (_I, [ctypes.POINTER(RasterInputs), ctypes.POINTER(ForwardOutputs), _P]),
+    "gstex_texture_edit": (_I, [ctypes.POINTER(RasterInputs), ctypes.POINTER(EditIO), _P]),
     "gstex_backward_workspace_bytes": (ctypes.c_size_t, [_I]),
     "gstex_texture_backward": (_I, [ctypes.POINTER(RasterInputs), ctypes.POINTER(BackwardIO), _P]),
     "gstex_texture_sample_forward": (_I, [_I, _I, _P, _P, _P, _P, _P]),

@@ -26,7 +26,8 @@ namespace gstex {
 __device__ __forceinline__ void stage(const Recs& R, int slot, const SceneArgs& a, const View& V, const float3* colors,
                                       int gid, bool use_blur) {
     make_record(R.hot[slot], R.warm[slot], R.cold[slot], gid, V, a.means[gid], a.quats[gid],
-                make_float2(a.scales[3 * gid], a.scales[3 * gid + 1]), a.glob, a.opac[gid], colors[gid], a.uv0[gid],
+                make_float2(a.scales[3 * gid], a.scales[3 * gid + 1]), a.glob, a.opac[gid],
+                colors ? colors[gid] : make_float3(0.f, 0.f, 0.f), a.uv0[gid],
                 a.umap[gid], a.vmap[gid], a.dims[gid], use_blur, true, R.edge ? R.edge + slot : nullptr);
 }
 
@@ -685,6 +686,104 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
 }
 
 // ---------------------------------------------------------------------------
+// Texture editing (csrc/texture_edit.cu:11-236): the forward walk, front to
+// back (blur is settings bit 0 here), and for every contributing pair whose
+// camera depth lies in the pixel's [lower, upper] range a bilinear splat of
+// (r a, g a, b a, a, 1) of the edited pixel into the chart's [T, 5] texels.
+// ---------------------------------------------------------------------------
+struct EditIO {
+    const float3* img;
+    const float* alpha;
+    const float* lower;
+    const float* upper;
+    float* out;  // [T, 5]
+};
+
+__device__ __forceinline__ void edit_tile(const SceneArgs& a, const TileJob& J, const EditIO& E, const Recs& R) {
+    const int nthr = blockDim.x * blockDim.y;
+    const int tr = threadIdx.y * blockDim.x + threadIdx.x;
+    const int bw = blockDim.x;
+    const View& V = J.V;
+    const bool use_blur = a.settings & 1;
+    const int2 lp = thread_pixel<1>(bw);
+    const int pj = J.tx * bw + lp.y, pi = J.ty * bw + lp.x;
+    const PixelRay P = make_pixel(V, pi, pj);
+    const bool inside = pi < J.H && pj < J.W;
+    bool done = !inside;
+    float vals[5] = { 0.f, 0.f, 0.f, 0.f, 1.f };
+    float lo = 0.f, hi = 0.f;
+    if (inside) {
+        const size_t pix = J.pix_base + (size_t)pi * J.W + pj;
+        const float3 c = E.img[pix];
+        const float m = E.alpha[pix];
+        vals[0] = c.x * m; vals[1] = c.y * m; vals[2] = c.z * m; vals[3] = m;
+        lo = E.lower[pix];
+        hi = E.upper[pix];
+    }
+    float T = 1.f;
+    const int2 range = J.range;
+    const int nb = ceil_div(range.y - range.x, nthr);
+    for (int b = 0; b < nb; ++b) {
+        if (__syncthreads_count(done) >= nthr) break;
+        const int bstart = range.x + nthr * b;
+        const int idx = bstart + tr;
+        if (idx < range.y) stage_job(R, tr, a, J, a.gids[idx], use_blur);
+        __syncthreads();
+        const int bsize = min(nthr, range.y - bstart);
+        for (int k = 0; k < bsize && !done; ++k) {
+            const RecHot Hr = R.hot[k];
+            // outside the alpha >= 1/255 box a splat is skipped; it can end the
+            // pixel there only when T <= 1e-4 * 255/254
+            if (outside_box(Hr, P) && T > 1.01e-4f) continue;
+            const Hit H = hit_pixel(Hr, R, k, a, V, P);
+            const float sigma = 0.5f * (H.l1s * H.l1s + H.l2s * H.l2s);
+            float nbf = 1.f, bf = 0.f, sigma_blur = 0.f;
+            if (use_blur) {
+                const float4 uvs = R.warm[k].uvs;
+                const float dx = uvs.z - P.px, dy = uvs.w - P.py;
+                sigma_blur = 0.5f * kBlurFsq * (dx * dx + dy * dy);
+                if (sigma_blur < sigma) { bf = 1.f; nbf = 0.f; }
+            }
+            const float alpha = fminf(kAlphaMax, Hr.d.z * (nbf * __expf(-sigma) + bf * __expf(-sigma_blur)));
+            const bool skip = H.t < kTNear || H.t > kTFar || alpha < kAlphaMin;
+            const float next_T = T * (1.f - alpha);
+            if (next_T <= kTDone) { done = true; continue; }
+            if (skip) continue;
+            if (H.tcam >= lo && H.tcam <= hi) {
+                const RecWarm& Wm = R.warm[k];
+                const float2 uv = hit_uv(H, Wm);
+                const int4 tx = Wm.tex;
+                const Bilerp B = bilerp(tx.x, tx.y, tx.z, clamp01(uv.x), clamp01(uv.y), true);
+                const int rows[4] = { B.i00, B.i01, B.i10, B.i11 };
+                const float wts[4] = { B.w00, B.w01, B.w10, B.w11 };
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    float* dst = E.out + 5 * (size_t)rows[q];
+#pragma unroll
+                    for (int c = 0; c < 5; c++) atomicAdd(dst + c, wts[q] * vals[c]);
+                }
+            }
+            T = next_T;
+        }
+    }
+}
+
+template <int PPT>
+__global__ void __launch_bounds__(256, 4) edit_view_kernel(SceneArgs a, ViewArgs va, EditIO E) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    TileJob J;
+    J.V = load_view(va.viewmat, va.fx, va.fy, va.cx, va.cy);
+    J.W = va.W; J.H = va.H;
+    J.tx = blockIdx.x; J.ty = blockIdx.y;
+    J.range = va.bins[blockIdx.y * va.tiles_x + blockIdx.x];
+    J.pix_base = 0;
+    J.colors = nullptr;
+    J.vcolors = nullptr;
+    J.recs = nullptr;
+    edit_tile(a, J, E, Recs::carve(smem, blockDim.x * blockDim.y, false));
+}
+
+// ---------------------------------------------------------------------------
 // Launch forms
 // ---------------------------------------------------------------------------
 // Minimum resident CTAs per SM asked of the register allocator.
@@ -1019,6 +1118,55 @@ extern "C" int gstex_texture_forward(const gstex_raster_inputs* in, const gstex_
     if ((rc = set_smem(k, fwd_smem(bw, ppt), "texture_forward"))) return rc;
     k<<<grid, block_of(bw, ppt), fwd_smem(bw, ppt), stream>>>(a, va, o);
     return check_launch("texture_forward");
+}
+
+extern "C" int gstex_texture_edit(const gstex_raster_inputs* in, const gstex_edit_io* io, gstex_stream_t s) {
+    GSTEX_REQUIRE(in && io);
+    GSTEX_REQUIRE(in->num_points >= 0 && in->img_width > 0 && in->img_height > 0);
+    GSTEX_REQUIRE(in->block_width >= 2 && in->block_width <= kMaxBlockWidth);
+    // the reference writes five channels at a stride of texture_info[2]
+    if (in->channels != 5) return GSTEX_ERR_UNSUPPORTED;
+    GSTEX_REQUIRE(in->tile_bins && in->viewmat && io->num_texels >= 0);
+    GSTEX_REQUIRE(io->updated_img && io->updated_alpha && io->depth_lower && io->depth_upper);
+    if (io->num_texels > 0) GSTEX_REQUIRE(io->updated_texture);
+    if (in->num_points > 0)
+        GSTEX_REQUIRE(in->texture_dims && in->gaussian_ids_sorted && in->opacities && in->means && in->scales &&
+                      in->quats && in->uv0 && in->umap && in->vmap);
+    cudaStream_t stream = (cudaStream_t)s;
+    if (io->num_texels > 0) {
+        cudaError_t e = cudaMemsetAsync(io->updated_texture, 0, (size_t)io->num_texels * 5 * sizeof(float), stream);
+        if (e != cudaSuccess) { set_cuda_error(e, "texture_edit"); return GSTEX_ERR_CUDA; }
+    }
+    if (in->num_points == 0) return GSTEX_OK;
+    SceneArgs a{};
+    a.N = in->num_points;
+    a.C = 5;
+    a.T = (int)io->num_texels;
+    a.dims = (const int3*)in->texture_dims;
+    a.gids = in->gaussian_ids_sorted;
+    a.means = (const float3*)in->means;
+    a.scales = in->scales;
+    a.glob = in->glob_scale;
+    a.quats = (const float4*)in->quats;
+    a.opac = in->opacities;
+    a.uv0 = (const float2*)in->uv0;
+    a.umap = (const float3*)in->umap;
+    a.vmap = (const float3*)in->vmap;
+    a.settings = in->settings;
+    const int bw = in->block_width;
+    ViewArgs va{};
+    va.viewmat = in->viewmat;
+    va.fx = in->fx; va.fy = in->fy; va.cx = in->cx; va.cy = in->cy;
+    va.W = in->img_width; va.H = in->img_height;
+    va.tiles_x = ceil_div(va.W, bw);
+    va.bins = (const int2*)in->tile_bins;
+    EditIO E{ (const float3*)io->updated_img, io->updated_alpha, io->depth_lower, io->depth_upper,
+              io->updated_texture };
+    const size_t smem = (size_t)kRecBytes * bw * bw;
+    int rc = set_smem(edit_view_kernel<1>, smem, "texture_edit");
+    if (rc) return rc;
+    edit_view_kernel<1><<<dim3(va.tiles_x, ceil_div(va.H, bw)), dim3(bw, bw), smem, stream>>>(a, va, E);
+    return check_launch("texture_edit");
 }
 
 extern "C" size_t gstex_backward_workspace_bytes(int num_points) {

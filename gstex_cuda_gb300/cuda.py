@@ -313,5 +313,45 @@ def texture_sample_backward(texture_info, texture_dims, uvs, texture, v_output, 
     return v_texture
 
 
-def texture_edit(*args, **kwargs):
-    raise NotImplementedError("texture_edit is not part of gstex_cuda_gb300 (outside the rasteriser hot path)")
+def texture_edit(tile_bounds, block, img_size, texture_info, texture_total_size, texture_dims, updated_img,
+                 updated_alpha, depth_lower, depth_upper, gaussian_ids_sorted, tile_bins, opacities, means, scales,
+                 glob_scale, quats, uv0, umap, vmap, viewmat, c2w, fx, fy, cx, cy, settings, background):
+    """Returns updated_texture [texture_total_size, 5]: per texel the bilinear
+    splat of (r*a, g*a, b*a, a) of the edited image and the total weight
+    (csrc/texture_edit.cu).  texture_info[2] must be 5 (the reference writes
+    five channels at a stride of texture_info[2]); blur is settings bit 0;
+    c2w and background are accepted for interface compatibility."""
+    named = [("texture_dims", texture_dims), ("updated_img", updated_img), ("updated_alpha", updated_alpha),
+             ("depth_lower", depth_lower), ("depth_upper", depth_upper),
+             ("gaussian_ids_sorted", gaussian_ids_sorted), ("tile_bins", tile_bins), ("opacities", opacities),
+             ("means", means), ("scales", scales), ("quats", quats), ("uv0", uv0), ("umap", umap), ("vmap", vmap),
+             ("viewmat", viewmat)]
+    _chk(*named)
+    for n, t in named:
+        if n in ("texture_dims", "gaussian_ids_sorted", "tile_bins"):
+            _i32(n, t)
+        else:
+            _f32(n, t)
+    if int(texture_info[2]) != 5:
+        raise _lib.GstexError("texture_edit: texture_info[2] must be 5 (r*a, g*a, b*a, a, weight)")
+    W, H = int(img_size[0]), int(img_size[1])
+    if updated_img.numel() != H * W * 3 or updated_alpha.numel() != H * W or depth_lower.numel() != H * W \
+            or depth_upper.numel() != H * W:
+        raise _lib.GstexError("texture_edit: per-pixel inputs must have H*W entries")
+    T = int(texture_total_size)
+    ri = _lib.RasterInputs()
+    ri.num_points = means.shape[0]
+    ri.img_width, ri.img_height, ri.block_width = W, H, int(block[0])
+    ri.channels = 5
+    ri.num_texels = T
+    ri.texture_dims, ri.gaussian_ids_sorted, ri.tile_bins = ptr(texture_dims), ptr(gaussian_ids_sorted), ptr(tile_bins)
+    ri.opacities, ri.means, ri.scales = ptr(opacities), ptr(means), ptr(scales)
+    ri.glob_scale = float(glob_scale)
+    ri.quats, ri.uv0, ri.umap, ri.vmap = ptr(quats), ptr(uv0), ptr(umap), ptr(vmap)
+    ri.viewmat = ptr(viewmat)
+    ri.fx, ri.fy, ri.cx, ri.cy = float(fx), float(fy), float(cx), float(cy)
+    ri.settings = int(settings)
+    out = torch.empty((T, 5), dtype=torch.float32, device=means.device)
+    io = _lib.EditIO(ptr(updated_img), ptr(updated_alpha), ptr(depth_lower), ptr(depth_upper), T, ptr(out))
+    check(_lib.lib().gstex_texture_edit(ctypes.byref(ri), ctypes.byref(io), _lib.stream_of(means)), "texture_edit")
+    return out

@@ -177,6 +177,21 @@ typedef struct gstex_forward_outputs {
 /* Replaces _C.texture_forward (csrc/texture.cu:766-901). */
 int gstex_texture_forward(const gstex_raster_inputs* in, const gstex_forward_outputs* out, gstex_stream_t stream);
 
+typedef struct gstex_edit_io {
+    const float* updated_img;    /* [H,W,3] edited colours */
+    const float* updated_alpha;  /* [H,W] edit mask (0 where nothing is edited) */
+    const float* depth_lower;    /* [H,W] camera depths outside [lower, upper] are not edited */
+    const float* depth_upper;    /* [H,W] */
+    long long num_texels;        /* rows of updated_texture (sum of h*w over the charts) */
+    float* updated_texture;      /* [num_texels, 5]: r*a, g*a, b*a, a, total weight; zeroed, then accumulated */
+} gstex_edit_io;
+
+/* Replaces _C.texture_edit (csrc/texture_edit.cu:238-346): in->channels must
+ * be 5 (texture_info[2]; the reference writes five channels at that stride),
+ * in->colors / in->texture / in->background are not read, blur is settings
+ * bit 0. */
+int gstex_texture_edit(const gstex_raster_inputs* in, const gstex_edit_io* io, gstex_stream_t stream);
+
 typedef struct gstex_backward_io {
     /* saved forward state */
     const float* final_T;

@@ -277,6 +277,28 @@ def texture_backward(scene: Scene, cam: Camera, gids_sorted, tile_bins, block_wi
     return out
 
 
+def texture_edit(scene: Scene, cam: Camera, gids_sorted, tile_bins, block_width, settings, updated_img,
+                 updated_alpha, depth_lower, depth_upper, num_texels, prec="f32", nthreads=0):
+    """csrc/texture_edit.cu:11-236: the five-channel splat of an edited image
+    into the texels ([num_texels, 5]: r*a, g*a, b*a, a, total weight)."""
+    dt = _dt(prec)
+    R = _r(prec)
+    H, W = cam.height, cam.width
+    tb = tile_bounds(H, W, block_width)
+    a = [_a(x, dt) for x in (updated_img, updated_alpha, depth_lower, depth_upper, scene.opacity, scene.means,
+                             scene.scales, scene.quats, scene.uv0, scene.umap, scene.vmap, cam.viewmat, cam.c2w)]
+    dims = _a(scene.texture_dims, np.int32)
+    gs = _a(gids_sorted, np.int32)
+    bins = _a(tile_bins, np.int32)
+    out = np.zeros((int(num_texels), 5), dt)
+    _fn(prec, "texture_edit")(
+        _I(tb[0]), _I(tb[1]), _I(block_width), _I(W), _I(H), _p(dims), _p(a[0]), _p(a[1]), _p(a[2]), _p(a[3]),
+        _p(gs), _p(bins), _p(a[4]), _p(a[5]), _p(a[6]), R(scene.glob_scale), _p(a[7]), _p(a[8]), _p(a[9]),
+        _p(a[10]), _p(a[11]), _p(a[12]), R(cam.fx), R(cam.fy), R(cam.cx), R(cam.cy), _I(settings), _p(out),
+        _I(nthreads))
+    return out
+
+
 def render(scene: Scene, cam: Camera, depths=None, block_width=16, settings=1 << 8, background=None,
            prec="f32", nthreads=0, binning=None):
     """Projection + binning (float32, like the reference) + forward."""

@@ -764,6 +764,81 @@ int FN(texture_backward)(int tiles_x, int tiles_y, int bw, int img_w, int img_h,
 }
 
 /* ------------------------------------------------------------------------
+ * Texture editing: csrc/texture_edit.cu:11-236.  Front to back like the
+ * forward compositor (blur is settings bit 0 here), and for every pair that
+ * contributes with its camera depth inside [depth_lower, depth_upper] of the
+ * pixel, the values (r*a, g*a, b*a, a, 1) of the edited pixel are splatted
+ * with the bilinear weights of the hit's texture coordinate into the five
+ * channels of the chart's texels (out is [num_texels, 5], accumulated).
+ * ---------------------------------------------------------------------- */
+void FN(texture_edit)(int tiles_x, int tiles_y, int bw, int img_w, int img_h, const int32_t* texture_dims,
+                      const REAL* upd_img, const REAL* upd_alpha, const REAL* depth_lower, const REAL* depth_upper,
+                      const int32_t* gids, const int32_t* tile_bins, const REAL* opac, const REAL* means,
+                      const REAL* scales, REAL glob_scale, const REAL* quats, const REAL* uv0, const REAL* umap,
+                      const REAL* vmap, const REAL* viewmat, const REAL* c2w, REAL fx, REAL fy, REAL cx, REAL cy,
+                      int settings, REAL* out, int nthreads) {
+    const int use_blur = (settings & 1) != 0;
+    set_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int bi = 0; bi < img_h; bi++) {
+        for (int bj = 0; bj < img_w; bj++) {
+            const int tile = (bi / bw) * tiles_x + (bj / bw);
+            const long pix = (long)bi * img_w + bj;
+            REAL px = (REAL)bj + (REAL)0.5, py = (REAL)bi + (REAL)0.5;
+            v3 o, ray;
+            get_ray(c2w, fx, fy, cx, cy, px, py, &o, &ray);
+            REAL view_depth = viewmat[8] * ray.x + viewmat[9] * ray.y + viewmat[10] * ray.z;
+            const REAL a = upd_alpha[pix];
+            const REAL vals[5] = { upd_img[3 * pix] * a, upd_img[3 * pix + 1] * a, upd_img[3 * pix + 2] * a, a, 1 };
+            const REAL lo = depth_lower[pix], hi = depth_upper[pix];
+            int rs = tile_bins[2 * tile], re = tile_bins[2 * tile + 1];
+            REAL T = 1;
+            int done = 0;
+            for (int idx = rs; idx < re && !done; idx++) {
+                const int g = gids[idx];
+                v3 mean = { means[3 * g], means[3 * g + 1], means[3 * g + 2] };
+                REAL sx = scales[3 * g], sy = scales[3 * g + 1];
+                v3 a1, a2, a3;
+                quat_axes(quats + 4 * g, &a1, &a2, &a3);
+                REAL t = compute_tt(o, ray, mean, a3);
+                v3 pos = { o.x + t * ray.x, o.y + t * ray.y, o.z + t * ray.z };
+                v3 d = { pos.x - mean.x, pos.y - mean.y, pos.z - mean.z };
+                REAL l1 = dot3(d, a1), l2 = dot3(d, a2);
+                REAL is1 = (REAL)1 / (sx * glob_scale), is2 = (REAL)1 / (sy * glob_scale);
+                REAL sigma = (REAL)0.5f * (is1 * is1 * l1 * l1 + is2 * is2 * l2 * l2);
+                v3 pv = transform_4x3(viewmat, mean);
+                REAL xyx, xyy;
+                project_pix(fx, fy, pv, cx, cy, &xyx, &xyy);
+                REAL ddx = xyx - px, ddy = xyy - py;
+                REAL sigma_blur = (REAL)0.5f * K_BLUR_FSQ * (ddx * ddx + ddy * ddy);
+                REAL nbf = 1, bf = 0;
+                if (use_blur && sigma_blur < sigma) { bf = 1; nbf = 0; }
+                REAL alpha = R_FMIN(K_ALPHA_MAX, opac[g] * (nbf * R_EXP(-sigma) + bf * R_EXP(-sigma_blur)));
+                int skip = (t < K_T_NEAR || t > K_T_FAR || alpha < K_ALPHA_MIN);
+                REAL next_T = T * ((REAL)1 - alpha);
+                if (next_T <= K_T_DONE) done = 1;
+                if (skip || done) continue;
+                REAL t_view = t * view_depth;
+                if (t_view >= lo && t_view <= hi) {
+                    const int32_t* dm = texture_dims + 3 * g;
+                    v3 um = { umap[3 * g], umap[3 * g + 1], umap[3 * g + 2] };
+                    v3 vm = { vmap[3 * g], vmap[3 * g + 1], vmap[3 * g + 2] };
+                    REAL uu = uv0[2 * g] + dot3(um, d), vv = uv0[2 * g + 1] + dot3(vm, d);
+                    clamp_coord(&uu, &vv);
+                    for (int k = 0; k < 5; k++) {
+                        REAL w[4], wx, wy;
+                        long id[4];
+                        chart_weights(dm[0], dm[1], dm[2], 5, k, uu, vv, 1, w, id, &wx, &wy);
+                        for (int q = 0; q < 4; q++) ATOMIC_ADD(out + id[q], w[q] * vals[k]);
+                    }
+                }
+                T = next_T;
+            }
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------
  * Integer binning (float32 inputs in both builds; defined once, in the
  * float build).
  * ---------------------------------------------------------------------- */

@@ -285,6 +285,23 @@ def texture_sample_forward(texture_info, texture_dims, uvs, texture):
     return out
 
 
+def texture_edit(tile_bounds, block, img_size, texture_info, texture_total_size, texture_dims, updated_img,
+                 updated_alpha, depth_lower, depth_upper, gaussian_ids_sorted, tile_bins, opacity, means, scales,
+                 glob_scale, quats, uv0, umap, vmap, viewmat, c2w, fx, fy, cx, cy, settings, background):
+    """texture_edit.cu:238-346.  The kernel writes five channels at a stride
+    of texture_info[2], so anything but 5 would write out of range."""
+    assert texture_info[2] == 5, "reference texture_edit needs texture_info[2] == 5"
+    assert block[0] * block[1] <= 256 and background.numel() == 3
+    out = torch.zeros((int(texture_total_size), 5), device=means.device)
+    _launch("texture_edit", "texture_edit", tile_bounds, block,
+            [Dim3(*tile_bounds), Dim3(*img_size), Int3(*texture_info), _ptr(texture_dims), _ptr(updated_img),
+             _ptr(updated_alpha), _ptr(depth_lower), _ptr(depth_upper), _ptr(gaussian_ids_sorted), _ptr(tile_bins),
+             _ptr(opacity), _ptr(means), _ptr(scales), _f(glob_scale), _ptr(quats), _ptr(uv0), _ptr(umap),
+             _ptr(vmap), _ptr(viewmat), _ptr(c2w), Float4(fx, fy, cx, cy), _i(settings), _ptr(background),
+             _ptr(out)])
+    return out
+
+
 # texture_sample_backward (texture_sample.cu:38-70) is not wrapped: it reads
 # its upstream gradient from its own output array (v_texture indexed by the
 # query), which races with its own atomics and reads past that array when

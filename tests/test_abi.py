@@ -56,6 +56,10 @@ def test_invalid_arguments_rejected_without_gpu():
     assert L.gstex_texture_forward(ctypes.byref(ri), ctypes.byref(fo), None) == 3
     ri.channels, ri.block_width = 3, 17
     assert L.gstex_texture_forward(ctypes.byref(ri), ctypes.byref(fo), None) == 1
+    # texture_edit writes five channels: any other texture_info[2] is refused
+    eio = _lib.EditIO()
+    ri.block_width = 16
+    assert L.gstex_texture_edit(ctypes.byref(ri), ctypes.byref(eio), None) == 3
 
 
 def test_cpu_tensors_fail_loudly():
