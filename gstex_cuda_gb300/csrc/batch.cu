@@ -311,7 +311,6 @@ static int batch_scene(const gstex_batch_inputs* in, SceneArgs& a, BatchArgs& ba
     GSTEX_REQUIRE(in->channels >= 0);
     if (in->channels > kMaxChannels) return GSTEX_ERR_UNSUPPORTED;
     if (in->texture_dtype == 1 && in->channels != 3) return GSTEX_ERR_UNSUPPORTED;
-    if (in->settings & (1 << 16)) return GSTEX_ERR_UNSUPPORTED;
     GSTEX_REQUIRE(in->views && in->tile_view && in->tile_bins && in->colors && in->background && in->queue);
     if (in->num_points > 0)
         GSTEX_REQUIRE(in->gaussian_ids_sorted && in->texture_dims && in->opacities && in->means && in->scales &&
@@ -400,6 +399,7 @@ extern "C" int gstex_batch_backward(const gstex_batch_inputs* in, const gstex_ba
     BatchArgs ba;
     int rc = batch_scene(in, a, ba);
     if (rc) return rc;
+    if (in->settings & (1 << 16)) return GSTEX_ERR_UNSUPPORTED;  // alpha-visualisation mode: forward only
     GSTEX_REQUIRE(io && io->final_T && io->final_idx && io->depth_idx && io->reg_s && io->workspace);
     GSTEX_REQUIRE(io->v_colors && io->v_opacity && io->v_means && io->v_scales && io->v_quats && io->v_uv0 &&
                   io->v_umap && io->v_vmap);

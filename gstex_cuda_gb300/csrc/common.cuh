@@ -257,7 +257,7 @@ __device__ __forceinline__ bool make_record(RecHot& H, RecWarm& Wm, RecCold& Cd,
                                             const float3 mean, const float4 quat, const float2 scale,
                                             float glob_scale, float opac, float3 color, float2 uv0, float3 umap,
                                             float3 vmap, int3 dims, bool use_blur, bool allow_double = true,
-                                            RecEdge* E = nullptr) {
+                                            RecEdge* E = nullptr, bool cull = true) {
     const Axes A = quat_axes(quat);
     const float3 mc = V.xform(mean);
     const float3 a1c = V.rot(A.a1), a2c = V.rot(A.a2), nc = V.rot(A.a3);
@@ -318,6 +318,15 @@ __device__ __forceinline__ bool make_record(RecHot& H, RecWarm& Wm, RecCold& Cd,
         // a NaN opacity gives alpha = fminf(0.99, NaN) = 0.99 in the reference: never cull it
         x0 = y0 = -INFINITY;
         x1 = y1 = INFINITY;
+    }
+    if (!cull) {
+        // alpha-visualisation mode sets alpha without the opacity: no box
+        x0 = y0 = -INFINITY;
+        x1 = y1 = INFINITY;
+        if (E) {
+            E->A = E->B = make_float4(0.f, 0.f, 0.f, 0.f);
+            E->C = make_float4(1.f, 1.f, 1.f, 1.f);
+        }
     }
 
     if (flags) {

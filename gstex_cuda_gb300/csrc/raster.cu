@@ -28,7 +28,8 @@ __device__ __forceinline__ void stage(const Recs& R, int slot, const SceneArgs& 
     make_record(R.hot[slot], R.warm[slot], R.cold[slot], gid, V, a.means[gid], a.quats[gid],
                 make_float2(a.scales[3 * gid], a.scales[3 * gid + 1]), a.glob, a.opac[gid],
                 colors ? colors[gid] : make_float3(0.f, 0.f, 0.f), a.uv0[gid],
-                a.umap[gid], a.vmap[gid], a.dims[gid], use_blur, true, R.edge ? R.edge + slot : nullptr);
+                a.umap[gid], a.vmap[gid], a.dims[gid], use_blur, true, R.edge ? R.edge + slot : nullptr,
+                !(a.settings & (1 << 16)));
 }
 
 // Stages the record of Gaussian gid for one tile: a copy of the prebuilt
@@ -81,6 +82,23 @@ __device__ __forceinline__ Hit hit_pixel(const RecHot& Hr, const Recs& R, int k,
     if (H.direct)
         direct_hit(H, a.quats, a.means, a.scales, a.glob, a.uv0, a.umap, a.vmap, V, R.warm[k].tex.w, P, Hr.a.w);
     return H;
+}
+
+// Distance (in pixels) from the pixel to the nearest pixel of its 7x7
+// neighbourhood whose ray meets the splat outside sigma <= sth
+// (texture_helpers.cuh:390-417); 1000 when there is none.
+__device__ __noinline__ float local_outline(const RecHot& Hr, const Recs& R, int k, const SceneArgs& a, const View& V,
+                                            const TileJob& J, const PixelRay& P, float sth) {
+    float best = 1000.f;
+    const int pi = (int)(P.py - 0.5f), pj = (int)(P.px - 0.5f);
+    for (int dx = -3; dx <= 3; dx++) {
+        for (int dy = -3; dy <= 3; dy++) {
+            const PixelRay Q = make_pixel(V, pi + dy, pj + dx);
+            const Hit H = hit_pixel(Hr, R, k, a, V, Q);
+            if (0.5f * (H.l1s * H.l1s + H.l2s * H.l2s) > sth) best = fminf(best, sqrtf((float)(dx * dx + dy * dy)));
+        }
+    }
+    return best;
 }
 
 // All channels of the 4 bilinear corners (C == 3 fast path).
@@ -191,6 +209,16 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
     const bool use_ndc = a.settings & (1 << 10);
     const bool flip = a.settings & (1 << 15);
     const bool bilinear = !(a.settings & (1 << 2));
+    // alpha-visualisation mode (texture.cu:58-63, 201-241; settings bit 16,
+    // selected at launch as TEXMODE | 2): alpha 0.99 inside
+    // sigma <= alpha_bound^2 / 2, outlines within outline_bound pixels of its edge
+    constexpr bool alpha_vis = (TEXMODE & 2) != 0;
+    constexpr int TM = TEXMODE & 1;
+    const float alpha_bound = (float)((a.settings >> 17) & 31) / 8.f;
+    const float vis_sth = 0.5f * alpha_bound * alpha_bound;
+    const float outline_bound = (float)((a.settings >> 26) & 15) / 4.f;
+    const bool accept_opac = a.settings & (1 << 25);
+    const bool white_outline = a.settings & (1 << 24);
     const int C = CT >= 0 ? CT : a.C;
     constexpr int CA = CT > 0 ? CT : (CT == 0 ? 1 : kMaxChannels);
     const int2 lp = thread_pixel<PPT>(bw);
@@ -283,7 +311,13 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
                     sigma_blur = 0.5f * kBlurFsq * (dx * dx + dy * dy);
                     if (sigma_blur < sigma) { bf = 1.f; nbf = 0.f; }
                 }
-                const float alpha = fminf(kAlphaMax, Hr.d.z * (nbf * __expf(-sigma) + bf * __expf(-sigma_blur)));
+                float alpha = fminf(kAlphaMax, Hr.d.z * (nbf * __expf(-sigma) + bf * __expf(-sigma_blur)));
+                float pixel_dis = 1000.f;
+                if (alpha_vis) {
+                    alpha = sigma > vis_sth ? 0.f : kAlphaMax;
+                    if (accept_opac && Hr.d.z < 0.5f) alpha = 0.f;
+                    pixel_dis = local_outline(Hr, R, k, a, V, J, P[p], vis_sth);
+                }
                 const bool skip = H.t < kTNear || H.t > kTFar || alpha < kAlphaMin;
                 const float next_T = T[p] * (1.f - alpha);
                 if (next_T <= kTDone) { done[p] = true; continue; }
@@ -291,9 +325,12 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
                 const RecWarm& Wm = R.warm[k];
                 const float vis = alpha * T[p];
                 const float4 col = Wm.col;
-                out[p].x = out[p].x + col.x * vis;
-                out[p].y = out[p].y + col.y * vis;
-                out[p].z = out[p].z + col.z * vis;
+                // outside the outline: the colour; on it: white (bit 24) or nothing
+                const bool plain = !alpha_vis || pixel_dis > outline_bound;
+                const float wv = plain ? 0.f : (white_outline ? vis : 0.f);
+                out[p].x = out[p].x + (plain ? col.x * vis : wv);
+                out[p].y = out[p].y + (plain ? col.y * vis : wv);
+                out[p].z = out[p].z + (plain ? col.z * vis : wv);
                 float3 hn = f3(Wm.nrm);
                 if (flip && H.nd > 0.f) hn = make_float3(-hn.x, -hn.y, -hn.z);
                 nrm[p].x += vis * hn.x; nrm[p].y += vis * hn.y; nrm[p].z += vis * hn.z;
@@ -303,16 +340,18 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
                     const Bilerp B = bilerp(tx.x, tx.y, tx.z, clamp01(uv.x), clamp01(uv.y), bilinear);
                     if (CT == 3) {
                         float c[4][3];
-                        fetch3<TEXMODE>(a.tex, B, c);
+                        fetch3<TM>(a.tex, B, c);
 #pragma unroll
                         for (int ch = 0; ch < 3; ch++)
-                            otex[p][ch] += vis * (B.w00 * c[0][ch] + B.w01 * c[1][ch] + B.w10 * c[2][ch] + B.w11 * c[3][ch]);
+                            otex[p][ch] += plain ? vis * (B.w00 * c[0][ch] + B.w01 * c[1][ch] + B.w10 * c[2][ch] +
+                                                          B.w11 * c[3][ch])
+                                                 : wv;
                     } else if (CT != 0) {
                         const float* t = (const float*)a.tex;
                         for (int ch = 0; ch < C; ch++) {
                             const float v = B.w00 * __ldg(t + (size_t)B.i00 * C + ch) + B.w01 * __ldg(t + (size_t)B.i01 * C + ch) +
                                             B.w10 * __ldg(t + (size_t)B.i10 * C + ch) + B.w11 * __ldg(t + (size_t)B.i11 * C + ch);
-                            otex[p][ch] += vis * v;
+                            otex[p][ch] += plain ? vis * v : wv;
                         }
                     }
                 }
@@ -896,7 +935,8 @@ __global__ void records_kernel(SceneArgs a, BatchArgs ba, const int32_t* __restr
     RecAll r;
     const bool defer = make_record(r.h, r.w, r.c, i, V, a.means[i], a.quats[i],
                                    make_float2(a.scales[3 * i], a.scales[3 * i + 1]), a.glob, a.opac[i], ba.colors[j],
-                                   a.uv0[i], a.umap[i], a.vmap[i], a.dims[i], a.settings & (1 << 9), false, &r.e);
+                                   a.uv0[i], a.umap[i], a.vmap[i], a.dims[i], a.settings & (1 << 9), false, &r.e,
+                                   !(a.settings & (1 << 16)));
     recs[j] = r;
     if (defer) fix[atomicAdd(fix_count, 1)] = (uint32_t)j;
 }
@@ -982,7 +1022,6 @@ int fill_scene(const gstex_raster_inputs* in, SceneArgs& a) {
     if (in->channels > kMaxChannels) return GSTEX_ERR_UNSUPPORTED;
     if (in->texture_dtype == 1 && in->channels != 3) return GSTEX_ERR_UNSUPPORTED;
     GSTEX_REQUIRE(in->texture_dtype == 0 || in->texture_dtype == 1);
-    if (in->settings & (1 << 16)) return GSTEX_ERR_UNSUPPORTED;  // alpha-visualisation mode
     GSTEX_REQUIRE(in->tile_bins && in->viewmat && in->background);
     if (in->num_points > 0)
         GSTEX_REQUIRE(in->texture_dims && in->colors && in->opacities && in->means && in->scales && in->quats &&
@@ -1022,6 +1061,16 @@ static typename Sel<0, 0, 1>::type pick(int C, int texmode, int ppt) {
     if (C == 3) return texmode == 1 ? Sel<1, 3, 1>::get() : Sel<0, 3, 1>::get();
     return Sel<0, -1, 1>::get();
 }
+// Forward kernel: the alpha-visualisation variants (settings bit 16) come
+// with 1 pixel per thread and the generic fp32 or the bf16 texel path.
+template <template <int, int, int> class Sel>
+static typename Sel<0, 0, 1>::type pick_fwd(int C, int texmode, int& ppt, int settings) {
+    if (settings & (1 << 16)) {
+        ppt = 1;
+        return texmode == 1 ? Sel<3, 3, 1>::get() : Sel<2, -1, 1>::get();
+    }
+    return pick<Sel>(C, texmode, ppt);
+}
 template <int M, int C, int P> struct FwdView { typedef void (*type)(SceneArgs, ViewArgs, FwdOut); static type get() { return fwd_view_kernel<M, C, P>; } };
 template <int M, int C, int P> struct BwdView { typedef void (*type)(SceneArgs, ViewArgs, BwdArgs); static type get() { return bwd_view_kernel<M, C, P>; } };
 template <int M, int C, int P> struct FwdBatch { typedef void (*type)(SceneArgs, BatchArgs, FwdOut); static type get() { return fwd_batch_kernel<M, C, P>; } };
@@ -1051,7 +1100,7 @@ int launch_finalize(const SceneArgs& a, const float* moments, float* v_opac, flo
 int launch_fwd_batch(const SceneArgs& a, const BatchArgs& ba, const FwdOut& o, int bw, int texmode, int ppt, int grid,
                      cudaStream_t stream) {
     ppt = ppt_of(bw, ppt);
-    auto k = pick<FwdBatch>(a.C, texmode, ppt);
+    auto k = pick_fwd<FwdBatch>(a.C, texmode, ppt, a.settings);
     int rc = set_smem(k, fwd_smem(bw, ppt), "batch forward");
     if (rc) return rc;
     k<<<grid, block_of(bw, ppt), fwd_smem(bw, ppt), stream>>>(a, ba, o);
@@ -1113,8 +1162,8 @@ extern "C" int gstex_texture_forward(const gstex_raster_inputs* in, const gstex_
     va.vcolors = nullptr;
     cudaStream_t stream = (cudaStream_t)s;
     const dim3 grid(va.tiles_x, ceil_div(va.H, bw));
-    const int ppt = ppt_of(bw, in->pixels_per_thread);
-    auto k = pick<FwdView>(a.C, in->texture_dtype, ppt);
+    int ppt = ppt_of(bw, in->pixels_per_thread);
+    auto k = pick_fwd<FwdView>(a.C, in->texture_dtype, ppt, a.settings);
     if ((rc = set_smem(k, fwd_smem(bw, ppt), "texture_forward"))) return rc;
     k<<<grid, block_of(bw, ppt), fwd_smem(bw, ppt), stream>>>(a, va, o);
     return check_launch("texture_forward");
@@ -1177,6 +1226,8 @@ extern "C" int gstex_texture_backward(const gstex_raster_inputs* in, const gstex
     SceneArgs a;
     int rc = fill_scene(in, a);
     if (rc) return rc;
+    // alpha-visualisation mode is a forward-only view: its alpha has no adjoint
+    if (in->settings & (1 << 16)) return GSTEX_ERR_UNSUPPORTED;
     GSTEX_REQUIRE(io && io->final_T && io->final_idx && io->depth_idx && io->reg_s && io->v_img && io->v_depth &&
                   io->v_reg && io->v_alpha && io->v_normal);
     GSTEX_REQUIRE(io->v_colors && io->v_opacity && io->v_means && io->v_scales && io->v_quats && io->v_uv0 &&

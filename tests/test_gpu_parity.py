@@ -260,3 +260,29 @@ def test_untextured_800_full_size_vs_oracle():
     case = Case(spec)
     bg = np.zeros(3)
     b, out, bgt, ref = _compare_forward(case, 16, 1 << 8, bg, 1e-4, frac=1e-3)
+
+
+VIS = (1 << 16) | (10 << 17) | (4 << 26)  # alpha-visualisation, alpha_bound 1.25, outline 1 px
+
+
+@pytest.mark.parametrize("extra", [0, 1 << 24, (1 << 24) | (1 << 25), 1 << 8])
+def test_alpha_visualisation_forward_vs_oracle(extra):
+    """Settings bits 16-29 (texture.cu:58-63, 201-241): alpha 0.99 inside
+    sigma <= alpha_bound^2/2, outline pixels black or white (bit 24),
+    low-opacity splats hidden (bit 25).  Forward only: the backward refuses
+    the mode."""
+    import gstex_cuda_gb300 as G
+    case = Case(small_scene(n=150, width=64, height=48, seed=8))
+    bw = 16
+    settings = VIS | extra
+    bg = np.array([0.2, 0.3, 0.4])
+    b = case.binning_cuda(bw)
+    ref = oracle.texture_forward(case.scene_np, case.cam_np, b["gaussian_ids_sorted"].cpu().numpy(),
+                                 b["tile_bins"].cpu().numpy(), bw, settings, bg, prec="f64")
+    out, bgt = case.forward_cuda(b["gaussian_ids_sorted"], b["tile_bins"], bw, settings, bg)
+    # the outline distance compares sigma at neighbouring pixels with a threshold
+    for k in ("img", "texture", "normal", "final_T"):
+        _close(np_(out[k]), ref[k], 1e-4, 2e-2, k, cap=np.inf)
+    with pytest.raises(Exception):
+        ups = upstream(case.cam.height, case.cam.width, case.spec.texture.shape[1])
+        case.backward_cuda(out, b["gaussian_ids_sorted"], b["tile_bins"], ups, bw, settings, bgt)

@@ -291,3 +291,22 @@ def test_full_size_vs_reference_kernels(which):
     assert torch.equal(keys, r["isect_sorted"])
     assert torch.equal(G.cuda.get_tile_bin_edges(r["n"], keys, r["tile_bounds"]), r["bins"])
     _compare(fr, fg, gr, gg, 1e-4, 3e-3, 2e-3, rows_frac=1e-3, one_texel=which.startswith("untextured"))
+
+
+def test_alpha_visualisation_forward_vs_reference_kernels():
+    """Settings bits 16, 17-21, 24-29 against the reference's forward kernel."""
+    case = Case(_scene("small"))
+    settings = (1 << 16) | (10 << 17) | (4 << 26) | (1 << 24)
+    R, G = _R(), _G()
+    r = _ref_binning(case, 16)
+    t, cam, sp = case.t, case.cam, case.spec
+    info = (sp.num_points, 1, sp.texture.shape[1])
+    bgt = torch.tensor([0.2, 0.3, 0.4], dtype=torch.float32, device=DEV)
+    common = (info, t["dims"], r["gids_sorted"], r["bins"], t["colors"], t["opacity"], t["means"], t["scales"],
+              sp.glob_scale, t["quats"], t["uv0"], t["umap"], t["vmap"], t["texture"], t["viewmat"], t["c2w"],
+              *case.intr, settings, bgt)
+    tb = r["tile_bounds"]
+    fr = dict(zip(OUT_NAMES, R.texture_forward(tb, (16, 16, 1), (cam.width, cam.height, 1), *common)))
+    fg = dict(zip(OUT_NAMES, G.cuda.texture_forward(tb, (16, 16, 1), (cam.width, cam.height, 1), *common)))
+    for k in ("img", "texture", "normal", "final_T"):
+        close_frac(np_(fg[k]), np_(fr[k]), 1e-4, 2e-2, k, cap=np.inf)
