@@ -67,6 +67,8 @@ _SIGS = {
     "gstex_get_tile_bin_edges": (_I, [_I, _P, _I, _P, _P]),
     "gstex_texture_forward": (_I, [ctypes.POINTER(RasterInputs), ctypes.POINTER(ForwardOutputs), _P]),
     "gstex_texture_edit": (_I, [ctypes.POINTER(RasterInputs), ctypes.POINTER(EditIO), _P]),
+    "gstex_preprocess_forward": (_I, [_I, _I] + [_P] * 10 + [_P]),
+    "gstex_preprocess_backward": (_I, [_I, _I] + [_P] * 14 + [_P]),
     "gstex_backward_workspace_bytes": (ctypes.c_size_t, [_I]),
     "gstex_texture_backward": (_I, [ctypes.POINTER(RasterInputs), ctypes.POINTER(BackwardIO), _P]),
     "gstex_texture_sample_forward": (_I, [_I, _I, _P, _P, _P, _P, _P]),

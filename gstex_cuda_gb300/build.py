@@ -32,6 +32,7 @@ PER_FILE = {
     "sample.cu": ["-fmad=false"],
     "status.cu": [],
     "sort_static.cu": [],
+    "preprocess.cu": [],
 }
 
 

@@ -357,6 +357,32 @@ int gstex_batch_image_loss(long long total_pixels, int num_views, const long lon
                            float w_normal, float* v_img, float* v_tex, float* v_normal, float* v_reg, float* loss,
                            gstex_stream_t stream);
 
+/* ------------------------------------------------------------------------
+ * Parameter activation of a GStex training step on the device: the demo
+ * trainer's per-step preprocessing (example.py:126-143 and the opacity
+ * sigmoid of example.py:155-171) as one kernel each way.  No native
+ * counterpart in the reference (there it is a dozen PyTorch ops).
+ *   scales[:, :2] = exp(raw_scales[:, :2]); scales[:, 2] = 1e-5 * mean(scales[:, :2])
+ *   quats = raw_quats / |raw_quats|
+ *   uv0 = mapping[..., 0:2]
+ *   umap = exp(mapping[..., 2]) * ( ax1 cos(theta) + ax2 sin(theta))
+ *   vmap = exp(mapping[..., 2]) * (-ax1 sin(theta) + ax2 cos(theta)), theta = mapping[..., 3]
+ *   opacity = sigmoid(raw_opacity)            (when raw_opacity is not null)
+ * Shapes: raw_scales/scales [N,3], raw_quats/quats [N,4], mapping [N,P,4],
+ * uv0 [N,P,2], umap/vmap [N,P,3], raw_opacity/opacity [N]. */
+int gstex_preprocess_forward(int N, int P, const float* raw_scales, const float* raw_quats, const float* mapping,
+                             const float* raw_opacity, float* scales, float* quats, float* uv0, float* umap,
+                             float* vmap, float* opacity, gstex_stream_t stream);
+
+/* The adjoint of gstex_preprocess_forward (null upstream gradients are zero;
+ * the third scale is detached, as in the trainer): gradients with respect to
+ * raw_scales, raw_quats, mapping and raw_opacity. */
+int gstex_preprocess_backward(int N, int P, const float* raw_scales, const float* raw_quats, const float* mapping,
+                              const float* raw_opacity, const float* v_scales, const float* v_quats,
+                              const float* v_uv0, const float* v_umap, const float* v_vmap, const float* v_opacity,
+                              float* v_raw_scales, float* v_raw_quats, float* v_mapping, float* v_raw_opacity,
+                              gstex_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -280,9 +280,10 @@ def test_alpha_visualisation_forward_vs_oracle(extra):
     ref = oracle.texture_forward(case.scene_np, case.cam_np, b["gaussian_ids_sorted"].cpu().numpy(),
                                  b["tile_bins"].cpu().numpy(), bw, settings, bg, prec="f64")
     out, bgt = case.forward_cuda(b["gaussian_ids_sorted"], b["tile_bins"], bw, settings, bg)
-    # the outline distance compares sigma at neighbouring pixels with a threshold
+    # the outline distance compares sigma at neighbouring pixels with a threshold,
+    # so a rounding difference may flip a pixel
     for k in ("img", "texture", "normal", "final_T"):
-        _close(np_(out[k]), ref[k], 1e-4, 2e-2, k, cap=np.inf)
+        _close(np_(out[k]), ref[k], 1e-4, 1e-3, k)
     with pytest.raises(Exception):
         ups = upstream(case.cam.height, case.cam.width, case.spec.texture.shape[1])
         case.backward_cuda(out, b["gaussian_ids_sorted"], b["tile_bins"], ups, bw, settings, bgt)

@@ -309,4 +309,4 @@ def test_alpha_visualisation_forward_vs_reference_kernels():
     fr = dict(zip(OUT_NAMES, R.texture_forward(tb, (16, 16, 1), (cam.width, cam.height, 1), *common)))
     fg = dict(zip(OUT_NAMES, G.cuda.texture_forward(tb, (16, 16, 1), (cam.width, cam.height, 1), *common)))
     for k in ("img", "texture", "normal", "final_T"):
-        close_frac(np_(fg[k]), np_(fr[k]), 1e-4, 2e-2, k, cap=np.inf)
+        close_frac(np_(fg[k]), np_(fr[k]), 1e-4, 1e-2, k)
