@@ -266,7 +266,7 @@ class BatchRenderer:
             N = self.N
             tex_cols = 4 if self.texmode == 1 else self.C
             nb = s.sh_coeffs.shape[1]
-            self.grads = dict(vcolors=torch.empty((self.V, N, 3), **f32), opacity=torch.empty(s.opacity.shape, **f32),
+            self.grads = dict(vcolors=torch.empty((self.V, N, 4), **f32), opacity=torch.empty(s.opacity.shape, **f32),
                               means=torch.empty((N, 3), **f32), scales=torch.empty((N, 3), **f32),
                               quats=torch.empty((N, 4), **f32), uv0=torch.empty(s.uv0.shape, **f32),
                               umap=torch.empty(s.umap.shape, **f32), vmap=torch.empty(s.vmap.shape, **f32),

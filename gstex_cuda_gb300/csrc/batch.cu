@@ -166,7 +166,7 @@ __global__ void batch_loss_kernel(long long total, int V, const long long* __res
 // SH adjoint summed over views: v_coeffs[i,b,c] = sum_v Y_b(dir_v) v_color[v,i,c].
 __global__ void batch_sh_backward_kernel(int N, int V, const BatchView* __restrict__ views,
                                          const float3* __restrict__ means, int sh_degree,
-                                         const float3* __restrict__ vcol, float* __restrict__ v_coeffs) {
+                                         const float4* __restrict__ vcol, float* __restrict__ v_coeffs) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     const int B = sh_bases(sh_degree);
@@ -174,7 +174,7 @@ __global__ void batch_sh_backward_kernel(int N, int V, const BatchView* __restri
     for (int b = 0; b < 25; b++) acc[b][0] = acc[b][1] = acc[b][2] = 0.f;
     const float3 p = means[i];
     for (int v = 0; v < V; v++) {
-        const float3 g = vcol[(size_t)v * N + i];
+        const float4 g = vcol[(size_t)v * N + i];
         if (g.x == 0.f && g.y == 0.f && g.z == 0.f) continue;
         const BatchView& bv = views[v];
         float Y[25];
@@ -410,7 +410,7 @@ extern "C" int gstex_batch_backward(const gstex_batch_inputs* in, const gstex_ba
     cudaError_t e = cudaMemsetAsync(in->queue, 0, sizeof(int), stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(io->workspace, 0, gstex_batch_backward_workspace_bytes(a.N), stream);
     if (e == cudaSuccess)
-        e = cudaMemsetAsync(io->v_colors, 0, (size_t)in->num_views * a.N * 3 * sizeof(float), stream);
+        e = cudaMemsetAsync(io->v_colors, 0, (size_t)in->num_views * a.N * 4 * sizeof(float), stream);
     if (e != cudaSuccess) { set_cuda_error(e, "batch_backward"); return GSTEX_ERR_CUDA; }
     ba.vcolors = io->v_colors;
     BwdArgs g{ io->final_T, io->final_idx, io->depth_idx, (const float3*)io->reg_s, (const float3*)io->v_img,
@@ -429,7 +429,7 @@ extern "C" int gstex_batch_sh_backward(int N, int V, const void* views_dev, cons
     if (N == 0) return GSTEX_OK;
     GSTEX_REQUIRE(means && v_colors && v_coeffs);
     batch_sh_backward_kernel<<<ceil_div(N, 128), 128, 0, (cudaStream_t)s>>>(
-        N, V, (const BatchView*)views_dev, (const float3*)means, sh_degree, (const float3*)v_colors, v_coeffs);
+        N, V, (const BatchView*)views_dev, (const float3*)means, sh_degree, (const float4*)v_colors, v_coeffs);
     return check_launch("batch_sh_backward");
 }
 

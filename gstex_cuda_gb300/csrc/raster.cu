@@ -575,7 +575,7 @@ __device__ __forceinline__ void bwd_pair(const SceneArgs& a, const BwdArgs& g, c
 
 template <int TEXMODE, int CT, int PPT>
 __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, const BwdArgs& g, const Recs& R,
-                                         float* smom, uint8_t* lists) {
+                                         float* smom, uint8_t* lists, uint8_t* touched) {
     const int nthr = blockDim.x * blockDim.y;
     const int tr = threadIdx.y * blockDim.x + threadIdx.x;
     const int bw = blockDim.x;
@@ -631,6 +631,7 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
         const int idx = bend - tr;
         if (idx >= range.x) stage_job(R, tr, a, J, a.gids[idx], use_blur);
         for (int q = tr; q < nthr * kMoments; q += nthr) smom[q] = 0.f;
+        touched[tr] = 0;
         __syncthreads();
         // splats outside their alpha >= 1/255 box contribute nothing here:
         // walk the warp's candidates, back to front
@@ -685,6 +686,7 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
                     bwd_pair<TEXMODE, CT, CA>(a, g, R, k, gidx, Hr, H[p], alpha[p], e[p], eb[p], nbf[p], bf[p], S[p],
                                               C, use_ndc, prop_uv, bilinear, m);
             float* dst = smom + k * kMoments;
+            if (lane == 0) touched[k] = 1;
             // few valid lanes: each adds its own moments; else one transpose reduction
             if (full_warp && __popc(vmask) > GSTEX_SPARSE_LANES) {
                 const float s = warp_transpose_reduce(m, lane);
@@ -695,17 +697,18 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
             }
         }
         __syncthreads();
-        if (idx >= range.x) {
+        if (idx >= range.x && touched[tr]) {
             const float* sm = smom + tr * kMoments;
-            bool any = false;
-#pragma unroll
-            for (int q = 0; q < kMoments; q++) any |= sm[q] != 0.f;
-            if (any) {
+            {
                 const int gid = R.warm[tr].tex.w;
-                float* vc = J.vcolors + 3 * (size_t)gid;
-                atomicAdd(vc + 0, sm[0]);
-                atomicAdd(vc + 1, sm[1]);
-                atomicAdd(vc + 2, sm[2]);
+                if (J.vc_stride == 4) {
+                    atomicAdd(reinterpret_cast<float4*>(J.vcolors) + gid, make_float4(sm[0], sm[1], sm[2], 0.f));
+                } else {
+                    float* vc = J.vcolors + 3 * (size_t)gid;
+                    atomicAdd(vc + 0, sm[0]);
+                    atomicAdd(vc + 1, sm[1]);
+                    atomicAdd(vc + 2, sm[2]);
+                }
                 float4* dst = reinterpret_cast<float4*>(g.moments + (size_t)gid * kMomStride);
                 // blur moments -> world-space mean gradient (helpers.cuh:155-164, 114-121)
                 const float3 p = f3(R.cold[tr].mu);
@@ -818,6 +821,7 @@ __global__ void __launch_bounds__(256, 4) edit_view_kernel(SceneArgs a, ViewArgs
     J.pix_base = 0;
     J.colors = nullptr;
     J.vcolors = nullptr;
+    J.vc_stride = 3;
     J.recs = nullptr;
     edit_tile(a, J, E, Recs::carve(smem, blockDim.x * blockDim.y, false));
 }
@@ -852,6 +856,7 @@ __global__ void FWD_BOUNDS(PPT) fwd_view_kernel(SceneArgs a, ViewArgs va, FwdOut
     J.pix_base = 0;
     J.colors = va.colors;
     J.vcolors = nullptr;
+    J.vc_stride = 3;
     J.recs = nullptr;
     const int nthr = blockDim.x * blockDim.y;
     fwd_tile<TEXMODE, CT, PPT>(a, J, o, Recs::carve(smem, nthr, false), smem + (size_t)kRecBytes * nthr);
@@ -869,10 +874,12 @@ __global__ void BWD_BOUNDS(PPT) bwd_view_kernel(SceneArgs a, ViewArgs va, BwdArg
     J.pix_base = 0;
     J.colors = va.colors;
     J.vcolors = va.vcolors;
+    J.vc_stride = 3;
     J.recs = nullptr;
+    uint8_t* lists = smem + (size_t)(kRecBytes + kEdgeBytes + kMoments * sizeof(float)) * nthr;
     bwd_tile<TEXMODE, CT, PPT>(a, J, g, Recs::carve(smem, nthr, true),
-                               reinterpret_cast<float*>(smem + (size_t)(kRecBytes + kEdgeBytes) * nthr),
-                               smem + (size_t)(kRecBytes + kEdgeBytes + kMoments * sizeof(float)) * nthr);
+                               reinterpret_cast<float*>(smem + (size_t)(kRecBytes + kEdgeBytes) * nthr), lists,
+                               lists + (size_t)ceil_div(nthr, 32) * nthr);
 }
 
 __device__ __forceinline__ bool next_job(const BatchArgs& ba, int* s_tile, TileJob& J) {
@@ -892,7 +899,8 @@ __device__ __forceinline__ bool next_job(const BatchArgs& ba, int* s_tile, TileJ
     J.range = ba.bins[t];
     J.pix_base = bv.pix_offset;
     J.colors = ba.colors + (size_t)v * ba.num_points;
-    J.vcolors = ba.vcolors ? ba.vcolors + (size_t)v * ba.num_points * 3 : nullptr;
+    J.vcolors = ba.vcolors ? ba.vcolors + (size_t)v * ba.num_points * 4 : nullptr;
+    J.vc_stride = 4;
     J.recs = ba.recs ? ba.recs + (size_t)v * ba.num_points : nullptr;
     return true;
 }
@@ -917,7 +925,8 @@ __global__ void BWD_BOUNDS(PPT) bwd_batch_kernel(SceneArgs a, BatchArgs ba, BwdA
     const Recs R = Recs::carve(smem, nthr, true);
     float* smom = reinterpret_cast<float*>(smem + (size_t)(kRecBytes + kEdgeBytes) * nthr);
     uint8_t* lists = smem + (size_t)(kRecBytes + kEdgeBytes + kMoments * sizeof(float)) * nthr;
-    while (next_job(ba, &s_tile, J)) bwd_tile<TEXMODE, CT, PPT>(a, J, g, R, smom, lists);
+    uint8_t* touched = lists + (size_t)ceil_div(nthr, 32) * nthr;
+    while (next_job(ba, &s_tile, J)) bwd_tile<TEXMODE, CT, PPT>(a, J, g, R, smom, lists, touched);
 }
 
 // Records of every (view, Gaussian) pair with tiles in the view, and of
@@ -1085,7 +1094,9 @@ static size_t list_bytes(int bw, int ppt) {
 }
 size_t fwd_smem(int bw, int ppt) { return (size_t)kRecBytes * threads_of(bw, ppt) + list_bytes(bw, ppt); }
 size_t bwd_smem(int bw, int ppt) {
-    return ((size_t)kRecBytes + kEdgeBytes + kMoments * sizeof(float)) * threads_of(bw, ppt) + list_bytes(bw, ppt);
+    // ... then one "touched" flag per slot
+    return ((size_t)kRecBytes + kEdgeBytes + kMoments * sizeof(float) + 1) * threads_of(bw, ppt) +
+           list_bytes(bw, ppt);
 }
 
 int launch_finalize(const SceneArgs& a, const float* moments, float* v_opac, float* v_means, float* v_scales,

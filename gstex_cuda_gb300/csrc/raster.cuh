@@ -53,7 +53,7 @@ struct BatchArgs {
     const int32_t* order;      // optional queue order of global tiles
     const int2* bins;          // [total_tiles]
     const float3* colors;      // [V, N, 3]
-    float* vcolors;            // [V, N, 3]
+    float* vcolors;            // [V, N, 4] (rgb + pad: one vector atomic per flush)
     int* queue;                // tile counter, zero before each launch
     const RecAll* recs;        // optional [V, N] prebuilt records; null: built per tile
 };
@@ -65,7 +65,8 @@ struct TileJob {
     int2 range;
     size_t pix_base;
     const float3* colors;
-    float* vcolors;
+    float* vcolors;       // colour gradients: [N, 3] (per-view launch) or [N, 4] rows (batched)
+    int vc_stride;        // 3 or 4 floats per Gaussian in vcolors
     const RecAll* recs;   // the view's prebuilt records, or null
 };
 

@@ -337,15 +337,17 @@ int gstex_batch_records(const gstex_batch_inputs* in, const int32_t* counts, voi
  * (pixel p of view v at pix_offsets[v] + p).  Batched texture_forward. */
 int gstex_batch_forward(const gstex_batch_inputs* in, const gstex_forward_outputs* out, gstex_stream_t stream);
 
-/* Backward of all views.  io->v_colors is [V, N, 3] (per-view colour
- * gradients, for the SH adjoint); the other Gaussian gradients are summed
+/* Backward of all views.  io->v_colors is [V, N, 4] (per-view colour
+ * gradients rgb + one unused float per row, for the SH adjoint; 16-byte
+ * aligned); the other Gaussian gradients are summed
  * over views; null upstream-gradient pointers mean zero.  Workspace:
  * gstex_batch_backward_workspace_bytes(N).  Batched texture_backward. */
 size_t gstex_batch_backward_workspace_bytes(int num_points);
 int gstex_batch_backward(const gstex_batch_inputs* in, const gstex_backward_io* io, gstex_stream_t stream);
 
-/* SH coefficient gradients [N, bases(degree), 3] summed over views.
- * Batched compute_sh_backward. */
+/* SH coefficient gradients [N, bases(degree), 3] summed over views, from
+ * the [V, N, 4] colour gradients of gstex_batch_backward.  Batched
+ * compute_sh_backward. */
 int gstex_batch_sh_backward(int num_points, int num_views, const void* views_dev, const float* means,
                             int sh_degree, const float* v_colors, float* v_coeffs, gstex_stream_t stream);
 

@@ -68,7 +68,7 @@ def test_batch_forward_backward_vs_oracle(setup):
     spec, cams, r, scene, loss = setup
     gs = r.gids_sorted.cpu().numpy()
     bins = r.bins.cpu().numpy()
-    vcol = r.grads["vcolors"].cpu().numpy()
+    vcol = r.grads["vcolors"][..., :3].cpu().numpy()
     ups = {k: v.cpu().numpy() for k, v in r.ups.items()}
     tot = None
     vcoef = 0
