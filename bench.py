@@ -31,8 +31,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
 METRIC = "fwd+bwd frames/s, 1080p 500k splats/16M texels: batched bf16 vs plain fp32, same tol"
-WORKLOAD = ("32 cameras (512^2/800^2/1280x720/1920x1080, r=8 sphere), 500k Gaussians, 16M bf16 texels, "
-            "SH deg 3 (bf16), fwd + image losses + bwd + SH adjoint")
+WORKLOADS = {
+    "batched": ("32 cameras (512^2/800^2/1280x720/1920x1080, r=8 sphere), 500k Gaussians, 16M bf16 texels, "
+                "SH deg 3 (bf16), fwd + image losses + bwd + SH adjoint"),
+    "stress": ("8 cameras 1920x1080 (r=8 sphere), 1M Gaussians in 64 clusters (sigma 0.3), 32M bf16 texels, "
+               "SH deg 3 (bf16), fwd + image losses + bwd + SH adjoint"),
+}
 
 
 def log(msg):
@@ -45,9 +49,11 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--views", type=int, default=32)
-    p.add_argument("--points", type=int, default=500_000)
-    p.add_argument("--texels", type=int, default=16_000_000)
+    p.add_argument("--workload", default="batched", choices=sorted(WORKLOADS),
+                   help="batched: the headline 32-view scene; stress: 8 x 1080p, 1M clustered Gaussians")
+    p.add_argument("--views", type=int, default=None, help="cameras (default 32 batched, 8 stress)")
+    p.add_argument("--points", type=int, default=None, help="Gaussians (default 500k batched, 1M stress)")
+    p.add_argument("--texels", type=int, default=None, help="texels (default 16M batched, 32M stress)")
     p.add_argument("--no-plain", action="store_true", help="skip the plain per-view fp32 comparison")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     p.add_argument("--no-e2e", action="store_true")
@@ -56,9 +62,13 @@ def parse():
 
 
 # ---------------------------------------------------------------------------
-def build_workload(args, seed=3):
+def build_workload(args, seed=None):
     from gstex_cuda_gb300 import synthetic
-    return synthetic.batched(seed=seed, n=args.points, texels=args.texels, views=args.views)
+    if args.workload == "stress":
+        return synthetic.stress(seed=4 if seed is None else seed, n=args.points or 1_000_000,
+                                texels=args.texels or 32_000_000, views=args.views or 8)
+    return synthetic.batched(seed=3 if seed is None else seed, n=args.points or 500_000,
+                             texels=args.texels or 16_000_000, views=args.views or 32)
 
 
 def device_scene(spec, dev, bf16=True):
@@ -166,8 +176,9 @@ def algorithmic_bytes(I, tiles, T, P, C, N, tex_bytes_per_texel, grad_texel_byte
 
 
 # ---------------------------------------------------------------------------
-def cpu_sample(spec, seconds, prec="f32", loss_weights=None):
-    """Oracle fwd + bwd of whole views (round robin) until `seconds` elapse."""
+def cpu_sample(spec, seconds, prec="f32", loss_weights=None, start=0):
+    """Oracle fwd + bwd of whole views (round robin from camera `start`) until
+    `seconds` elapse."""
     import numpy as np
     import oracle
     from gstex_cuda_gb300.batch import LOSS_WEIGHTS
@@ -178,7 +189,7 @@ def cpu_sample(spec, seconds, prec="f32", loss_weights=None):
     done, t0 = 0, time.perf_counter()
     views = []
     while True:
-        cam = spec.cameras[done % len(spec.cameras)]
+        cam = spec.cameras[(start + done) % len(spec.cameras)]
         dirs = (spec.means - cam.position[None]).numpy()
         col = oracle.sh_forward(spec.sh_degree, spec.sh_degree, dirs, spec.sh_coeffs.numpy(), prec=prec)
         sc = oracle.Scene(means=spec.means.numpy(), scales=spec.scales.numpy(), quats=spec.quats.numpy(),
@@ -221,17 +232,19 @@ def run_reference(args):
         cpu_sample(spec, 0.0)
     t0 = time.perf_counter()
     n_views = 0
-    for _ in range(steps):
-        fps, cores, n, el, views = cpu_sample(spec, 0.0)
+    for i in range(steps):
+        fps, cores, n, el, views = cpu_sample(spec, 0.0, start=i)
         n_views += n
     el = time.perf_counter() - t0
     value = n_views / el
     line = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": args.gpus, "steps": steps,
             "warmup": warm, "ms_per_step": 1000 * el / steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
-            "config": {"workload": WORKLOAD, "sample": f"{steps} views fwd+bwd (round robin over the 32 cameras)"},
+            "config": {"workload": WORKLOADS[args.workload],
+                       "sample": f"{steps} views fwd+bwd (cameras 0..{steps - 1} of {len(spec.cameras)})"},
             "cpu_baseline": {"value": value, "unit": "frames/s", "cores": os.cpu_count() or 1, "kind": "port",
-                             "sample": f"{steps} of the 32 views, full fwd+bwd each (CPU oracle, OpenMP)"},
+                             "sample": f"{steps} of the {len(spec.cameras)} views, full fwd+bwd each "
+                                       f"(CPU oracle, OpenMP)"},
             "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -255,7 +268,9 @@ def main():
     from gstex_cuda_gb300 import batch as B
     from gstex_cuda_gb300 import _lib
 
-    spec = build_workload(args, seed=3 + rank)
+    base_seed = 4 if args.workload == "stress" else 3
+    spec = build_workload(args, seed=base_seed + rank)
+    nviews = len(spec.cameras)
     cams = cameras_of(spec)
     scene = device_scene(spec, dev, bf16=True)
     r = B.BatchRenderer(cams, spec.num_points, channels=3, texture_dtype=torch.bfloat16, device=dev)
@@ -312,7 +327,7 @@ def main():
         elapsed = float(t.item())
     fwd_ms = sum(a.elapsed_time(b) for a, b, _, _ in pairs) / len(pairs)
     bwd_ms = sum(c.elapsed_time(d) for _, _, c, d in pairs) / len(pairs)
-    value = world * args.views * args.steps / elapsed
+    value = world * nviews * args.steps / elapsed
     log(f"eager: {1000 * elapsed / args.steps:.2f} ms/step, {value:.1f} frames/s; fwd {fwd_ms:.2f} ms, bwd {bwd_ms:.2f} ms")
 
     # graph replay of the same step (launch overhead removed)
@@ -328,7 +343,7 @@ def main():
             r.replay()
         g1.record(stream)
         torch.cuda.synchronize(dev)
-        graph_fps = args.views * args.steps / (g0.elapsed_time(g1) / 1000.0)
+        graph_fps = nviews * args.steps / (g0.elapsed_time(g1) / 1000.0)
     except Exception as ex:  # graph capture is an optimisation; report why it was skipped
         graph_fps = f"unavailable: {type(ex).__name__}: {ex}"
     log(f"graph: {graph_fps}")
@@ -349,7 +364,7 @@ def main():
             float(loss.item())
         torch.cuda.synchronize(dev)
         el = time.perf_counter() - t0
-        e2e = {"value": world * args.views * args.steps / el, "unit": "frames/s", "h2d_bytes_per_step": h2d,
+        e2e = {"value": world * nviews * args.steps / el, "unit": "frames/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": 4}
         log(f"e2e: {e2e}")
 
@@ -365,7 +380,7 @@ def main():
             for _ in range(ks):
                 B.plain_step(scene32, cams, tgt_img, tgt_tex, r.pix_offsets_host)
             torch.cuda.synchronize(dev)
-            plain = args.views * ks / (time.perf_counter() - t0)
+            plain = nviews * ks / (time.perf_counter() - t0)
             del scene32
         except Exception as ex:
             plain = f"unavailable: {type(ex).__name__}: {ex}"
@@ -380,7 +395,8 @@ def main():
     peak, peak_kind = measured_peak_hbm()
     dom = ("backward", bb, bwd_ms) if bwd_ms >= fwd_ms else ("forward", fb, fwd_ms)
     achieved = dom[1] / (dom[2] / 1000.0) / 1e9
-    tpi = traffic_per_intersection().get(dom[0])
+    # the measured bytes per intersection belong to the batched scene
+    tpi = traffic_per_intersection().get(dom[0]) if args.workload == "batched" else None
     traffic = tpi * I if tpi else None
 
     cpu = None
@@ -390,7 +406,8 @@ def main():
         try:
             fps, cores, n, el, views = cpu_sample(spec, args.cpu_seconds)
             cpu = {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port",
-                   "sample": f"{n} of the 32 views ({', '.join(views)}), full fwd+bwd each, {el:.1f} s (CPU oracle)"}
+                   "sample": f"{n} of the {nviews} views ({', '.join(views)}), full fwd+bwd each, {el:.1f} s "
+                             f"(CPU oracle)"}
         except Exception as ex:
             cpu = {"value": None, "unavailable": f"{type(ex).__name__}: {ex}"}
         log(f"cpu: {cpu}")
@@ -399,7 +416,7 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1000 * elapsed / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": {"workload": WORKLOAD, "views": args.views, "num_points": N, "texels": T,
+                "config": {"workload": WORKLOADS[args.workload], "views": nviews, "num_points": N, "texels": T,
                            "storage": "bf16 texels [T,4] + bf16 SH; fp32 blending and gradients",
                            "intersections": I, "pixels": P, "tiles": tiles, "parallelism": f"replicas x{world}",
                            "l2": "working set > L2 (no flush)", "timed": "eager, one launch per stage",

@@ -205,7 +205,20 @@ def _both(case, bw, settings, bg):
     return r, fr, fg, gr, gg
 
 
-def _compare(fr, fg, gr, gg, tol, frac, rtol_grad, rows_frac=0.0, one_texel=False):
+def _edge_on(spec, cam, cut=0.05):
+    """Splats seen almost edge-on (|n . mu| / |mu| < cut in camera space): their
+    mean and rotation gradients carry 1/|n.r| and are compared against fp64
+    in test_edge_on_splats_vs_fp64_oracle instead of the reference's fp32."""
+    q = spec.quats.double()
+    w, x, y, z = q.unbind(-1)
+    n = torch.stack([2 * (x * z + w * y), 2 * (y * z - w * x), 1 - 2 * (x * x + y * y)], -1)
+    vm = cam.viewmat.double()
+    mc = spec.means.double() @ vm[:3, :3].T + vm[:3, 3]
+    nc = n @ vm[:3, :3].T
+    return ((nc * mc).sum(-1).abs() / mc.norm(dim=-1) < cut).numpy()
+
+
+def _compare(fr, fg, gr, gg, tol, frac, rtol_grad, rows_frac=0.0, one_texel=False, edge_on=None, row_cap=10.0):
     """Outputs within tol except a fraction frac of threshold flips.  Each
     gradient row (one Gaussian, or one texel) within rtol_grad of the
     reference kernels' largest entry, except a fraction rows_frac of rows,
@@ -221,7 +234,10 @@ def _compare(fr, fg, gr, gg, tol, frac, rtol_grad, rows_frac=0.0, one_texel=Fals
     tmax = float(np.abs(ref_s[..., 1]).max() / max(float(ref_s[..., 0].max()), 1e-6)) + 1.0
     close_frac(np_(fg["reg_s"]), ref_s, tol * (1 + np.abs(ref_s)), frac, "reg_s",
                cap=(1 + tmax + tmax * tmax) / 255 + 1e-2 * np.abs(ref_s))
-    close_frac(np_(fg["reg"]), np_(fr["reg"]), tol * 10 + tol * np.abs(np_(fr["reg"])), frac, "reg")
+    # a flip moves reg by up to (alpha = 1/255) x (t - mean t)^2 x ...: the same bound as reg_s
+    rr = np_(fr["reg"])
+    close_frac(np_(fg["reg"]), rr, tol * 10 + tol * np.abs(rr), frac, "reg",
+               cap=(1 + tmax + tmax * tmax) / 255 + 1e-2 * np.abs(rr))
     same = np_(fg["depth_idx"]) == np_(fr["depth_idx"])
     assert same.mean() >= 1 - frac, ("depth_idx", float(same.mean()))
     # the same depth Gaussian can still give a different depth where the ray
@@ -241,7 +257,9 @@ def _compare(fr, fg, gr, gg, tol, frac, rtol_grad, rows_frac=0.0, one_texel=Fals
         got = got.reshape(ref.shape[0], -1)[:, :ref.shape[1]]
         row = np.abs(got - ref).max(-1) / (np.abs(ref).max() + 1e-12)
         assert (row > rtol_grad).mean() <= rows_frac, (k, float((row > rtol_grad).mean()), float(row.max()))
-        assert row.max() < 10 * rtol_grad, (k, float(row.max()))
+        if edge_on is not None and row.shape[0] == edge_on.shape[0]:
+            row = row[~edge_on]
+        assert row.max() < row_cap * rtol_grad, (k, float(row.max()))
 
 
 @pytest.mark.parametrize("settings", [1 << 8, 0, (1 << 8) | (1 << 9), (1 << 8) | (1 << 10), (1 << 8) | (1 << 2)])
@@ -269,14 +287,18 @@ def test_raster_vs_reference_kernels(which, bw):
     _compare(fr, fg, gr, gg, 1e-4, 3e-3, 2e-3, rows_frac=1e-3, one_texel=which == "untextured")
 
 
-@pytest.mark.parametrize("which", ["untextured_800_100k", "textured_1080p_200k"])
+@pytest.mark.parametrize("which", ["untextured_800_100k", "textured_1080p_200k", "stress_1080p_1M"])
 def test_full_size_vs_reference_kernels(which):
-    """The two single-view workloads at full size against the reference
-    kernels: 800x800 with 100k untextured (1x1-chart) Gaussians and SH degree
-    3 colours; 1920x1080 with 200k Gaussians and 8M fp32 texels.  The tile
-    counts, keys and ranges are compared bit for bit on the way."""
+    """The single-view workloads at full size against the reference kernels:
+    800x800 with 100k untextured (1x1-chart) Gaussians and SH degree 3
+    colours; 1920x1080 with 200k Gaussians and 8M fp32 texels; and one
+    1920x1080 view of the stress scene (1M Gaussians in 64 clusters, 32M fp32
+    texels, heavy per-tile overlap).  The tile counts, keys and ranges are
+    compared bit for bit on the way."""
     from gstex_cuda_gb300 import synthetic
-    spec = synthetic.untextured(seed=1) if which.startswith("untextured") else synthetic.textured_1080p(seed=2)
+    spec = {"untextured_800_100k": lambda: synthetic.untextured(seed=1),
+            "textured_1080p_200k": lambda: synthetic.textured_1080p(seed=2),
+            "stress_1080p_1M": lambda: synthetic.stress(seed=4, views=1)}[which]()
     case = Case(spec)
     bw = 16
     r, fr, fg, gr, gg = _both(case, bw, 1 << 8, [0.0, 0.0, 0.0])
@@ -290,7 +312,77 @@ def test_full_size_vs_reference_kernels(which):
     keys, _ = G.cuda.sort_pairs(isect, gids, G.cuda.sort_end_bit(r["bins"].shape[0]))
     assert torch.equal(keys, r["isect_sorted"])
     assert torch.equal(G.cuda.get_tile_bin_edges(r["n"], keys, r["tile_bounds"]), r["bins"])
-    _compare(fr, fg, gr, gg, 1e-4, 3e-3, 2e-3, rows_frac=1e-3, one_texel=which.startswith("untextured"))
+    # The stress scene's 64 dense clusters put more pairs near the thresholds,
+    # and its smallest splats (s = 0.005) have uv maps of 1/(6 s) = 33 per unit,
+    # which carry a texel-edge flip of the uv gradient into the mean gradient
+    # 33 times over: its rare outlier rows get a cap of 5% of the largest entry.
+    stress = which.startswith("stress")
+    _compare(fr, fg, gr, gg, 1e-4, 5e-3 if stress else 3e-3, 2e-3, rows_frac=1e-3,
+             one_texel=which.startswith("untextured"), edge_on=_edge_on(spec, case.cam),
+             row_cap=25.0 if stress else 10.0)
+
+
+def test_edge_on_splats_vs_fp64_oracle():
+    """A scene of splats seen almost edge-on (|n.d| from 1e-4 to 5e-2 at the
+    mean), where the ray-plane solve is ill-conditioned: the gradients of this
+    package (records solved in double for these splats) and of the reference
+    kernels (fp32, fast math) against the fp64 oracle.  Both are within a few
+    1e-3 of the largest entry; ours must be within twice the reference's error
+    or 5e-3."""
+    import oracle
+    g = torch.Generator().manual_seed(31)
+    spec = small_scene(n=120, width=96, height=64, seed=31, f=96.0)
+    # rotate every splat so that its normal is nearly perpendicular to the view ray
+    mc = spec.means.double()
+    d = mc / mc.norm(dim=-1, keepdim=True)
+    t = torch.cross(d, torch.randn(mc.shape, generator=g, dtype=torch.float64), dim=-1)
+    t = t / t.norm(dim=-1, keepdim=True)
+    eps = torch.exp(torch.empty(mc.shape[0], 1, dtype=torch.float64).uniform_(np.log(1e-4), np.log(5e-2),
+                                                                              generator=g))
+    n = t + eps * d
+    n = n / n.norm(dim=-1, keepdim=True)
+    a1 = torch.cross(n, torch.randn(mc.shape, generator=g, dtype=torch.float64), dim=-1)
+    a1 = a1 / a1.norm(dim=-1, keepdim=True)
+    a2 = torch.cross(n, a1, dim=-1)
+    Rm = torch.stack([a1, a2, n], -1)  # columns = axes
+    # rotation matrix -> quaternion (w, x, y, z), trace method with a safe branch
+    qs = []
+    for R in Rm:
+        tr = R.trace()
+        if tr > 0:
+            sq = torch.sqrt(tr + 1.0) * 2
+            qs.append(torch.stack([0.25 * sq, (R[2, 1] - R[1, 2]) / sq, (R[0, 2] - R[2, 0]) / sq,
+                                   (R[1, 0] - R[0, 1]) / sq]))
+        else:
+            i = int(torch.argmax(torch.diagonal(R)))
+            j, k = (i + 1) % 3, (i + 2) % 3
+            sq = torch.sqrt(1.0 + R[i, i] - R[j, j] - R[k, k]) * 2
+            q = torch.zeros(4, dtype=torch.float64)
+            q[0] = (R[k, j] - R[j, k]) / sq
+            q[1 + i] = 0.25 * sq
+            q[1 + j] = (R[j, i] + R[i, j]) / sq
+            q[1 + k] = (R[k, i] + R[i, k]) / sq
+            qs.append(q)
+    spec.quats.copy_(torch.stack(qs).float())
+    spec.umap.copy_((a1 / (6 * spec.scales[:, :1].double()))[:, None].float())
+    spec.vmap.copy_((a2 / (6 * spec.scales[:, 1:2].double()))[:, None].float())
+    case = Case(spec)
+    assert _edge_on(spec, case.cam).all()
+    bg = [0.0, 0.0, 0.0]
+    r, fr, fg, gr, gg = _both(case, 16, 1 << 8, bg)
+    C = spec.texture.shape[1]
+    ups = upstream(case.cam.height, case.cam.width, C)
+    gids, bins = r["gids_sorted"].cpu().numpy(), r["bins"].cpu().numpy()
+    fwd = oracle.texture_forward(case.scene_np, case.cam_np, gids, bins, 16, 1 << 8, np.asarray(bg), prec="f64")
+    go = oracle.texture_backward(case.scene_np, case.cam_np, gids, bins, 16, 1 << 8, np.asarray(bg), fwd,
+                                 ups["img"], ups["depth"], ups["reg"], ups["alpha"], ups["texture"], ups["normal"],
+                                 prec="f64")
+    for k in ("means", "quats", "scales", "opacity", "colors", "uv0", "umap", "vmap"):
+        truth = np.asarray(go[k]).reshape(spec.num_points, -1)
+        scale = np.abs(truth).max() + 1e-12
+        e_ours = np.abs(np_(gg[k]).reshape(spec.num_points, -1) - truth).max() / scale
+        e_ref = np.abs(np_(gr[k]).reshape(spec.num_points, -1) - truth).max() / scale
+        assert e_ours <= max(2 * e_ref, 5e-3), (k, float(e_ours), float(e_ref))
 
 
 def test_alpha_visualisation_forward_vs_reference_kernels():
