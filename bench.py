@@ -145,6 +145,25 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
+def max_over_ranks(x: float) -> float:
+    """The largest value of x over the ranks of the default process group
+    (NCCL: through a CUDA tensor; gloo: a CPU tensor); x without a group."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    dev = torch.device("cuda", torch.cuda.current_device()) if dist.get_backend() == "nccl" else torch.device("cpu")
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_frames_per_s(world: int, views: int, steps: int, elapsed_max: float) -> float:
+    """Whole-job throughput: every rank renders `views` frames per step (weak
+    scaling, replicas), timed by the slowest rank."""
+    return world * views * steps / elapsed_max
+
+
 def traffic_per_intersection():
     """DRAM bytes per intersection of the compositor kernels, measured with ncu
     on a smaller case of the same workload (the committed profile summary); the full
@@ -318,16 +337,14 @@ def main():
         pairs.append((f0, f1, b0, b1))
     e_end.record(stream)
     torch.cuda.synchronize(dev)
+    if world > 1:
+        dist.barrier()
     launches = _lib.lib().gstex_launch_count() - n0
     clk = clocks.stop()
-    elapsed = e_start.elapsed_time(e_end) / 1000.0
-    if world > 1:
-        t = torch.tensor([elapsed], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
+    elapsed = max_over_ranks(e_start.elapsed_time(e_end) / 1000.0)
     fwd_ms = sum(a.elapsed_time(b) for a, b, _, _ in pairs) / len(pairs)
     bwd_ms = sum(c.elapsed_time(d) for _, _, c, d in pairs) / len(pairs)
-    value = world * nviews * args.steps / elapsed
+    value = job_frames_per_s(world, nviews, args.steps, elapsed)
     log(f"eager: {1000 * elapsed / args.steps:.2f} ms/step, {value:.1f} frames/s; fwd {fwd_ms:.2f} ms, bwd {bwd_ms:.2f} ms")
 
     # graph replay of the same step (launch overhead removed)
