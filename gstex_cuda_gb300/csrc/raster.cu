@@ -630,7 +630,8 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
         const int bsize = min(nthr, bend + 1 - range.x);
         const int idx = bend - tr;
         if (idx >= range.x) stage_job(R, tr, a, J, a.gids[idx], use_blur);
-        for (int q = tr; q < nthr * kMoments; q += nthr) smom[q] = 0.f;
+        for (int q = tr; q < nthr * (kMomSlot / 4); q += nthr)
+            reinterpret_cast<float4*>(smom)[q] = make_float4(0.f, 0.f, 0.f, 0.f);
         touched[tr] = 0;
         __syncthreads();
         // splats outside their alpha >= 1/255 box contribute nothing here:
@@ -685,7 +686,7 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
                 if (valid[p])
                     bwd_pair<TEXMODE, CT, CA>(a, g, R, k, gidx, Hr, H[p], alpha[p], e[p], eb[p], nbf[p], bf[p], S[p],
                                               C, use_ndc, prop_uv, bilinear, m);
-            float* dst = smom + k * kMoments;
+            float* dst = smom + k * kMomSlot;
             if (lane == 0) touched[k] = 1;
             // few valid lanes: each adds its own moments; else one transpose reduction
             if (full_warp && __popc(vmask) > GSTEX_SPARSE_LANES) {
@@ -698,7 +699,12 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
         }
         __syncthreads();
         if (idx >= range.x && touched[tr]) {
-            const float* sm = smom + tr * kMoments;
+            float sm[kMomSlot];
+#pragma unroll
+            for (int q = 0; q < kMomSlot / 4; q++) {
+                const float4 v4 = reinterpret_cast<const float4*>(smom + tr * kMomSlot)[q];
+                sm[4 * q] = v4.x; sm[4 * q + 1] = v4.y; sm[4 * q + 2] = v4.z; sm[4 * q + 3] = v4.w;
+            }
             {
                 const int gid = R.warm[tr].tex.w;
                 if (J.vc_stride == 4) {
@@ -876,7 +882,7 @@ __global__ void BWD_BOUNDS(PPT) bwd_view_kernel(SceneArgs a, ViewArgs va, BwdArg
     J.vcolors = va.vcolors;
     J.vc_stride = 3;
     J.recs = nullptr;
-    uint8_t* lists = smem + (size_t)(kRecBytes + kEdgeBytes + kMoments * sizeof(float)) * nthr;
+    uint8_t* lists = smem + (size_t)(kRecBytes + kEdgeBytes + kMomSlot * sizeof(float)) * nthr;
     bwd_tile<TEXMODE, CT, PPT>(a, J, g, Recs::carve(smem, nthr, true),
                                reinterpret_cast<float*>(smem + (size_t)(kRecBytes + kEdgeBytes) * nthr), lists,
                                lists + (size_t)ceil_div(nthr, 32) * nthr);
@@ -924,7 +930,7 @@ __global__ void BWD_BOUNDS(PPT) bwd_batch_kernel(SceneArgs a, BatchArgs ba, BwdA
     TileJob J;
     const Recs R = Recs::carve(smem, nthr, true);
     float* smom = reinterpret_cast<float*>(smem + (size_t)(kRecBytes + kEdgeBytes) * nthr);
-    uint8_t* lists = smem + (size_t)(kRecBytes + kEdgeBytes + kMoments * sizeof(float)) * nthr;
+    uint8_t* lists = smem + (size_t)(kRecBytes + kEdgeBytes + kMomSlot * sizeof(float)) * nthr;
     uint8_t* touched = lists + (size_t)ceil_div(nthr, 32) * nthr;
     while (next_job(ba, &s_tile, J)) bwd_tile<TEXMODE, CT, PPT>(a, J, g, R, smom, lists, touched);
 }
@@ -1095,7 +1101,7 @@ static size_t list_bytes(int bw, int ppt) {
 size_t fwd_smem(int bw, int ppt) { return (size_t)kRecBytes * threads_of(bw, ppt) + list_bytes(bw, ppt); }
 size_t bwd_smem(int bw, int ppt) {
     // ... then one "touched" flag per slot
-    return ((size_t)kRecBytes + kEdgeBytes + kMoments * sizeof(float) + 1) * threads_of(bw, ppt) +
+    return ((size_t)kRecBytes + kEdgeBytes + kMomSlot * sizeof(float) + 1) * threads_of(bw, ppt) +
            list_bytes(bw, ppt);
 }
 
