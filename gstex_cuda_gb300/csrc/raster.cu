@@ -135,15 +135,6 @@ __device__ __forceinline__ void fetch3(const void* tex, const Bilerp& B, float c
 #ifndef GSTEX_WARP_BLOCK
 #define GSTEX_WARP_BLOCK 1
 #endif
-// Candidate lists in the forward (off: forward pixels saturate early, and
-// walking every staged slot with a per-thread box test measured faster).
-// Warps with at most this many valid lanes skip the transpose reduction.
-#ifndef GSTEX_SPARSE_LANES
-#define GSTEX_SPARSE_LANES 0
-#endif
-#ifndef GSTEX_FWD_LIST
-#define GSTEX_FWD_LIST 0
-#endif
 template <int PPT>
 __device__ __forceinline__ int2 thread_pixel(int bw) {
 #if GSTEX_WARP_BLOCK
@@ -196,14 +187,11 @@ __device__ __forceinline__ int build_list(uint8_t* wl, const Recs& R, int k0, in
 // staged record read from shared memory is used for PPT pixels.
 // ---------------------------------------------------------------------------
 template <int TEXMODE, int CT, int PPT>
-__device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, const FwdOut& o, const Recs& R,
-                                         uint8_t* lists) {
+__device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, const FwdOut& o, const Recs& R) {
     const int nthr = blockDim.x * blockDim.y;
     const int tr = threadIdx.y * blockDim.x + threadIdx.x;
     const int bw = blockDim.x;
     const unsigned wmask = __activemask();
-    const unsigned lane = tr & 31;
-    uint8_t* wl = lists + (tr >> 5) * nthr;
     const View& V = J.V;
     const bool use_blur = a.settings & (1 << 9);
     const bool use_ndc = a.settings & (1 << 10);
@@ -257,38 +245,8 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
         __syncthreads();
         const int bsize = min(nthr, range.y - bstart);
         if (__all_sync(wmask, all_done)) continue;
-        // Outside its alpha >= 1/255 box the reference skips a splat, and can
-        // end a pixel there only when T <= 1e-4 * 255/254.  While every live
-        // pixel of the warp has T > 1.01e-4 the warp walks its candidate list;
-        // once one has not, it walks every remaining slot in order.
-        int cnt = 0;
-        bool low = false;
-#pragma unroll
-        for (int p = 0; p < PPT; p++) low = low || (!done[p] && T[p] <= 1.01e-4f);
-#if GSTEX_FWD_LIST
-        bool slow = __any_sync(wmask, low);
-        if (!slow) {
-            // rectangle of the warp's pixel centres (pixel centres are positive,
-            // so their float bits order like integers)
-            const float rx0 = __int_as_float(__reduce_min_sync(wmask, __float_as_int(P[0].px)));
-            const float rx1 = __int_as_float(__reduce_max_sync(wmask, __float_as_int(P[0].px)));
-            const float ry0 = __int_as_float(__reduce_min_sync(wmask, __float_as_int(P[0].py)));
-            const float ry1 = __int_as_float(__reduce_max_sync(wmask, __float_as_int(P[PPT - 1].py)));
-            cnt = build_list(wl, R, 0, bsize, rx0, rx1, ry0, ry1, wmask, lane);
-        }
-#else
-        bool slow = true;
-#endif
-        int j = 0, k = -1;
-        int kn = (!slow && cnt > 0) ? wl[0] : 0;
-        while (true) {
-            if (!slow) {
-                if (j >= cnt) break;
-                k = kn;
-                if (++j < cnt) kn = wl[j];
-            } else if (++k >= bsize) {
-                break;
-            }
+        // Every staged slot in order; each pixel tests the splat's box first.
+        for (int k = 0; k < bsize; ++k) {
             const float4 hb = R.hot[k].b, hd = R.hot[k].d;
             bool need = false;
 #pragma unroll
@@ -367,15 +325,10 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
             }
             }
             bool ad = true;
-            low = false;
 #pragma unroll
-            for (int p = 0; p < PPT; p++) {
-                ad = ad && done[p];
-                low = low || (!done[p] && T[p] <= 1.01e-4f);
-            }
+            for (int p = 0; p < PPT; p++) ad = ad && done[p];
             all_done = ad;
             if (__all_sync(wmask, all_done)) break;
-            if (!slow) slow = __any_sync(wmask, low);
         }
     }
 #pragma unroll
@@ -688,8 +641,7 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
                                               C, use_ndc, prop_uv, bilinear, m);
             float* dst = smom + k * kMomSlot;
             if (lane == 0) touched[k] = 1;
-            // few valid lanes: each adds its own moments; else one transpose reduction
-            if (full_warp && __popc(vmask) > GSTEX_SPARSE_LANES) {
+            if (full_warp) {
                 const float s = warp_transpose_reduce(m, lane);
                 if (lane < (unsigned)kMoments) atomicAdd(dst + lane, s);
             } else if (any) {
@@ -865,7 +817,7 @@ __global__ void FWD_BOUNDS(PPT) fwd_view_kernel(SceneArgs a, ViewArgs va, FwdOut
     J.vc_stride = 3;
     J.recs = nullptr;
     const int nthr = blockDim.x * blockDim.y;
-    fwd_tile<TEXMODE, CT, PPT>(a, J, o, Recs::carve(smem, nthr, false), smem + (size_t)kRecBytes * nthr);
+    fwd_tile<TEXMODE, CT, PPT>(a, J, o, Recs::carve(smem, nthr, false));
 }
 
 template <int TEXMODE, int CT, int PPT>
@@ -918,8 +870,7 @@ __global__ void FWD_BOUNDS(PPT) fwd_batch_kernel(SceneArgs a, BatchArgs ba, FwdO
     TileJob J;
     const int nthr = blockDim.x * blockDim.y;
     const Recs R = Recs::carve(smem, nthr, false);
-    uint8_t* lists = smem + (size_t)kRecBytes * nthr;
-    while (next_job(ba, &s_tile, J)) fwd_tile<TEXMODE, CT, PPT>(a, J, o, R, lists);
+    while (next_job(ba, &s_tile, J)) fwd_tile<TEXMODE, CT, PPT>(a, J, o, R);
 }
 
 template <int TEXMODE, int CT, int PPT>
@@ -1098,7 +1049,7 @@ static size_t list_bytes(int bw, int ppt) {
     const int n = threads_of(bw, ppt);
     return (size_t)ceil_div(n, 32) * n;
 }
-size_t fwd_smem(int bw, int ppt) { return (size_t)kRecBytes * threads_of(bw, ppt) + list_bytes(bw, ppt); }
+size_t fwd_smem(int bw, int ppt) { return (size_t)kRecBytes * threads_of(bw, ppt); }
 size_t bwd_smem(int bw, int ppt) {
     // ... then one "touched" flag per slot
     return ((size_t)kRecBytes + kEdgeBytes + kMomSlot * sizeof(float) + 1) * threads_of(bw, ppt) +
