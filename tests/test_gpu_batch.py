@@ -165,3 +165,104 @@ def test_prebuilt_records_match_per_tile_records(setup):
     for k in ("opacity", "means", "scales", "quats", "uv0", "umap", "vmap", "texture", "sh_coeffs"):
         a, b = r2.grads[k].cpu().numpy(), g1[k].cpu().numpy()
         assert np.abs(a - b).max() <= 1e-3 * (np.abs(b).max() + 1e-12), k
+
+
+def _bf16_case():
+    from gstex_cuda_gb300 import batch as B, synthetic
+    g = torch.Generator().manual_seed(19)
+    cams = synthetic.sphere_cameras(g, 3, radius=8.0, resolutions=[(96, 64), (80, 80), (128, 72)])
+    spec = synthetic._finish_with_area(g, torch.empty(2500, 3).uniform_(-3, 3, generator=g), 0.01, 0.1, 3, "normal",
+                                       cams, 30_000, "multi", {})
+    t16 = torch.zeros(spec.texture.shape[0], 4, dtype=torch.bfloat16)
+    t16[:, :3] = spec.texture.to(torch.bfloat16)
+    sh16 = spec.sh_coeffs.to(torch.bfloat16)
+    scene = B.Scene(means=spec.means.to(DEV), scales=spec.scales.to(DEV), quats=spec.quats.to(DEV),
+                    opacity=spec.opacity.to(DEV), sh_coeffs=sh16.to(DEV), sh_degree=3, uv0=spec.uv0.to(DEV),
+                    umap=spec.umap.to(DEV), vmap=spec.vmap.to(DEV), texture_dims=spec.texture_dims.to(DEV),
+                    texture=t16.to(DEV))
+    bcams = [B.Camera(c.viewmat, c.fx, c.fy, c.cx, c.cy, c.width, c.height) for c in cams]
+    r = B.BatchRenderer(bcams, spec.num_points, texture_dtype=torch.bfloat16, capacity=1 << 20)
+    gen = torch.Generator().manual_seed(2)
+    tgt_img = torch.rand(r.total_pixels, 3, generator=gen).to(DEV)
+    tgt_tex = torch.rand(r.total_pixels, 3, generator=gen).to(DEV)
+    r.step(scene, tgt_img, tgt_tex)
+    torch.cuda.synchronize()
+    return spec, cams, r, t16[:, :3].double().numpy(), sh16.double().numpy()
+
+
+def _oracle_views(spec, cams, r, texture, sh):
+    """Per-view fp64 oracle outputs and view-summed gradients for the given
+    texel values and SH coefficients, on the renderer's binning."""
+    gs, bins = r.gids_sorted.cpu().numpy(), r.bins.cpu().numpy()
+    ups = {k: v.cpu().numpy() for k, v in r.ups.items()}
+    outs, tot, toff = [], None, 0
+    for v, cam in enumerate(cams):
+        dirs = (spec.means - cam.position[None]).numpy()
+        col = oracle.sh_forward(3, 3, dirs, sh, prec="f64")
+        sc = _scene_np(spec, col)
+        sc.texture = texture
+        oc = oracle.Camera(cam.viewmat.numpy(), cam.c2w.numpy(), cam.fx, cam.fy, cam.cx, cam.cy, cam.height,
+                           cam.width)
+        nt = ((cam.width + 15) // 16) * ((cam.height + 15) // 16)
+        vb = bins[toff:toff + nt]
+        toff += nt
+        ref = oracle.texture_forward(sc, oc, gs, vb, 16, 1 << 8, np.zeros(3), prec="f64")
+        outs.append(ref)
+        a, b = r.pix_offsets_host[v], r.pix_offsets_host[v + 1]
+        H, W = cam.height, cam.width
+        gg = oracle.texture_backward(sc, oc, gs, vb, 16, 1 << 8, np.zeros(3), ref,
+                                     ups["img"][a:b].reshape(H, W, 3), np.zeros((H, W)),
+                                     ups["reg"][a:b].reshape(H, W), np.zeros((H, W)),
+                                     ups["texture"][a:b].reshape(H, W, 3), ups["normal"][a:b].reshape(H, W, 3),
+                                     prec="f64")
+        tot = gg if tot is None else {k: tot[k] + gg[k] for k in tot}
+    return outs, tot
+
+
+def _errors(r, outs, tot):
+    img_err = []
+    for v, ref in enumerate(outs):
+        for k in ("img", "texture"):
+            got = r.view_output(k, v).cpu().numpy()
+            img_err.append(np.abs(got - ref[k].reshape(got.shape)).reshape(-1))
+    img_err = np.concatenate(img_err)
+    g_err = {}
+    for k in ("opacity", "means", "scales", "quats", "uv0", "umap", "vmap", "texture"):
+        got = r.grads[k].cpu().numpy()
+        if k == "texture":
+            got = got[:, :3]
+        ref = tot[k].reshape(got.shape)
+        rows = np.abs(got - ref).reshape(got.shape[0], -1).max(-1) / (np.abs(ref).max() + 1e-12)
+        # (largest row error, fraction of rows above 1e-3, fraction above 1e-2)
+        g_err[k] = (float(rows.max()), float((rows > 1e-3).mean()), float((rows > 1e-2).mean()))
+    return img_err, g_err
+
+
+def test_bf16_storage_accuracy_vs_fp64_oracle():
+    """The headline storage: bf16 texels [T,4] and bf16 SH coefficients, all
+    blending, transmittance and gradient accumulation in fp32.  (A) Against
+    the fp64 oracle at the stored (bf16) parameter values: outputs within
+    1e-4 and gradients within 1e-3 of the largest entry, threshold flips
+    excepted: at most 0.5% of the gradient rows (one Gaussian or texel)
+    beyond 1e-3 of the largest entry, none beyond 5e-2.  A pixel whose alpha
+    flips at 1/255 changes its final distortion sums, and with the distortion
+    weight of 100 that moves the geometry gradients of every splat at that
+    pixel.  (B) Against the fp64 oracle at the unrounded fp32 values (what
+    storing in bf16 changes): image and texture within 2e-3 abs, at most
+    0.5% of the gradient rows beyond 1e-2, none beyond 1e-1."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    spec, cams, r, tex16, sh16 = _bf16_case()
+    img_a, g_a = _errors(r, *_oracle_views(spec, cams, r, tex16, sh16))
+    print("bf16 storage vs stored values: image/texture frac > 1e-4", float((img_a > 1e-4).mean()),
+          "gradients (max row, frac > 1e-3)", g_a)
+    assert (img_a > 1e-4).mean() <= 1e-3, float((img_a > 1e-4).mean())
+    for k, (mx, fr, _) in g_a.items():
+        assert fr <= 5e-3 and mx < 5e-2, ("stored values", k, mx, fr)
+    img_b, g_b = _errors(r, *_oracle_views(spec, cams, r, spec.texture.double().numpy(),
+                                           spec.sh_coeffs.double().numpy()))
+    print("bf16 storage vs fp32 values: image/texture 99.9% quantile", float(np.quantile(img_b, 0.999)),
+          "gradients", g_b)
+    assert (img_b > 2e-3).mean() <= 1e-3, float((img_b > 2e-3).mean())
+    for k, (mx, _, fr2) in g_b.items():
+        assert fr2 <= 5e-3 and mx < 1e-1, ("fp32 values", k, mx, fr2)
