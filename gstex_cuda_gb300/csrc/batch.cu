@@ -311,10 +311,10 @@ static int batch_scene(const gstex_batch_inputs* in, SceneArgs& a, BatchArgs& ba
     GSTEX_REQUIRE(in->channels >= 0);
     if (in->channels > kMaxChannels) return GSTEX_ERR_UNSUPPORTED;
     if (in->texture_dtype == 1 && in->channels != 3) return GSTEX_ERR_UNSUPPORTED;
-    GSTEX_REQUIRE(in->views && in->tile_view && in->tile_bins && in->colors && in->background && in->queue);
+    GSTEX_REQUIRE(in->views && in->tile_view && in->tile_bins && in->background && in->queue);
     if (in->num_points > 0)
-        GSTEX_REQUIRE(in->gaussian_ids_sorted && in->texture_dims && in->opacities && in->means && in->scales &&
-                      in->quats && in->uv0 && in->umap && in->vmap);
+        GSTEX_REQUIRE(in->gaussian_ids_sorted && in->colors && in->texture_dims && in->opacities && in->means &&
+                      in->scales && in->quats && in->uv0 && in->umap && in->vmap);
     a.N = in->num_points;
     a.C = in->channels;
     a.T = in->num_texels;
@@ -358,6 +358,7 @@ extern "C" int gstex_batch_records(const gstex_batch_inputs* in, const int32_t* 
     BatchArgs ba;
     int rc = batch_scene(in, a, ba);
     if (rc) return rc;
+    if (a.N == 0) return GSTEX_OK;
     GSTEX_REQUIRE(records && ((uintptr_t)records & 15) == 0 && workspace && ((uintptr_t)workspace & 15) == 0);
     if ((unsigned long long)a.N * (unsigned long long)in->num_views > 0xffffffffull) return GSTEX_ERR_UNSUPPORTED;
     if (workspace_bytes < gstex_batch_records_workspace_bytes(a.N, in->num_views)) return GSTEX_ERR_CAPACITY;
@@ -400,7 +401,9 @@ extern "C" int gstex_batch_backward(const gstex_batch_inputs* in, const gstex_ba
     int rc = batch_scene(in, a, ba);
     if (rc) return rc;
     if (in->settings & (1 << 16)) return GSTEX_ERR_UNSUPPORTED;  // alpha-visualisation mode: forward only
-    GSTEX_REQUIRE(io && io->final_T && io->final_idx && io->depth_idx && io->reg_s && io->workspace);
+    GSTEX_REQUIRE(io);
+    if (a.N == 0) return GSTEX_OK;  // no Gaussian, no gradient
+    GSTEX_REQUIRE(io->final_T && io->final_idx && io->depth_idx && io->reg_s && io->workspace);
     GSTEX_REQUIRE(io->v_colors && io->v_opacity && io->v_means && io->v_scales && io->v_quats && io->v_uv0 &&
                   io->v_umap && io->v_vmap);
     if (a.C > 0) GSTEX_REQUIRE(io->v_tex_grad);
