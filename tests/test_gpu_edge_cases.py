@@ -47,7 +47,7 @@ def test_nothing_on_screen_renders_the_background():
     case, outs, nt = _render(spec)
     img, depth, reg, alpha, tex, normal = outs
     np.testing.assert_allclose(np_(img), np.broadcast_to([0.25, 0.5, 0.75], img.shape), atol=1e-7)
-    assert float(alpha.abs().max()) == 0.0 and float(tex.abs().max()) == 0.0
+    assert float(alpha.detach().abs().max()) == 0.0 and float(tex.detach().abs().max()) == 0.0
     (img.sum() + tex.sum() + normal.sum() + reg.sum() + depth.sum()).backward()
     for k in ("means", "opacity", "texture", "quats"):
         assert float(case.t[k].grad.abs().max()) == 0.0, k
