@@ -181,6 +181,22 @@ def traffic_per_intersection():
     return out
 
 
+def reference_kernels_plain_fps():
+    """frames/s of the reference's own kernels run per view in fp32 on the
+    batched scene, from the committed measurement (the reference's kernels
+    are test infrastructure and do not run inside this benchmark)."""
+    import re
+    try:
+        with open(os.path.join(HERE, "profiles", "reference_kernels_plain_32views.md")) as f:
+            for line in f:
+                m = re.match(r"^\| reference kernels, plain per-view fp32 \| ([0-9.]+) \|", line.strip())
+                if m:
+                    return float(m.group(1))
+    except OSError:
+        pass
+    return None
+
+
 def algorithmic_bytes(I, tiles, T, P, C, N, tex_bytes_per_texel, grad_texel_bytes, backward):
     """Compulsory bytes of one compositor launch: per intersection a 4-byte id
     and the 96-byte fp32 Gaussian record; per tile its range; every texel once;
@@ -416,6 +432,8 @@ def main():
     tpi = traffic_per_intersection().get(dom[0]) if args.workload == "batched" else None
     traffic = tpi * I if tpi else None
 
+    ref_plain = reference_kernels_plain_fps() if args.workload == "batched" and nviews == 32 else None
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         import oracle
@@ -446,7 +464,11 @@ def main():
                 "kernels_ms": {"forward": fwd_ms, "backward": bwd_ms},
                 "graph_frames_per_s": graph_fps,
                 "plain_fp32_frames_per_s": plain,
-                "speedup_vs_plain_fp32": (value / plain) if plain else None,
+                "speedup_vs_plain_fp32": (value / plain) if isinstance(plain, float) else None,
+                "reference_kernels_plain_fp32_frames_per_s": ref_plain,
+                "speedup_vs_reference_kernels_plain_fp32": (value / ref_plain) if ref_plain else None,
+                "reference_kernels_source": "profiles/reference_kernels_plain_32views.md (same scene, same GPU model, "
+                                            "oracle/refkern/time_plain.py)" if ref_plain else None,
                 "cpu_baseline": cpu, "clocks": clk}
         print(json.dumps(line), flush=True)
     if world > 1:

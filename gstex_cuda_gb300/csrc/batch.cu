@@ -20,19 +20,23 @@ namespace gstex {
 // One thread per Gaussian loops over the views so parameters and SH
 // coefficients are read once.
 // ---------------------------------------------------------------------------
-template <typename SHT>
+// SH degree DEG is a template parameter so that the coefficient and basis
+// arrays stay in registers.
+template <typename SHT, int DEG>
 __global__ void batch_project_kernel(int N, int V, const BatchView* __restrict__ views, const float3* __restrict__ means,
                                      const float* __restrict__ scales, float glob, const float4* __restrict__ quats,
-                                     const SHT* __restrict__ sh, int sh_degree, int bw, float3* __restrict__ colors,
+                                     const SHT* __restrict__ sh, int bw, float3* __restrict__ colors,
                                      int32_t* __restrict__ counts) {
+    constexpr int B = (DEG + 1) * (DEG + 1);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     const float3 p = means[i];
     const float4 q = quats[i];
     const float sx = scales[3 * i], sy = scales[3 * i + 1];
-    const int B = sh_bases(sh_degree);
-    float k[25][3];
+    float k[B][3];
+#pragma unroll
     for (int b = 0; b < B; b++)
+#pragma unroll
         for (int c = 0; c < 3; c++) k[b][c] = (float)sh[((size_t)i * B + b) * 3 + c];
     for (int v = 0; v < V; v++) {
         const BatchView& bv = views[v];
@@ -49,9 +53,10 @@ __global__ void batch_project_kernel(int N, int V, const BatchView* __restrict__
         aabb_2d(m, bv.V.fx, bv.V.fy, bv.V.cx, bv.V.cy, p, q, sx, sy, glob, c, e, z);
         counts[(size_t)v * N + i] = tiles_hit(c, e, bv.tiles_x, bv.tiles_y, (float)bw);
         float Y[25];
-        const int nb = sh_basis(sh_degree, make_float3(p.x - bv.campos[0], p.y - bv.campos[1], p.z - bv.campos[2]), Y);
+        sh_basis(DEG, make_float3(p.x - bv.campos[0], p.y - bv.campos[1], p.z - bv.campos[2]), Y);
         float3 col = make_float3(0.f, 0.f, 0.f);
-        for (int b = 0; b < nb; b++) {
+#pragma unroll
+        for (int b = 0; b < B; b++) {
             col.x += Y[b] * k[b][0];
             col.y += Y[b] * k[b][1];
             col.z += Y[b] * k[b][2];
@@ -164,28 +169,32 @@ __global__ void batch_loss_kernel(long long total, int V, const long long* __res
 }
 
 // SH adjoint summed over views: v_coeffs[i,b,c] = sum_v Y_b(dir_v) v_color[v,i,c].
+template <int DEG>
 __global__ void batch_sh_backward_kernel(int N, int V, const BatchView* __restrict__ views,
-                                         const float3* __restrict__ means, int sh_degree,
-                                         const float4* __restrict__ vcol, float* __restrict__ v_coeffs) {
+                                         const float3* __restrict__ means, const float4* __restrict__ vcol,
+                                         float* __restrict__ v_coeffs) {
+    constexpr int B = (DEG + 1) * (DEG + 1);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
-    const int B = sh_bases(sh_degree);
-    float acc[25][3];
-    for (int b = 0; b < 25; b++) acc[b][0] = acc[b][1] = acc[b][2] = 0.f;
+    float acc[B][3];
+#pragma unroll
+    for (int b = 0; b < B; b++) acc[b][0] = acc[b][1] = acc[b][2] = 0.f;
     const float3 p = means[i];
     for (int v = 0; v < V; v++) {
         const float4 g = vcol[(size_t)v * N + i];
         if (g.x == 0.f && g.y == 0.f && g.z == 0.f) continue;
         const BatchView& bv = views[v];
         float Y[25];
-        const int nb = sh_basis(sh_degree, make_float3(p.x - bv.campos[0], p.y - bv.campos[1], p.z - bv.campos[2]), Y);
-        for (int b = 0; b < nb; b++) {
+        sh_basis(DEG, make_float3(p.x - bv.campos[0], p.y - bv.campos[1], p.z - bv.campos[2]), Y);
+#pragma unroll
+        for (int b = 0; b < B; b++) {
             acc[b][0] += Y[b] * g.x;
             acc[b][1] += Y[b] * g.y;
             acc[b][2] += Y[b] * g.z;
         }
     }
     float* o = v_coeffs + (size_t)i * B * 3;
+#pragma unroll
     for (int b = 0; b < B; b++) {
         o[3 * b + 0] = acc[b][0];
         o[3 * b + 1] = acc[b][1];
@@ -270,6 +279,23 @@ extern "C" int gstex_batch_prepare(int num_views, const gstex_view_desc* views, 
     return GSTEX_OK;
 }
 
+template <typename SHT>
+static void project_launch(int deg, int N, int V, const BatchView* bv, const float* means, const float* scales,
+                           float glob, const float* quats, const SHT* sh, int bw, float* colors, int32_t* counts,
+                           cudaStream_t stream) {
+    const dim3 grid(ceil_div(N, 128)), block(128);
+    const float3* m = (const float3*)means;
+    const float4* q = (const float4*)quats;
+    float3* c = (float3*)colors;
+    switch (deg) {
+        case 0: batch_project_kernel<SHT, 0><<<grid, block, 0, stream>>>(N, V, bv, m, scales, glob, q, sh, bw, c, counts); break;
+        case 1: batch_project_kernel<SHT, 1><<<grid, block, 0, stream>>>(N, V, bv, m, scales, glob, q, sh, bw, c, counts); break;
+        case 2: batch_project_kernel<SHT, 2><<<grid, block, 0, stream>>>(N, V, bv, m, scales, glob, q, sh, bw, c, counts); break;
+        case 3: batch_project_kernel<SHT, 3><<<grid, block, 0, stream>>>(N, V, bv, m, scales, glob, q, sh, bw, c, counts); break;
+        default: batch_project_kernel<SHT, 4><<<grid, block, 0, stream>>>(N, V, bv, m, scales, glob, q, sh, bw, c, counts); break;
+    }
+}
+
 extern "C" int gstex_batch_project(int N, int V, const void* views_dev, const float* means, const float* scales,
                                    float glob_scale, const float* quats, const void* sh_coeffs, int sh_dtype,
                                    int sh_degree, int block_width, float* colors, int32_t* counts, gstex_stream_t s) {
@@ -280,13 +306,11 @@ extern "C" int gstex_batch_project(int N, int V, const void* views_dev, const fl
     cudaStream_t stream = (cudaStream_t)s;
     const BatchView* bv = (const BatchView*)views_dev;
     if (sh_dtype == 1)
-        batch_project_kernel<__nv_bfloat16><<<ceil_div(N, 128), 128, 0, stream>>>(
-            N, V, bv, (const float3*)means, scales, glob_scale, (const float4*)quats,
-            (const __nv_bfloat16*)sh_coeffs, sh_degree, block_width, (float3*)colors, counts);
+        project_launch<__nv_bfloat16>(sh_degree, N, V, bv, means, scales, glob_scale, quats,
+                                      (const __nv_bfloat16*)sh_coeffs, block_width, colors, counts, stream);
     else
-        batch_project_kernel<float><<<ceil_div(N, 128), 128, 0, stream>>>(
-            N, V, bv, (const float3*)means, scales, glob_scale, (const float4*)quats, (const float*)sh_coeffs,
-            sh_degree, block_width, (float3*)colors, counts);
+        project_launch<float>(sh_degree, N, V, bv, means, scales, glob_scale, quats, (const float*)sh_coeffs,
+                              block_width, colors, counts, stream);
     return check_launch("batch_project");
 }
 
@@ -431,8 +455,18 @@ extern "C" int gstex_batch_sh_backward(int N, int V, const void* views_dev, cons
     GSTEX_REQUIRE(N >= 0 && V > 0 && views_dev && sh_degree >= 0 && sh_degree <= 4);
     if (N == 0) return GSTEX_OK;
     GSTEX_REQUIRE(means && v_colors && v_coeffs);
-    batch_sh_backward_kernel<<<ceil_div(N, 128), 128, 0, (cudaStream_t)s>>>(
-        N, V, (const BatchView*)views_dev, (const float3*)means, sh_degree, (const float4*)v_colors, v_coeffs);
+    const dim3 grid(ceil_div(N, 128)), block(128);
+    const BatchView* bv = (const BatchView*)views_dev;
+    const float3* m = (const float3*)means;
+    const float4* vc = (const float4*)v_colors;
+    cudaStream_t stream = (cudaStream_t)s;
+    switch (sh_degree) {
+        case 0: batch_sh_backward_kernel<0><<<grid, block, 0, stream>>>(N, V, bv, m, vc, v_coeffs); break;
+        case 1: batch_sh_backward_kernel<1><<<grid, block, 0, stream>>>(N, V, bv, m, vc, v_coeffs); break;
+        case 2: batch_sh_backward_kernel<2><<<grid, block, 0, stream>>>(N, V, bv, m, vc, v_coeffs); break;
+        case 3: batch_sh_backward_kernel<3><<<grid, block, 0, stream>>>(N, V, bv, m, vc, v_coeffs); break;
+        default: batch_sh_backward_kernel<4><<<grid, block, 0, stream>>>(N, V, bv, m, vc, v_coeffs); break;
+    }
     return check_launch("batch_sh_backward");
 }
 
