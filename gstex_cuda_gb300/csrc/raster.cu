@@ -815,7 +815,7 @@ __global__ void FWD_BOUNDS(PPT) fwd_view_kernel(SceneArgs a, ViewArgs va, FwdOut
     J.colors = va.colors;
     J.vcolors = nullptr;
     J.vc_stride = 3;
-    J.recs = nullptr;
+    J.recs = va.recs;
     const int nthr = blockDim.x * blockDim.y;
     fwd_tile<TEXMODE, CT, PPT>(a, J, o, Recs::carve(smem, nthr, false));
 }
@@ -833,7 +833,7 @@ __global__ void BWD_BOUNDS(PPT) bwd_view_kernel(SceneArgs a, ViewArgs va, BwdArg
     J.colors = va.colors;
     J.vcolors = va.vcolors;
     J.vc_stride = 3;
-    J.recs = nullptr;
+    J.recs = va.recs;
     uint8_t* lists = smem + (size_t)(kRecBytes + kEdgeBytes + kMomSlot * sizeof(float)) * nthr;
     bwd_tile<TEXMODE, CT, PPT>(a, J, g, Recs::carve(smem, nthr, true),
                                reinterpret_cast<float*>(smem + (size_t)(kRecBytes + kEdgeBytes) * nthr), lists,
@@ -907,6 +907,20 @@ __global__ void records_kernel(SceneArgs a, BatchArgs ba, const int32_t* __restr
     if (defer) fix[atomicAdd(fix_count, 1)] = (uint32_t)j;
 }
 
+// The double solve of one deferred near-edge-on record of Gaussian i.
+__device__ __forceinline__ void fix_record(const SceneArgs& a, const View& V, int i, RecAll* __restrict__ rec) {
+    const Axes A = quat_axes(a.quats[i]);
+    const float3 mc = V.xform(a.means[i]);
+    const float3 a1c = V.rot(A.a1), a2c = V.rot(A.a2), nc = V.rot(A.a3);
+    const float3 umc = V.rot(a.umap[i]), vmc = V.rot(a.vmap[i]);
+    const float is1 = 1.f / (a.scales[3 * i] * a.glob), is2 = 1.f / (a.scales[3 * i + 1] * a.glob);
+    RecHot h = rec->h;
+    RecWarm w = rec->w;
+    edge_on_solve(h, w, V, mc, a1c, a2c, nc, umc, vmc, is1, is2, dot3(nc, mc));
+    rec->h = h;
+    rec->w.uvm = w.uvm;
+}
+
 // The double solve of the deferred near-edge-on records, densely.
 __global__ void records_fixup_kernel(SceneArgs a, BatchArgs ba, const int* __restrict__ fix_count,
                                      const uint32_t* __restrict__ fix, RecAll* __restrict__ recs) {
@@ -915,17 +929,34 @@ __global__ void records_fixup_kernel(SceneArgs a, BatchArgs ba, const int* __res
         const uint32_t j = fix[t];
         const int v = (int)(j / (uint32_t)ba.num_points);
         const int i = (int)(j - (uint32_t)v * (uint32_t)ba.num_points);
-        const View V = ba.views[v].V;
-        const Axes A = quat_axes(a.quats[i]);
-        const float3 mc = V.xform(a.means[i]);
-        const float3 a1c = V.rot(A.a1), a2c = V.rot(A.a2), nc = V.rot(A.a3);
-        const float3 umc = V.rot(a.umap[i]), vmc = V.rot(a.vmap[i]);
-        const float is1 = 1.f / (a.scales[3 * i] * a.glob), is2 = 1.f / (a.scales[3 * i + 1] * a.glob);
-        RecHot h = recs[j].h;
-        RecWarm w = recs[j].w;
-        edge_on_solve(h, w, V, mc, a1c, a2c, nc, umc, vmc, is1, is2, dot3(nc, mc));
-        recs[j].h = h;
-        recs[j].w.uvm = w.uvm;
+        fix_record(a, ba.views[v].V, i, recs + j);
+    }
+}
+
+// Per-view form (texture_forward / texture_backward): the record of every
+// Gaussian of one view, so that any Gaussian a tile names has one.
+__global__ void view_records_kernel(SceneArgs a, ViewArgs va, RecAll* __restrict__ recs, int* __restrict__ fix_count,
+                                    uint32_t* __restrict__ fix) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.N) return;
+    const View V = load_view(va.viewmat, va.fx, va.fy, va.cx, va.cy);
+    RecAll r;
+    const bool defer = make_record(r.h, r.w, r.c, i, V, a.means[i], a.quats[i],
+                                   make_float2(a.scales[3 * i], a.scales[3 * i + 1]), a.glob, a.opac[i], va.colors[i],
+                                   a.uv0[i], a.umap[i], a.vmap[i], a.dims[i], a.settings & (1 << 9), false, &r.e,
+                                   !(a.settings & (1 << 16)));
+    recs[i] = r;
+    if (defer) fix[atomicAdd(fix_count, 1)] = (uint32_t)i;
+}
+
+__global__ void view_records_fixup_kernel(SceneArgs a, ViewArgs va, const int* __restrict__ fix_count,
+                                          const uint32_t* __restrict__ fix, RecAll* __restrict__ recs) {
+    const int n = *fix_count;
+    if (blockIdx.x * blockDim.x >= n) return;
+    const View V = load_view(va.viewmat, va.fx, va.fy, va.cx, va.cy);
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int i = (int)fix[t];
+        fix_record(a, V, i, recs + i);
     }
 }
 
@@ -980,7 +1011,7 @@ static int set_smem(K kernel, size_t smem, const char* what) {
     return GSTEX_OK;
 }
 
-int fill_scene(const gstex_raster_inputs* in, SceneArgs& a) {
+int fill_scene(const gstex_raster_inputs* in, SceneArgs& a, bool need_bins) {
     GSTEX_REQUIRE(in);
     GSTEX_REQUIRE(in->num_points >= 0 && in->img_width > 0 && in->img_height > 0);
     GSTEX_REQUIRE(in->block_width >= 2 && in->block_width <= kMaxBlockWidth);
@@ -988,7 +1019,10 @@ int fill_scene(const gstex_raster_inputs* in, SceneArgs& a) {
     if (in->channels > kMaxChannels) return GSTEX_ERR_UNSUPPORTED;
     if (in->texture_dtype == 1 && in->channels != 3) return GSTEX_ERR_UNSUPPORTED;
     GSTEX_REQUIRE(in->texture_dtype == 0 || in->texture_dtype == 1);
-    GSTEX_REQUIRE(in->tile_bins && in->viewmat && in->background);
+    GSTEX_REQUIRE(in->viewmat && in->background);
+    if (need_bins) GSTEX_REQUIRE(in->tile_bins);
+    // prebuilt records are copied as 16-byte vectors
+    GSTEX_REQUIRE(((uintptr_t)in->records & 15) == 0);
     if (in->num_points > 0)
         GSTEX_REQUIRE(in->texture_dims && in->colors && in->opacities && in->means && in->scales && in->quats &&
                       in->uv0 && in->umap && in->vmap);
@@ -1109,10 +1143,51 @@ int resident_ctas(int bw, bool backward, int texmode, int C, int ppt) {
 
 using namespace gstex;
 
+static ViewArgs view_args(const gstex_raster_inputs* in) {
+    ViewArgs va;
+    va.viewmat = in->viewmat;
+    va.fx = in->fx; va.fy = in->fy; va.cx = in->cx; va.cy = in->cy;
+    va.W = in->img_width; va.H = in->img_height;
+    va.tiles_x = ceil_div(va.W, in->block_width);
+    va.bins = (const int2*)in->tile_bins;
+    va.colors = (const float3*)in->colors;
+    va.vcolors = nullptr;
+    va.recs = (const RecAll*)in->records;
+    return va;
+}
+
+// records [N], then the count and list of deferred near-edge-on records
+static size_t view_records_fix_offset(int n) { return (size_t)n * sizeof(RecAll); }
+
+extern "C" size_t gstex_view_records_bytes(int num_points) {
+    const int n = num_points > 0 ? num_points : 0;
+    return view_records_fix_offset(n) + 16 + (size_t)n * sizeof(uint32_t);
+}
+
+extern "C" int gstex_view_records(const gstex_raster_inputs* in, void* records, size_t records_bytes,
+                                  gstex_stream_t s) {
+    SceneArgs a;
+    int rc = fill_scene(in, a, false);
+    if (rc) return rc;
+    GSTEX_REQUIRE(records && ((uintptr_t)records & 15) == 0);
+    if (records_bytes < gstex_view_records_bytes(a.N)) return GSTEX_ERR_CAPACITY;
+    if (a.N == 0) return GSTEX_OK;
+    ViewArgs va = view_args(in);
+    RecAll* recs = (RecAll*)records;
+    int* fix_count = (int*)((char*)records + view_records_fix_offset(a.N));
+    uint32_t* fix = (uint32_t*)((char*)records + view_records_fix_offset(a.N) + 16);
+    cudaStream_t stream = (cudaStream_t)s;
+    cudaError_t e = cudaMemsetAsync(fix_count, 0, sizeof(int), stream);
+    if (e != cudaSuccess) { set_cuda_error(e, "view_records"); return GSTEX_ERR_CUDA; }
+    view_records_kernel<<<ceil_div(a.N, 128), 128, 0, stream>>>(a, va, recs, fix_count, fix);
+    view_records_fixup_kernel<<<152 * 2, 128, 0, stream>>>(a, va, fix_count, fix, recs);
+    return check_launch("view_records", 2);
+}
+
 extern "C" int gstex_texture_forward(const gstex_raster_inputs* in, const gstex_forward_outputs* out,
                                      gstex_stream_t s) {
     SceneArgs a;
-    int rc = fill_scene(in, a);
+    int rc = fill_scene(in, a, true);
     if (rc) return rc;
     GSTEX_REQUIRE(out && out->img && out->depth && out->reg && out->normal && out->final_T && out->final_idx &&
                   out->depth_idx && out->reg_s);
@@ -1120,14 +1195,7 @@ extern "C" int gstex_texture_forward(const gstex_raster_inputs* in, const gstex_
     FwdOut o{ (float3*)out->img, out->depth, out->reg, out->texture, (float3*)out->normal, out->final_T,
               out->final_idx, out->depth_idx, (float3*)out->reg_s };
     const int bw = in->block_width;
-    ViewArgs va;
-    va.viewmat = in->viewmat;
-    va.fx = in->fx; va.fy = in->fy; va.cx = in->cx; va.cy = in->cy;
-    va.W = in->img_width; va.H = in->img_height;
-    va.tiles_x = ceil_div(va.W, bw);
-    va.bins = (const int2*)in->tile_bins;
-    va.colors = (const float3*)in->colors;
-    va.vcolors = nullptr;
+    ViewArgs va = view_args(in);
     cudaStream_t stream = (cudaStream_t)s;
     const dim3 grid(va.tiles_x, ceil_div(va.H, bw));
     int ppt = ppt_of(bw, in->pixels_per_thread);
@@ -1192,7 +1260,7 @@ extern "C" size_t gstex_backward_workspace_bytes(int num_points) {
 
 extern "C" int gstex_texture_backward(const gstex_raster_inputs* in, const gstex_backward_io* io, gstex_stream_t s) {
     SceneArgs a;
-    int rc = fill_scene(in, a);
+    int rc = fill_scene(in, a, true);
     if (rc) return rc;
     // alpha-visualisation mode is a forward-only view: its alpha has no adjoint
     if (in->settings & (1 << 16)) return GSTEX_ERR_UNSUPPORTED;
@@ -1211,13 +1279,7 @@ extern "C" int gstex_texture_backward(const gstex_raster_inputs* in, const gstex
                io->v_depth, io->v_reg, io->v_alpha, io->v_texture, (const float3*)io->v_normal,
                (float*)io->workspace, io->v_tex_grad };
     const int bw = in->block_width;
-    ViewArgs va;
-    va.viewmat = in->viewmat;
-    va.fx = in->fx; va.fy = in->fy; va.cx = in->cx; va.cy = in->cy;
-    va.W = in->img_width; va.H = in->img_height;
-    va.tiles_x = ceil_div(va.W, bw);
-    va.bins = (const int2*)in->tile_bins;
-    va.colors = (const float3*)in->colors;
+    ViewArgs va = view_args(in);
     va.vcolors = io->v_colors;
     const dim3 grid(va.tiles_x, ceil_div(va.H, bw));
     const int ppt = ppt_of(bw, in->pixels_per_thread);

@@ -35,6 +35,7 @@ struct ViewArgs {
     const int2* bins;
     const float3* colors;
     float* vcolors;       // [N,3] colour gradients (backward)
+    const RecAll* recs;   // optional [N] prebuilt records of the view; null: built per tile
 };
 
 // Per-view constants of a batched launch (device array).
@@ -98,7 +99,7 @@ struct BwdArgs {
     float* v_texgrad;       // [T, C] (fp32 texture) or [T, 4] (bf16 texture)
 };
 
-int fill_scene(const gstex_raster_inputs* in, SceneArgs& a);
+int fill_scene(const gstex_raster_inputs* in, SceneArgs& a, bool need_bins);
 int ppt_of(int bw, int requested);
 size_t fwd_smem(int bw, int ppt);
 size_t bwd_smem(int bw, int ppt);

@@ -180,6 +180,10 @@ def _texture_mode(texture, channels):
 
 
 PIXELS_PER_THREAD = 1  # 1 or 2 (2 halves the threads per tile; even block widths only)
+# texture_forward / texture_backward build one splat record per Gaussian of the
+# view first (gstex_view_records) and the tiles copy them; False: every tile
+# derives the records of its Gaussians itself.
+PREBUILT_RECORDS = True
 
 
 def _raster_inputs(img_w, img_h, bw, texture_info, texture_dims, gaussian_ids_sorted, tile_bins, colors, opacities,
@@ -217,6 +221,20 @@ def _raster_inputs(img_w, img_h, bw, texture_info, texture_dims, gaussian_ids_so
     return ri, C
 
 
+def _attach_records(ri, device):
+    """Builds the view's splat records into a fresh buffer and points `ri` at
+    it; returns the buffer (kept alive by the caller until the launch is
+    queued)."""
+    if not PREBUILT_RECORDS or ri.num_points == 0:
+        return None
+    L = _lib.lib()
+    nb = L.gstex_view_records_bytes(ri.num_points)
+    buf = torch.empty(nb, dtype=torch.uint8, device=device)
+    check(L.gstex_view_records(ctypes.byref(ri), ptr(buf), nb, _lib.stream_of(buf)), "view_records")
+    ri.records = ptr(buf)
+    return buf
+
+
 def texture_forward(tile_bounds, block, img_size, texture_info, texture_dims, gaussian_ids_sorted, tile_bins,
                     colors, opacities, means, scales, glob_scale, quats, uv0, umap, vmap, texture, viewmat, c2w, fx,
                     fy, cx, cy, settings, background):
@@ -242,6 +260,7 @@ def texture_forward(tile_bounds, block, img_size, texture_info, texture_dims, ga
     reg_s = torch.empty((H, W, 3), **f32)
     fo = _lib.ForwardOutputs(ptr(out_img), ptr(out_depth), ptr(out_reg), ptr(out_tex), ptr(out_normal), ptr(final_T),
                              ptr(final_idx), ptr(depth_idx), ptr(reg_s))
+    recs = _attach_records(ri, dev)  # noqa: F841 (alive until the launch is queued)
     check(_lib.lib().gstex_texture_forward(ctypes.byref(ri), ctypes.byref(fo), _lib.stream_of(means)),
           "texture_forward")
     return out_img, out_depth, out_reg, out_tex, out_normal, final_T, final_idx, depth_idx, reg_s
@@ -279,6 +298,7 @@ def texture_backward(img_height, img_width, block_width, texture_info, texture_d
                           ptr(v_output_depth), ptr(v_output_reg), ptr(v_output_alpha), ptr(v_output_texture),
                           ptr(v_output_normal), ptr(v_colors), ptr(v_opacity), ptr(v_means), ptr(v_scales),
                           ptr(v_quats), ptr(v_uv0), ptr(v_umap), ptr(v_vmap), ptr(v_texture), ptr(ws), wsb)
+    recs = _attach_records(ri, dev)  # noqa: F841 (alive until the launch is queued)
     check(L.gstex_texture_backward(ctypes.byref(ri), ctypes.byref(bio), _lib.stream_of(means)), "texture_backward")
     return v_colors, v_opacity, v_means, v_scales, v_quats, v_uv0, v_umap, v_vmap, v_texture
 

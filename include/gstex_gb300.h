@@ -160,7 +160,23 @@ typedef struct gstex_raster_inputs {
     int settings;                       /* reference settings bitfield */
     const float* background;            /* [3] device */
     int pixels_per_thread;              /* 0 = default (1); 2 needs an even block width */
+    /* Optional splat records of this view built by gstex_view_records from
+     * the same inputs (16-byte aligned); NULL: every tile derives the records
+     * of its Gaussians itself.  Read by texture_forward / texture_backward,
+     * not by texture_edit. */
+    const void* records;
 } gstex_raster_inputs;
+
+/* Bytes of the records buffer of one view: 224 per Gaussian plus the list
+ * of near-edge-on records solved in double precision. */
+size_t gstex_view_records_bytes(int num_points);
+/* One camera-space splat record per Gaussian of the view (all N, whatever
+ * the binning), from the scene, camera, colours and settings of `in`
+ * (tile_bins and gaussian_ids_sorted are not read).  Two launches; the
+ * texture_forward / texture_backward calls that pass them copy a record per
+ * (tile, Gaussian) instead of recomputing it.  No counterpart in the
+ * reference, whose kernels derive the same per pixel (csrc/texture.cu:160-181). */
+int gstex_view_records(const gstex_raster_inputs* in, void* records, size_t records_bytes, gstex_stream_t stream);
 
 typedef struct gstex_forward_outputs {
     float* img;        /* [H,W,3] */

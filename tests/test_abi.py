@@ -40,6 +40,9 @@ def test_status_strings_and_workspace_queries():
     assert L.gstex_sort_workspace_bytes(1000) >= 1000 * 12
     assert L.gstex_backward_workspace_bytes(10) >= 10 * 24 * 4
     assert L.gstex_scan_workspace_bytes(1) > 0
+    # 224-byte record per Gaussian, then the deferred-record count and list
+    assert L.gstex_view_records_bytes(1000) == 1000 * 224 + 16 + 1000 * 4
+    assert L.gstex_view_records_bytes(0) == 16
 
 
 def test_invalid_arguments_rejected_without_gpu():
@@ -60,6 +63,14 @@ def test_invalid_arguments_rejected_without_gpu():
     eio = _lib.EditIO()
     ri.block_width = 16
     assert L.gstex_texture_edit(ctypes.byref(ri), ctypes.byref(eio), None) == 3
+    # records: a buffer that is too small, and a misaligned one, are refused
+    ri.channels = 3
+    ri.colors = ri.opacities = ri.means = ri.scales = ri.quats = ri.uv0 = ri.umap = ri.vmap = 16
+    ri.texture = ri.texture_dims = 16
+    assert L.gstex_view_records(ctypes.byref(ri), 16, L.gstex_view_records_bytes(1) - 1, None) == 2
+    assert L.gstex_view_records(ctypes.byref(ri), 8, L.gstex_view_records_bytes(1), None) == 1
+    ri.records = 8
+    assert L.gstex_texture_forward(ctypes.byref(ri), ctypes.byref(fo), None) == 1
 
 
 def test_cpu_tensors_fail_loudly():

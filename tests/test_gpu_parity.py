@@ -228,6 +228,37 @@ def test_raster_small_matches_oracle(w, h, bw, pixels_per_thread):
     _compare_backward(case, b, out, bgt, ref, bw, 1 << 8, bg, 5e-4)
 
 
+@pytest.mark.parametrize("settings", [1 << 8, (1 << 8) | (1 << 9), (1 << 8) | (1 << 10)])
+def test_view_records_match_per_tile_records(settings):
+    """texture_forward / texture_backward with the view's splat records built
+    once (gstex_view_records, the default) and with every tile deriving the
+    records of its Gaussians: both against the oracle, and the same outputs
+    and gradients up to float rounding (threshold flips against the fp64
+    oracle allowed at the rate of the other parity tests)."""
+    import gstex_cuda_gb300.cuda as CU
+    case = Case(small_scene(n=400, width=80, height=64, seed=41))
+    bg = np.array([0.3, 0.2, 0.1])
+    ups = upstream(case.cam.height, case.cam.width, case.spec.texture.shape[1])
+    old = CU.PREBUILT_RECORDS
+    res = {}
+    try:
+        for pre in (True, False):
+            CU.PREBUILT_RECORDS = pre
+            b, out, bgt, ref = _compare_forward(case, 16, settings, bg, 5e-5, frac=1e-3)
+            _compare_backward(case, b, out, bgt, ref, 16, settings, bg, 5e-4)
+            g = case.backward_cuda(out, b["gaussian_ids_sorted"], b["tile_bins"], ups, 16, settings, bgt)
+            res[pre] = (out, g)
+    finally:
+        CU.PREBUILT_RECORDS = old
+    (o1, g1), (o2, g2) = res[True], res[False]
+    for k in ("img", "texture", "normal", "final_T", "reg"):
+        _close(np_(o1[k]), np_(o2[k]), 1e-5, 1e-3, k)
+    assert (np_(o1["final_idx"]) == np_(o2["final_idx"])).mean() > 0.999
+    for k in ("colors", "opacity", "means", "scales", "quats", "uv0", "umap", "vmap", "texture"):
+        a, r = np_(g1[k]), np_(g2[k])
+        assert np.abs(a - r).max() <= 1e-4 * (np.abs(r).max() + 1e-12), k
+
+
 @pytest.mark.parametrize("C", [0, 1, 5])
 def test_raster_generic_channels(C):
     case = Case(small_scene(n=120, width=40, height=40, seed=C, channels=max(C, 1)))
