@@ -7,10 +7,10 @@
 // with a handful of FMAs instead of the reference's per-pixel quaternion,
 // ray-plane and projection work.
 //
-// Backward: per (pixel, Gaussian) the adjoint reduces to 26 scalar moments
+// Backward: per (pixel, Gaussian) the adjoint reduces to 23 scalar moments
 // whose sums over pixels determine every parameter gradient (on the splat
 // plane delta = l1*ax1 + l2*ax2, and the quaternion adjoint is linear in dR).
-// Moments are reduced across a warp with a 31-shuffle transpose reduction,
+// Moments are reduced across a warp with a 24-shuffle transpose reduction,
 // summed per CTA in shared memory, and flushed with one set of vector atomics
 // per (tile, Gaussian).  A finalize kernel turns the per-Gaussian sums into
 // v_means, v_quats, ...
@@ -351,20 +351,40 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
 // ---------------------------------------------------------------------------
 // Backward body: one tile
 // ---------------------------------------------------------------------------
-// Transpose reduction: lane l ends with the warp sum of m[l].
-__device__ __forceinline__ float warp_transpose_reduce(float (&m)[32], unsigned lane) {
+// Transpose reduction of N values per lane over the lanes that differ in bits
+// OFF, OFF/2, ..., 1: at each level a lane keeps the lower or the upper half
+// of its values (H = ceil(N/2) of them) and receives its partner's copy of
+// that half, one shuffle per kept value (N - 1 + log2 32 shuffles in all for
+// N <= 32).  Afterwards every lane holds one sum; slot() names the value
+// index it belongs to (N when the lane holds padding).
+template <int N, int OFF>
+struct Ragged {
+    static constexpr int H = (N + 1) / 2;
+    static __device__ __forceinline__ void reduce(float* m, unsigned lane) {
+        const bool upper = lane & OFF;
 #pragma unroll
-    for (int off = 16; off >= 1; off >>= 1) {
-        const bool upper = lane & off;
-#pragma unroll
-        for (int j = 0; j < off; j++) {
-            const float send = upper ? m[j] : m[j + off];
-            const float keep = upper ? m[j + off] : m[j];
-            m[j] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+        for (int j = 0; j < H; j++) {
+            const float lo = m[j];
+            const float hi = j + H < N ? m[j + H] : 0.f;
+            const float send = upper ? lo : hi;
+            const float keep = upper ? hi : lo;
+            m[j] = keep + __shfl_xor_sync(0xffffffffu, send, OFF);
         }
+        Ragged<H, OFF / 2>::reduce(m, lane);
     }
-    return m[0];
-}
+    static __device__ __forceinline__ int slot(unsigned lane) {
+        const int inner = Ragged<H, OFF / 2>::slot(lane);
+        if (inner >= H) return N;
+        const int idx = ((lane & OFF) ? H : 0) + inner;
+        return idx < N ? idx : N;
+    }
+};
+template <int N>
+struct Ragged<N, 0> {
+    static_assert(N == 1, "five levels reduce at most 32 values to one");
+    static __device__ __forceinline__ void reduce(float*, unsigned) {}
+    static __device__ __forceinline__ int slot(unsigned) { return 0; }
+};
 
 template <typename T>
 __device__ __forceinline__ T ld_or(const T* p, size_t i, T z) {
@@ -389,7 +409,7 @@ template <int TEXMODE, int CT, int CA>
 __device__ __forceinline__ void bwd_pair(const SceneArgs& a, const BwdArgs& g, const Recs& R, int k, int gidx,
                                          const RecHot& Hr, const Hit& H, float alpha, float e, float eb, float nbf,
                                          float bf, BwdPix<CA>& S, int C, bool use_ndc, bool prop_uv, bool bilinear,
-                                         float (&m)[32]) {
+                                         float (&m)[kMoments]) {
     const RecWarm& Wm = R.warm[k];
     const float4 col = Wm.col, nw = Wm.nrm;
     const float is1 = col.w, is2 = nw.w;
@@ -476,16 +496,16 @@ __device__ __forceinline__ void bwd_pair(const SceneArgs& a, const BwdArgs& g, c
     vT_cur += v_w * alpha;
     S.vT_run = vT_cur;
     const float v_sigma = -nbf * Hr.d.z * e * v_alpha;
-    // sigma = (l1s^2 + l2s^2) / 2 with l_ks = l_k * is_k
+    // sigma = (l1s^2 + l2s^2) / 2 with l_ks = l_k * is_k, so v_lk = is_k l_ks v_sigma;
+    // the per-Gaussian factors is_k, 1 / is_k and glob are applied at the flush
+    const float p1 = H.l1s * v_sigma, p2 = H.l2s * v_sigma;
     const float l1 = __fdividef(H.l1s, is1), l2 = __fdividef(H.l2s, is2);
-    const float v_l1 = H.l1s * is1 * v_sigma;
-    const float v_l2 = H.l2s * is2 * v_sigma;
     // ray . axis from the hit: l = a . (t r - mu) gives a . r = (l + a . mu) / t
     const RecCold& Cd = R.cold[k];
     const float it = __fdividef(1.f, H.t);
     const float ra1 = (l1 + Cd.mu.w) * it;
     const float ra2 = (l2 + Cd.dt.x) * it;
-    v_t += v_l1 * ra1 + v_l2 * ra2;
+    v_t += is1 * p1 * ra1 + is2 * p2 * ra2;
     if (prop_uv) {
         const float2 uvr = hit_uv(H, Wm);
         const float rum = (uvr.x - Wm.uvs.x + Cd.dt.y) * it;
@@ -502,28 +522,25 @@ __device__ __forceinline__ void bwd_pair(const SceneArgs& a, const BwdArgs& g, c
     m[1] += vis * vout.y;
     m[2] += vis * vout.z;
     m[3] += (nbf * e + bf * eb) * v_alpha;
-    m[4] += -(H.l1s * H.l1s) * v_sigma * is1 * a.glob;
-    m[5] += -(H.l2s * H.l2s) * v_sigma * is2 * a.glob;
-    m[6] += v_l1;
-    m[7] += v_l2;
-    m[8] += vtd;
-    m[9] += l1 * v_l1;
-    m[10] += l2 * v_l1;
-    m[11] += l1 * v_l2;
-    m[12] += l2 * v_l2;
-    m[13] += l1 * vtd;
-    m[14] += l2 * vtd;
-    m[15] += vis * vnorm.x;
-    m[16] += vis * vnorm.y;
-    m[17] += vis * vnorm.z;
-    m[18] += v_u;
-    m[19] += v_v;
-    m[20] += l1 * v_u;
-    m[21] += l2 * v_u;
-    m[22] += l1 * v_v;
-    m[23] += l2 * v_v;
-    m[24] += kBlurFsq * v_sb * (Wm.uvs.z - P.px);
-    m[25] += kBlurFsq * v_sb * (Wm.uvs.w - P.py);
+    m[4] += H.l1s * p1;  // = l1 v_l1;  v_scale1 = -is1 glob m4
+    m[5] += H.l2s * p2;  // = l2 v_l2
+    m[6] += H.l1s * p2;  // l2 v_l1 = (is1 / is2) m6, l1 v_l2 = (is2 / is1) m6
+    m[7] += p1;          // v_l1 / is1
+    m[8] += p2;
+    m[9] += vtd;
+    m[10] += H.l1s * vtd;  // l1 vtd is1
+    m[11] += H.l2s * vtd;
+    m[12] += vis * vnorm.x;
+    m[13] += vis * vnorm.y;
+    m[14] += vis * vnorm.z;
+    m[15] += v_u;
+    m[16] += v_v;
+    m[17] += H.l1s * v_u;  // l1 v_u is1
+    m[18] += H.l2s * v_u;
+    m[19] += H.l1s * v_v;
+    m[20] += H.l2s * v_v;
+    m[21] += kBlurFsq * v_sb * (Wm.uvs.z - P.px);
+    m[22] += kBlurFsq * v_sb * (Wm.uvs.w - P.py);
 }
 
 template <int TEXMODE, int CT, int PPT>
@@ -536,6 +553,7 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
     const unsigned wmask = __activemask();
     uint8_t* wl = lists + (tr >> 5) * nthr;
     const bool full_warp = wmask == 0xffffffffu;
+    const int my_slot = Ragged<kMoments, 16>::slot(lane);
     const View& V = J.V;
     const bool use_blur = a.settings & (1 << 9);
     const bool use_ndc = a.settings & (1 << 10);
@@ -631,9 +649,9 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
             }
             const unsigned vmask = __ballot_sync(wmask, any);
             if (!vmask) continue;
-            float m[32];
+            float m[kMoments];
 #pragma unroll
-            for (int q = 0; q < 32; q++) m[q] = 0.f;
+            for (int q = 0; q < kMoments; q++) m[q] = 0.f;
 #pragma unroll
             for (int p = 0; p < PPT; p++)
                 if (valid[p])
@@ -642,8 +660,8 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
             float* dst = smom + k * kMomSlot;
             if (lane == 0) touched[k] = 1;
             if (full_warp) {
-                const float s = warp_transpose_reduce(m, lane);
-                if (lane < (unsigned)kMoments) atomicAdd(dst + lane, s);
+                Ragged<kMoments, 16>::reduce(m, lane);
+                if (my_slot < kMoments) atomicAdd(dst + my_slot, m[0]);
             } else if (any) {
 #pragma unroll
                 for (int q = 0; q < kMoments; q++) atomicAdd(dst + q, m[q]);
@@ -671,11 +689,30 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
                 // blur moments -> world-space mean gradient (helpers.cuh:155-164, 114-121)
                 const float3 p = f3(R.cold[tr].mu);
                 const float rw = 1.f / (p.z + 1e-6f);
-                const float vx = V.fx * sm[24], vy = V.fy * sm[25];
+                const float vx = V.fx * sm[21], vy = V.fy * sm[22];
                 const float3 vmb = V.rot_t(make_float3(vx * rw, vy * rw, -(vx * p.x + vy * p.y) * rw * rw));
+                // the per-Gaussian factors left out of the pixel sums
+                const float is1 = R.warm[tr].col.w, is2 = R.warm[tr].nrm.w;
+                const float r1 = 1.f / is1, r2 = 1.f / is2;
                 float v[kMomStride];
-#pragma unroll
-                for (int q = 0; q < 21; q++) v[q] = sm[3 + q];
+                v[0] = sm[3];
+                v[1] = -is1 * a.glob * sm[4];
+                v[2] = -is2 * a.glob * sm[5];
+                v[3] = is1 * sm[7];
+                v[4] = is2 * sm[8];
+                v[5] = sm[9];
+                v[6] = sm[4];
+                v[7] = is1 * r2 * sm[6];
+                v[8] = is2 * r1 * sm[6];
+                v[9] = sm[5];
+                v[10] = r1 * sm[10];
+                v[11] = r2 * sm[11];
+                v[12] = sm[12]; v[13] = sm[13]; v[14] = sm[14];
+                v[15] = sm[15]; v[16] = sm[16];
+                v[17] = r1 * sm[17];
+                v[18] = r2 * sm[18];
+                v[19] = r1 * sm[19];
+                v[20] = r2 * sm[20];
                 v[21] = vmb.x; v[22] = vmb.y; v[23] = vmb.z;
 #pragma unroll
                 for (int q = 0; q < kMomStride / 4; q++)

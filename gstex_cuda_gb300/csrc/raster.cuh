@@ -5,8 +5,8 @@
 
 namespace gstex {
 
-constexpr int kMoments = 26;    // per-pair moments reduced inside a CTA
-constexpr int kMomSlot = 28;    // shared-memory slot stride: 7 float4, conflict-free row reads
+constexpr int kMoments = 23;    // per-pair moments reduced inside a CTA
+constexpr int kMomSlot = 24;    // shared-memory slot stride: 6 float4
 constexpr int kMomStride = 24;  // per-Gaussian global moments (colour gradients live elsewhere)
 
 // View-independent scene inputs.
