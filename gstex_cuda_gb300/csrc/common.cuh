@@ -128,10 +128,10 @@ __device__ __forceinline__ View load_view(const float* viewmat, float fx, float 
 // Fields are grouped by how often the per-pixel loop reads them.
 // ---------------------------------------------------------------------------
 struct RecHot {   // every (pixel, Gaussian) pair
-    float4 a;     // px0, py0, g, tvn
-    float4 b;     // nu, nv, box x0, box x1
-    float4 c;     // p1u, p1v, p2u, p2v (scaled by 1 / (scale * glob_scale))
-    float4 d;     // box y0, box y1, opacity, flags (int bits; bit 0: direct form only)
+    float4 box;   // screen box of alpha >= 1/255: x0, x1, y0, y1 (one load for the per-visit test)
+    float4 org;   // px0, py0, g, tvn
+    float4 lc;    // p1u, p1v, p2u, p2v (scaled by 1 / (scale * glob_scale))
+    float4 nop;   // nu, nv, opacity, flags (int bits; bit 0: direct form only)
 };
 struct RecWarm {  // pairs that pass the alpha test
     float4 uvm;   // uu, uv_, vu, vv: texture uv numerators
@@ -186,7 +186,7 @@ __device__ __forceinline__ float4 f4(float3 v, float w) { return make_float4(v.x
 __device__ __forceinline__ float3 f3(float4 v) { return make_float3(v.x, v.y, v.z); }
 
 // Near-edge-on splats (|n_c . d0| < kEdgeOn): the plane coefficients in
-// double.  Writes H.a, H.b.x/.y, H.c and Wm.uvm.
+// double.  Writes H.org, H.nop.x/.y, H.lc and Wm.uvm.
 constexpr float kEdgeOn = 0.05f;
 __device__ __forceinline__ void edge_on_solve(RecHot& H, RecWarm& Wm, const View& V, float3 mc, float3 a1c,
                                               float3 a2c, float3 nc, float3 umc, float3 vmc, float is1, float is2,
@@ -197,10 +197,10 @@ __device__ __forceinline__ void edge_on_solve(RecHot& H, RecWarm& Wm, const View
     const double ifx = 1.0 / V.fx, ify = 1.0 / V.fy;
     const double a1d = a1c.x * u0 + a1c.y * v0 + a1c.z, a2d = a2c.x * u0 + a2c.y * v0 + a2c.z;
     const double umd = umc.x * u0 + umc.y * v0 + umc.z, vmd = vmc.x * u0 + vmc.y * v0 + vmc.z;
-    H.a = make_float4((float)(V.fx * u0 + V.cx), (float)(V.fy * v0 + V.cy), (float)g, tvn);
-    H.b.x = (float)(nc.x * ifx);
-    H.b.y = (float)(nc.y * ify);
-    H.c = make_float4((float)(mz * (g * a1c.x - a1d * nc.x) * ifx * is1),
+    H.org = make_float4((float)(V.fx * u0 + V.cx), (float)(V.fy * v0 + V.cy), (float)g, tvn);
+    H.nop.x = (float)(nc.x * ifx);
+    H.nop.y = (float)(nc.y * ify);
+    H.lc = make_float4((float)(mz * (g * a1c.x - a1d * nc.x) * ifx * is1),
                       (float)(mz * (g * a1c.y - a1d * nc.y) * ify * is1),
                       (float)(mz * (g * a2c.x - a2d * nc.x) * ifx * is2),
                       (float)(mz * (g * a2c.y - a2d * nc.y) * ify * is2));
@@ -329,16 +329,14 @@ __device__ __forceinline__ bool make_record(RecHot& H, RecWarm& Wm, RecCold& Cd,
         }
     }
 
+    H.box = make_float4(x0, x1, y0, y1);
     if (flags) {
-        H.a = make_float4(V.cx, V.cy, 0.f, tvn);
-        H.b = make_float4(0.f, 0.f, x0, x1);
-        H.c = make_float4(0.f, 0.f, 0.f, 0.f);
-        H.d = make_float4(y0, y1, opac, __int_as_float(flags));
+        H.org = make_float4(V.cx, V.cy, 0.f, tvn);
+        H.lc = make_float4(0.f, 0.f, 0.f, 0.f);
+        H.nop = make_float4(0.f, 0.f, opac, __int_as_float(flags));
         Wm.uvm = make_float4(0.f, 0.f, 0.f, 0.f);
         return false;
     }
-    H.b.z = x0;
-    H.b.w = x1;
     const float u0f = mc.x / mc.z, v0f = mc.y / mc.z;
     const float gf = nc.x * u0f + nc.y * v0f + nc.z;
     const bool edge_on = fabsf(gf) < kEdgeOn;
@@ -348,15 +346,16 @@ __device__ __forceinline__ bool make_record(RecHot& H, RecWarm& Wm, RecCold& Cd,
         const float mz = mc.z, ifx = 1.f / V.fx, ify = 1.f / V.fy;
         const float a1d = a1c.x * u0f + a1c.y * v0f + a1c.z, a2d = a2c.x * u0f + a2c.y * v0f + a2c.z;
         const float umd = umc.x * u0f + umc.y * v0f + umc.z, vmd = vmc.x * u0f + vmc.y * v0f + vmc.z;
-        H.a = make_float4(V.fx * u0f + V.cx, V.fy * v0f + V.cy, gf, tvn);
-        H.b.x = nc.x * ifx;
-        H.b.y = nc.y * ify;
-        H.c = make_float4(mz * (gf * a1c.x - a1d * nc.x) * ifx * is1, mz * (gf * a1c.y - a1d * nc.y) * ify * is1,
+        H.org = make_float4(V.fx * u0f + V.cx, V.fy * v0f + V.cy, gf, tvn);
+        H.nop.x = nc.x * ifx;
+        H.nop.y = nc.y * ify;
+        H.lc = make_float4(mz * (gf * a1c.x - a1d * nc.x) * ifx * is1, mz * (gf * a1c.y - a1d * nc.y) * ify * is1,
                           mz * (gf * a2c.x - a2d * nc.x) * ifx * is2, mz * (gf * a2c.y - a2d * nc.y) * ify * is2);
         Wm.uvm = make_float4(mz * (gf * umc.x - umd * nc.x) * ifx, mz * (gf * umc.y - umd * nc.y) * ify,
                              mz * (gf * vmc.x - vmd * nc.x) * ifx, mz * (gf * vmc.y - vmd * nc.y) * ify);
     }
-    H.d = make_float4(y0, y1, opac, __int_as_float(flags));
+    H.nop.z = opac;
+    H.nop.w = __int_as_float(flags);
     return edge_on && !allow_double;
 }
 
@@ -380,7 +379,7 @@ __device__ __forceinline__ PixelRay make_pixel(const View& V, int i, int j) {
 }
 
 __device__ __forceinline__ bool outside_box(const RecHot& H, const PixelRay& P) {
-    return P.px < H.b.z || P.px > H.b.w || P.py < H.d.x || P.py > H.d.y;
+    return P.px < H.box.x || P.px > H.box.y || P.py < H.box.z || P.py > H.box.w;
 }
 
 // Intersection of a pixel ray with a staged splat.
@@ -405,17 +404,17 @@ __device__ __forceinline__ float clamp_denom(float d) {
 // direct form (computed by the caller from the Gaussian's parameters).
 __device__ __forceinline__ Hit intersect(const RecHot& Hr, const PixelRay& P) {
     Hit H;
-    H.du = P.px - Hr.a.x;
-    H.dv = P.py - Hr.a.y;
-    const float den = Hr.a.z + Hr.b.x * H.du + Hr.b.y * H.dv;
+    H.du = P.px - Hr.org.x;
+    H.dv = P.py - Hr.org.y;
+    const float den = Hr.org.z + Hr.nop.x * H.du + Hr.nop.y * H.dv;
     H.nd = den;
-    H.direct = __float_as_int(Hr.d.w) != 0 || !(fabsf(den) >= kDenomEps * P.dn);
+    H.direct = __float_as_int(Hr.nop.w) != 0 || !(fabsf(den) >= kDenomEps * P.dn);
     const float inv = __fdividef(1.f, den);
     H.inv = inv;
-    H.tcam = Hr.a.w * inv;
+    H.tcam = Hr.org.w * inv;
     H.t = H.tcam * P.dn;
-    H.l1s = (Hr.c.x * H.du + Hr.c.y * H.dv) * inv;
-    H.l2s = (Hr.c.z * H.du + Hr.c.w * H.dv) * inv;
+    H.l1s = (Hr.lc.x * H.du + Hr.lc.y * H.dv) * inv;
+    H.l2s = (Hr.lc.z * H.du + Hr.lc.w * H.dv) * inv;
     return H;
 }
 

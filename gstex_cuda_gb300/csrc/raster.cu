@@ -80,7 +80,7 @@ __device__ __forceinline__ Hit hit_pixel(const RecHot& Hr, const Recs& R, int k,
                                          const PixelRay& P) {
     Hit H = intersect(Hr, P);
     if (H.direct)
-        direct_hit(H, a.quats, a.means, a.scales, a.glob, a.uv0, a.umap, a.vmap, V, R.warm[k].tex.w, P, Hr.a.w);
+        direct_hit(H, a.quats, a.means, a.scales, a.glob, a.uv0, a.umap, a.vmap, V, R.warm[k].tex.w, P, Hr.org.w);
     return H;
 }
 
@@ -160,8 +160,8 @@ __device__ __forceinline__ int build_list(uint8_t* wl, const Recs& R, int k0, in
         const int kk = base + (int)lane;
         bool hit = false;
         if (kk < bsize) {
-            const float4 hb = R.hot[kk].b, hd = R.hot[kk].d;
-            hit = !(hb.w < rx0 || hb.z > rx1 || hd.y < ry0 || hd.x > ry1);
+            const float4 bx = R.hot[kk].box;
+            hit = !(bx.y < rx0 || bx.x > rx1 || bx.w < ry0 || bx.z > ry1);
             if (hit && R.edge) {
                 // separating axes of the splat's quad: the rectangle's corner
                 // furthest inside each edge must be inside it
@@ -247,11 +247,11 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
         if (__all_sync(wmask, all_done)) continue;
         // Every staged slot in order; each pixel tests the splat's box first.
         for (int k = 0; k < bsize; ++k) {
-            const float4 hb = R.hot[k].b, hd = R.hot[k].d;
+            const float4 bx = R.hot[k].box;
             bool need = false;
 #pragma unroll
             for (int p = 0; p < PPT; p++) {
-                const bool out_box = P[p].px < hb.z || P[p].px > hb.w || P[p].py < hd.x || P[p].py > hd.y;
+                const bool out_box = P[p].px < bx.x || P[p].px > bx.y || P[p].py < bx.z || P[p].py > bx.w;
                 need = need || (!done[p] && !(out_box && T[p] > 1.01e-4f));
             }
             if (need) {
@@ -269,11 +269,11 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
                     sigma_blur = 0.5f * kBlurFsq * (dx * dx + dy * dy);
                     if (sigma_blur < sigma) { bf = 1.f; nbf = 0.f; }
                 }
-                float alpha = fminf(kAlphaMax, Hr.d.z * (nbf * __expf(-sigma) + bf * __expf(-sigma_blur)));
+                float alpha = fminf(kAlphaMax, Hr.nop.z * (nbf * __expf(-sigma) + bf * __expf(-sigma_blur)));
                 float pixel_dis = 1000.f;
                 if (alpha_vis) {
                     alpha = sigma > vis_sth ? 0.f : kAlphaMax;
-                    if (accept_opac && Hr.d.z < 0.5f) alpha = 0.f;
+                    if (accept_opac && Hr.nop.z < 0.5f) alpha = 0.f;
                     pixel_dis = local_outline(Hr, R, k, a, V, J, P[p], vis_sth);
                 }
                 const bool skip = H.t < kTNear || H.t > kTFar || alpha < kAlphaMin;
@@ -495,7 +495,7 @@ __device__ __forceinline__ void bwd_pair(const SceneArgs& a, const BwdArgs& g, c
     v_alpha += v_w * T;
     vT_cur += v_w * alpha;
     S.vT_run = vT_cur;
-    const float v_sigma = -nbf * Hr.d.z * e * v_alpha;
+    const float v_sigma = -nbf * Hr.nop.z * e * v_alpha;
     // sigma = (l1s^2 + l2s^2) / 2 with l_ks = l_k * is_k, so v_lk = is_k l_ks v_sigma;
     // the per-Gaussian factors is_k, 1 / is_k and glob are applied at the flush
     const float p1 = H.l1s * v_sigma, p2 = H.l2s * v_sigma;
@@ -517,7 +517,7 @@ __device__ __forceinline__ void bwd_pair(const SceneArgs& a, const BwdArgs& g, c
     if (use_ndc) v_t_view += (kTFar * kTNear) / ((kTFar - kTNear) * t_view * t_view) * v_t_ndc;
     v_t += P.idn * v_t_view;
     const float vtd = v_t * (P.dn * H.inv);  // v_t / (n . r)
-    const float v_sb = -bf * Hr.d.z * eb * v_alpha;
+    const float v_sb = -bf * Hr.nop.z * eb * v_alpha;
     m[0] += vis * vout.x;
     m[1] += vis * vout.y;
     m[2] += vis * vout.z;
@@ -612,12 +612,12 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
             const int k = wl[j];
             const int gidx = bend - k;
             {
-                const float4 hb = R.hot[k].b, hd = R.hot[k].d;
+                const float4 bx = R.hot[k].box;
                 bool need = false;
 #pragma unroll
                 for (int p = 0; p < PPT; p++)
                     need = need || (S[p].inside && gidx <= S[p].bfin &&
-                                    !(S[p].P.px < hb.z || S[p].P.px > hb.w || S[p].P.py < hd.x || S[p].P.py > hd.y));
+                                    !(S[p].P.px < bx.x || S[p].P.px > bx.y || S[p].P.py < bx.z || S[p].P.py > bx.w));
                 if (!__any_sync(wmask, need)) continue;
             }
             const RecHot Hr = R.hot[k];
@@ -642,7 +642,7 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
                     }
                     e[p] = __expf(-sigma);
                     eb[p] = use_blur ? __expf(-sigma_blur) : 0.f;
-                    alpha[p] = fminf(kAlphaMax, Hr.d.z * (nbf[p] * e[p] + bf[p] * eb[p]));
+                    alpha[p] = fminf(kAlphaMax, Hr.nop.z * (nbf[p] * e[p] + bf[p] * eb[p]));
                     if (H[p].t < kTNear || H[p].t > kTFar || alpha[p] < kAlphaMin) valid[p] = false;
                 }
                 any = any || valid[p];
@@ -781,7 +781,7 @@ __device__ __forceinline__ void edit_tile(const SceneArgs& a, const TileJob& J, 
                 sigma_blur = 0.5f * kBlurFsq * (dx * dx + dy * dy);
                 if (sigma_blur < sigma) { bf = 1.f; nbf = 0.f; }
             }
-            const float alpha = fminf(kAlphaMax, Hr.d.z * (nbf * __expf(-sigma) + bf * __expf(-sigma_blur)));
+            const float alpha = fminf(kAlphaMax, Hr.nop.z * (nbf * __expf(-sigma) + bf * __expf(-sigma_blur)));
             const bool skip = H.t < kTNear || H.t > kTFar || alpha < kAlphaMin;
             const float next_T = T * (1.f - alpha);
             if (next_T <= kTDone) { done = true; continue; }
