@@ -182,6 +182,11 @@ class BatchRenderer:
         self.moments = torch.empty(L.gstex_batch_backward_workspace_bytes(self.N), **u8)
         self.grads = None
         self.graph = None
+        # the splat records are built on a side stream, concurrently with the
+        # scan / emission / sort chain, and joined before the forward
+        self.side = torch.cuda.Stream(dev)
+        self.ev_fork = torch.cuda.Event()
+        self.ev_join = torch.cuda.Event()
 
     def _alloc_isect(self):
         L = _L()
@@ -224,9 +229,14 @@ class BatchRenderer:
                                     float(s.glob_scale), ptr(s.quats), ptr(s.sh_coeffs), sh_dtype, s.sh_degree,
                                     self.bw, ptr(self.colors), ptr(self.counts), st), "batch_project")
         VN = self.V * self.N
+        main = torch.cuda.current_stream(self.dev)
         if self.records is not None:
+            self.ev_fork.record(main)
+            self.side.wait_event(self.ev_fork)
             check(L.gstex_batch_records(ctypes.byref(self._inputs(s)), ptr(self.counts), ptr(self.records),
-                                        ptr(self.records_ws), self.records_ws.numel(), st), "batch_records")
+                                        ptr(self.records_ws), self.records_ws.numel(), self.side.cuda_stream),
+                  "batch_records")
+            self.ev_join.record(self.side)
         check(L.gstex_inclusive_scan_i32(VN, ptr(self.counts), ptr(self.cum), ptr(self.total), ptr(self.scan_ws),
                                          self.scan_ws.numel(), st), "scan")
         check(L.gstex_batch_emit(self.N, self.V, ptr(self.views_dev), ptr(s.means), ptr(s.scales),
@@ -238,6 +248,8 @@ class BatchRenderer:
                                      self.sort_ws.numel(), st), "sort_pairs_dyn")
         check(L.gstex_get_tile_bin_edges_dyn(self.capacity, ptr(self.count), ptr(self.keys_sorted), self.total_tiles,
                                              ptr(self.bins), st), "tile_bin_edges_dyn")
+        if self.records is not None:
+            main.wait_event(self.ev_join)
 
     def forward(self, s: Scene):
         L = _L()
