@@ -923,25 +923,48 @@ __global__ void BWD_BOUNDS(PPT) bwd_batch_kernel(SceneArgs a, BatchArgs ba, BwdA
     while (next_job(ba, &s_tile, J)) bwd_tile<TEXMODE, CT, PPT>(a, J, g, R, smom, lists, touched);
 }
 
+// Writes the 32 records of a warp, assembled in shared memory (src), to
+// dst[0, 32) as contiguous 16-byte chunks, skipping the records of lanes not
+// in `live`.
+__device__ __forceinline__ void copy_out_records(const RecAll* __restrict__ src, RecAll* __restrict__ dst,
+                                                 unsigned live, unsigned lane) {
+    constexpr int kChunks = (int)(sizeof(RecAll) / 16);
+    const uint4* s4 = reinterpret_cast<const uint4*>(src);
+    uint4* d4 = reinterpret_cast<uint4*>(dst);
+    __syncwarp();
+#pragma unroll 2
+    for (int c = (int)lane; c < 32 * kChunks; c += 32)
+        if ((live >> (c / kChunks)) & 1u) d4[c] = s4[c];
+}
+
 // Records of every (view, Gaussian) pair with tiles in the view, and of
 // Gaussian 0 in every view (the reference's zero-slot entries name it).
-// grid.y = view.  Near-edge-on pairs get fp32 coefficients here and are
-// appended to `fix` for records_fixup_kernel: on this GPU one lane in the
-// double branch would hold its whole warp at the fp64 rate.
-__global__ void records_kernel(SceneArgs a, BatchArgs ba, const int32_t* __restrict__ counts,
-                               RecAll* __restrict__ recs, int* __restrict__ fix_count, uint32_t* __restrict__ fix) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= ba.num_points) return;
-    const size_t j = (size_t)blockIdx.y * ba.num_points + i;
-    if (counts[j] <= 0 && i != 0) return;
-    const View V = ba.views[blockIdx.y].V;
-    RecAll r;
-    const bool defer = make_record(r.h, r.w, r.c, i, V, a.means[i], a.quats[i],
-                                   make_float2(a.scales[3 * i], a.scales[3 * i + 1]), a.glob, a.opac[i], ba.colors[j],
-                                   a.uv0[i], a.umap[i], a.vmap[i], a.dims[i], a.settings & (1 << 9), false, &r.e,
-                                   !(a.settings & (1 << 16)));
-    recs[j] = r;
-    if (defer) fix[atomicAdd(fix_count, 1)] = (uint32_t)j;
+// Block b covers Gaussians [128 (b / V), +128) of view b % V, so the blocks of
+// one Gaussian range run back to back and reread its parameters from cache.
+// Near-edge-on pairs get fp32 coefficients here and are appended to `fix`
+// for records_fixup_kernel: on this GPU one lane in the double branch would
+// hold its whole warp at the fp64 rate.
+__global__ void __launch_bounds__(128) records_kernel(SceneArgs a, BatchArgs ba, int num_views,
+                                                      const int32_t* __restrict__ counts, RecAll* __restrict__ recs,
+                                                      int* __restrict__ fix_count, uint32_t* __restrict__ fix) {
+    __shared__ RecAll srec[128];
+    const int v = blockIdx.x % num_views;
+    const int i0 = (blockIdx.x / num_views) * 128;
+    const int i = i0 + threadIdx.x;
+    const size_t j = (size_t)v * ba.num_points + i;
+    const bool live = i < ba.num_points && (i == 0 || counts[j] > 0);
+    if (live) {
+        const View V = ba.views[v].V;
+        RecAll& r = srec[threadIdx.x];
+        const bool defer = make_record(r.h, r.w, r.c, i, V, a.means[i], a.quats[i],
+                                       make_float2(a.scales[3 * i], a.scales[3 * i + 1]), a.glob, a.opac[i],
+                                       ba.colors[j], a.uv0[i], a.umap[i], a.vmap[i], a.dims[i],
+                                       a.settings & (1 << 9), false, &r.e, !(a.settings & (1 << 16)));
+        if (defer) fix[atomicAdd(fix_count, 1)] = (uint32_t)j;
+    }
+    const unsigned lane = threadIdx.x & 31;
+    const int w0 = threadIdx.x & ~31;
+    copy_out_records(srec + w0, recs + (size_t)v * ba.num_points + i0 + w0, __ballot_sync(0xffffffffu, live), lane);
 }
 
 // The double solve of one deferred near-edge-on record of Gaussian i.
@@ -972,18 +995,24 @@ __global__ void records_fixup_kernel(SceneArgs a, BatchArgs ba, const int* __res
 
 // Per-view form (texture_forward / texture_backward): the record of every
 // Gaussian of one view, so that any Gaussian a tile names has one.
-__global__ void view_records_kernel(SceneArgs a, ViewArgs va, RecAll* __restrict__ recs, int* __restrict__ fix_count,
-                                    uint32_t* __restrict__ fix) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.N) return;
-    const View V = load_view(va.viewmat, va.fx, va.fy, va.cx, va.cy);
-    RecAll r;
-    const bool defer = make_record(r.h, r.w, r.c, i, V, a.means[i], a.quats[i],
-                                   make_float2(a.scales[3 * i], a.scales[3 * i + 1]), a.glob, a.opac[i], va.colors[i],
-                                   a.uv0[i], a.umap[i], a.vmap[i], a.dims[i], a.settings & (1 << 9), false, &r.e,
-                                   !(a.settings & (1 << 16)));
-    recs[i] = r;
-    if (defer) fix[atomicAdd(fix_count, 1)] = (uint32_t)i;
+__global__ void __launch_bounds__(128) view_records_kernel(SceneArgs a, ViewArgs va, RecAll* __restrict__ recs,
+                                                           int* __restrict__ fix_count, uint32_t* __restrict__ fix) {
+    __shared__ RecAll srec[128];
+    const int i0 = blockIdx.x * 128;
+    const int i = i0 + threadIdx.x;
+    const bool live = i < a.N;
+    if (live) {
+        const View V = load_view(va.viewmat, va.fx, va.fy, va.cx, va.cy);
+        RecAll& r = srec[threadIdx.x];
+        const bool defer = make_record(r.h, r.w, r.c, i, V, a.means[i], a.quats[i],
+                                       make_float2(a.scales[3 * i], a.scales[3 * i + 1]), a.glob, a.opac[i],
+                                       va.colors[i], a.uv0[i], a.umap[i], a.vmap[i], a.dims[i], a.settings & (1 << 9),
+                                       false, &r.e, !(a.settings & (1 << 16)));
+        if (defer) fix[atomicAdd(fix_count, 1)] = (uint32_t)i;
+    }
+    const unsigned lane = threadIdx.x & 31;
+    const int w0 = threadIdx.x & ~31;
+    copy_out_records(srec + w0, recs + i0 + w0, __ballot_sync(0xffffffffu, live), lane);
 }
 
 __global__ void view_records_fixup_kernel(SceneArgs a, ViewArgs va, const int* __restrict__ fix_count,
@@ -1002,7 +1031,9 @@ int launch_records(const SceneArgs& a, const BatchArgs& ba, int num_views, const
     if (a.N == 0) return GSTEX_OK;
     cudaError_t e = cudaMemsetAsync(fix_count, 0, sizeof(int), stream);
     if (e != cudaSuccess) { set_cuda_error(e, "batch_records"); return GSTEX_ERR_CUDA; }
-    records_kernel<<<dim3(ceil_div(a.N, 128), num_views), 128, 0, stream>>>(a, ba, counts, recs, fix_count, fix);
+    const long long blocks = (long long)ceil_div(a.N, 128) * num_views;
+    if (blocks > 0x7fffffffLL) return GSTEX_ERR_UNSUPPORTED;
+    records_kernel<<<(unsigned)blocks, 128, 0, stream>>>(a, ba, num_views, counts, recs, fix_count, fix);
     records_fixup_kernel<<<152 * 4, 128, 0, stream>>>(a, ba, fix_count, fix, recs);
     return check_launch("batch_records", 2);
 }
