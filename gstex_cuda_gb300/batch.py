@@ -414,10 +414,14 @@ def plain_step(s: Scene, cameras: Sequence[Camera], tgt_img, tgt_tex, pix_offset
     loss_total = torch.zeros((), device=dev)
     st = torch.cuda.current_stream(dev).cuda_stream
     bw = block_width
+    # world->camera and camera->world matrices of every camera, as a caller
+    # keeps them (example.py:100-109 of the reference): one host inverse, one copy
+    vms = torch.stack([c.viewmat.detach().double().cpu().reshape(4, 4) for c in cameras])
+    mats = torch.stack([vms, torch.linalg.inv(vms)], 1).float().to(dev)
     for v, cam in enumerate(cameras):
         H, W = cam.height, cam.width
-        vm = cam.viewmat.to(dev).contiguous()
-        c2w = torch.linalg.inv(vm).contiguous()
+        vm = mats[v, 0].contiguous()
+        c2w = mats[v, 1].contiguous()
         campos = c2w[:3, 3]
         dirs = (s.means - campos[None]).contiguous()
         coeffs = s.sh_coeffs if s.sh_coeffs.dtype == torch.float32 else s.sh_coeffs.float()
