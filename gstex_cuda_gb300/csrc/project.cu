@@ -131,16 +131,20 @@ __global__ void scan_apply(int n, const int32_t* __restrict__ in, const int64_t*
 // ---------------------------------------------------------------------------
 // Spherical harmonics (csrc/sh.cuh:46-253; basis of gstex_cuda/_torch_impl.py:62-113)
 // ---------------------------------------------------------------------------
-__global__ void sh_forward_kernel(int n, int degree, int dtu, const float3* __restrict__ dirs,
+// Templated on the degree in use (DTU), so the basis stays in registers; the
+// coefficient stride follows the stored degree.
+template <int DTU>
+__global__ void sh_forward_kernel(int n, int degree, const float3* __restrict__ dirs,
                                   const float* __restrict__ coeffs, float* __restrict__ colors) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    constexpr int NB = (DTU + 1) * (DTU + 1);
     float Y[25];
-    const int nb = sh_basis(dtu, dirs[i], Y);
-    const int B = sh_bases(degree);
-    const float* k = coeffs + (size_t)i * B * 3;
+    sh_basis(DTU, dirs[i], Y);
+    const float* k = coeffs + (size_t)i * sh_bases(degree) * 3;
     float c0 = 0.f, c1 = 0.f, c2 = 0.f;
-    for (int b = 0; b < nb; b++) {
+#pragma unroll
+    for (int b = 0; b < NB; b++) {
         c0 += Y[b] * k[3 * b + 0];
         c1 += Y[b] * k[3 * b + 1];
         c2 += Y[b] * k[3 * b + 2];
@@ -150,20 +154,27 @@ __global__ void sh_forward_kernel(int n, int degree, int dtu, const float3* __re
     colors[3 * i + 2] = c2;
 }
 
-__global__ void sh_backward_kernel(int n, int degree, int dtu, const float3* __restrict__ dirs,
+template <int DTU>
+__global__ void sh_backward_kernel(int n, int degree, const float3* __restrict__ dirs,
                                    const float* __restrict__ v_colors, float* __restrict__ v_coeffs) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    constexpr int NB = (DTU + 1) * (DTU + 1);
     float Y[25];
-    const int nb = sh_basis(dtu, dirs[i], Y);
+    sh_basis(DTU, dirs[i], Y);
     const int B = sh_bases(degree);
     const float v0 = v_colors[3 * i], v1 = v_colors[3 * i + 1], v2 = v_colors[3 * i + 2];
     float* o = v_coeffs + (size_t)i * B * 3;
-    for (int b = 0; b < B; b++) {
-        const float y = b < nb ? Y[b] : 0.f;
-        o[3 * b + 0] = y * v0;
-        o[3 * b + 1] = y * v1;
-        o[3 * b + 2] = y * v2;
+#pragma unroll
+    for (int b = 0; b < NB; b++) {
+        o[3 * b + 0] = Y[b] * v0;
+        o[3 * b + 1] = Y[b] * v1;
+        o[3 * b + 2] = Y[b] * v2;
+    }
+    for (int b = NB; b < B; b++) {
+        o[3 * b + 0] = 0.f;
+        o[3 * b + 1] = 0.f;
+        o[3 * b + 2] = 0.f;
     }
 }
 
@@ -217,22 +228,51 @@ extern "C" int gstex_inclusive_scan_i32(int n, const int32_t* counts, int32_t* c
     return check_launch("inclusive_scan", 3);
 }
 
+// Degrees above 4 are not supported (sh.cuh:46-253 stops at 4); the degree in
+// use must not exceed the stored one (the reference's wrapper asserts it,
+// sh.py:54, and its kernel would read the next Gaussian's coefficients).
+static int sh_degrees_ok(int degree, int degrees_to_use) {
+    if (degree < 0 || degrees_to_use < 0 || degrees_to_use > degree) return GSTEX_ERR_INVALID_ARGUMENT;
+    if (degree > 4) return GSTEX_ERR_UNSUPPORTED;
+    return GSTEX_OK;
+}
+
 extern "C" int gstex_compute_sh_forward(int n, int degree, int degrees_to_use, const float* viewdirs,
                                         const float* coeffs, float* colors, gstex_stream_t stream) {
-    GSTEX_REQUIRE(n >= 0 && degree >= 0 && degrees_to_use >= 0);
+    GSTEX_REQUIRE(n >= 0);
+    int rc = sh_degrees_ok(degree, degrees_to_use);
+    if (rc) return rc;
     if (n == 0) return GSTEX_OK;
     GSTEX_REQUIRE(viewdirs && coeffs && colors);
-    sh_forward_kernel<<<ceil_div(n, 256), 256, 0, (cudaStream_t)stream>>>(
-        n, degree, degrees_to_use, (const float3*)viewdirs, coeffs, colors);
+    const dim3 grid(ceil_div(n, 256)), block(256);
+    cudaStream_t st = (cudaStream_t)stream;
+    const float3* d = (const float3*)viewdirs;
+    switch (degrees_to_use) {
+        case 0: sh_forward_kernel<0><<<grid, block, 0, st>>>(n, degree, d, coeffs, colors); break;
+        case 1: sh_forward_kernel<1><<<grid, block, 0, st>>>(n, degree, d, coeffs, colors); break;
+        case 2: sh_forward_kernel<2><<<grid, block, 0, st>>>(n, degree, d, coeffs, colors); break;
+        case 3: sh_forward_kernel<3><<<grid, block, 0, st>>>(n, degree, d, coeffs, colors); break;
+        default: sh_forward_kernel<4><<<grid, block, 0, st>>>(n, degree, d, coeffs, colors); break;
+    }
     return check_launch("compute_sh_forward");
 }
 
 extern "C" int gstex_compute_sh_backward(int n, int degree, int degrees_to_use, const float* viewdirs,
                                          const float* v_colors, float* v_coeffs, gstex_stream_t stream) {
-    GSTEX_REQUIRE(n >= 0 && degree >= 0 && degrees_to_use >= 0);
+    GSTEX_REQUIRE(n >= 0);
+    int rc = sh_degrees_ok(degree, degrees_to_use);
+    if (rc) return rc;
     if (n == 0) return GSTEX_OK;
     GSTEX_REQUIRE(viewdirs && v_colors && v_coeffs);
-    sh_backward_kernel<<<ceil_div(n, 256), 256, 0, (cudaStream_t)stream>>>(
-        n, degree, degrees_to_use, (const float3*)viewdirs, v_colors, v_coeffs);
+    const dim3 grid(ceil_div(n, 256)), block(256);
+    cudaStream_t st = (cudaStream_t)stream;
+    const float3* d = (const float3*)viewdirs;
+    switch (degrees_to_use) {
+        case 0: sh_backward_kernel<0><<<grid, block, 0, st>>>(n, degree, d, v_colors, v_coeffs); break;
+        case 1: sh_backward_kernel<1><<<grid, block, 0, st>>>(n, degree, d, v_colors, v_coeffs); break;
+        case 2: sh_backward_kernel<2><<<grid, block, 0, st>>>(n, degree, d, v_colors, v_coeffs); break;
+        case 3: sh_backward_kernel<3><<<grid, block, 0, st>>>(n, degree, d, v_colors, v_coeffs); break;
+        default: sh_backward_kernel<4><<<grid, block, 0, st>>>(n, degree, d, v_colors, v_coeffs); break;
+    }
     return check_launch("compute_sh_backward");
 }

@@ -50,6 +50,9 @@ def test_invalid_arguments_rejected_without_gpu():
     L = _lib.lib()
     assert L.gstex_get_aabb_2d(-1, None, None, 1.0, None, None, 1.0, 1.0, 0.0, 0.0, None, None, None) == 1
     assert L.gstex_sort_pairs(10, 70, None, None, None, None, None, 0, None) == 1
+    # SH: the degree in use above the stored degree, and degrees above 4
+    assert L.gstex_compute_sh_forward(1, 2, 3, 16, 16, 16, None) == 1
+    assert L.gstex_compute_sh_backward(1, 5, 5, 16, 16, 16, None) == 3
     ri = _lib.RasterInputs()
     ri.num_points, ri.img_width, ri.img_height, ri.block_width, ri.channels = 1, 8, 8, 16, 65
     import ctypes
