@@ -7,11 +7,12 @@ per stage, keeps every size on the device (intersection buffers are sized by
 capacity, an overflow flag reports a too-small capacity), and can capture a
 whole forward + backward step in a CUDA graph.
 
-Stages of ``step``: projection of all (view, Gaussian) pairs with SH colours
--> inclusive scan of tile counts -> emission of (global tile | depth) keys ->
-stable radix sort -> tile ranges -> persistent forward over a global tile
-queue -> image losses and their gradients -> persistent backward -> SH
-adjoint over views.
+Stages of ``step``: projection of all (view, Gaussian) pairs with SH colours,
+depth keys and tile rectangles -> (side stream) splat records -> stable sort
+of the pairs by depth -> inclusive scan of their tile counts in that order ->
+emission of (global tile << 1 | real) keys -> stable sort by tile -> tile
+ranges -> persistent forward over a global tile queue -> image losses and
+their gradients -> persistent backward -> SH adjoint over views.
 """
 from __future__ import annotations
 
@@ -49,6 +50,12 @@ _BATCH_SIGS = {
     "gstex_batch_views_bytes": (ctypes.c_size_t, [_I]),
     "gstex_batch_prepare": (_I, [_I, ctypes.POINTER(ViewDesc), _I, _P, _P, _P, _P]),
     "gstex_batch_project": (_I, [_I, _I, _P, _P, _P, _F, _P, _P, _I, _I, _I, _P, _P, _P]),
+    "gstex_batch_project_keys": (_I, [_I, _I, _P, _P, _P, _F, _P, _P, _I, _I, _I, _P, _P, _P, _P, _P, _P]),
+    "gstex_batch_gather_counts": (_I, [_I, _P, _P, _P, _P]),
+    "gstex_batch_emit_sorted": (_I, [_I, _I, _P, _P, _P, _P, _P, _LL, _P, _P, _P, _P, _P]),
+    "gstex_sort32_workspace_bytes": (ctypes.c_size_t, [_I]),
+    "gstex_sort_pairs32": (_I, [_I, _P, _I, _P, _P, _P, _P, _P, ctypes.c_size_t, _P]),
+    "gstex_get_tile_bin_edges32_dyn": (_I, [_I, _P, _P, _I, _I, _P, _P]),
     "gstex_batch_emit": (_I, [_I, _I, _P, _P, _P, _F, _P, _I, _P, _P, _LL, _P, _P, _P, _P, _P]),
     "gstex_sort_pairs_dyn": (_I, [_I, _P, _I, _P, _P, _P, _P, _P, ctypes.c_size_t, _P]),
     "gstex_get_tile_bin_edges_dyn": (_I, [_I, _P, _P, _I, _P, _P]),
@@ -157,6 +164,15 @@ class BatchRenderer:
         self.cum = torch.empty(VN, **i32)
         self.total = torch.zeros(1, **i64)
         self.scan_ws = torch.empty(L.gstex_scan_workspace_bytes(VN), **u8)
+        # depth-first binning: per-pair depth keys, ids and tile rectangles,
+        # their depth order, and the counts / offsets in that order
+        self.dkeys = torch.empty(VN, **i32)
+        self.pair_ids = torch.empty(VN, **i32)
+        self.rects = torch.empty((VN, 2), **i32)
+        self.dkeys_sorted = torch.empty(VN, **i32)
+        self.order = torch.empty(VN, **i32)
+        self.scounts = torch.empty(VN, **i32)
+        self.dsort_ws = torch.empty(L.gstex_sort32_workspace_bytes(VN), **u8)
         # splat records of every (view, Gaussian), built once per step by bin()
         self.records = (torch.empty(L.gstex_batch_records_bytes(self.N, self.V), **u8) if prebuilt_records
                         else None)
@@ -192,14 +208,15 @@ class BatchRenderer:
         L = _L()
         cap = self.capacity
         dev = self.dev
-        self.keys = torch.empty(cap, dtype=torch.int64, device=dev)
+        # (global tile << 1 | real) keys of the intersections and their Gaussians
+        self.keys = torch.empty(cap, dtype=torch.int32, device=dev)
         self.vals = torch.empty(cap, dtype=torch.int32, device=dev)
-        self.keys_sorted = torch.empty(cap, dtype=torch.int64, device=dev)
+        self.keys_sorted = torch.empty(cap, dtype=torch.int32, device=dev)
         self.gids_sorted = torch.empty(cap, dtype=torch.int32, device=dev)
-        self.sort_ws = torch.empty(L.gstex_sort_workspace_bytes(cap), dtype=torch.uint8, device=dev)
+        self.sort_ws = torch.empty(L.gstex_sort32_workspace_bytes(cap), dtype=torch.uint8, device=dev)
 
     def end_bit(self):
-        return 32 + max(1, int(self.total_tiles).bit_length())
+        return 1 + max(1, int(self.total_tiles).bit_length())
 
     # ------------------------------------------------------------------
     def _inputs(self, s: Scene, backward: bool = False) -> BatchInputs:
@@ -225,9 +242,10 @@ class BatchRenderer:
         L = _L()
         st = torch.cuda.current_stream(self.dev).cuda_stream
         sh_dtype = 1 if s.sh_coeffs.dtype == torch.bfloat16 else 0
-        check(L.gstex_batch_project(self.N, self.V, ptr(self.views_dev), ptr(s.means), ptr(s.scales),
-                                    float(s.glob_scale), ptr(s.quats), ptr(s.sh_coeffs), sh_dtype, s.sh_degree,
-                                    self.bw, ptr(self.colors), ptr(self.counts), st), "batch_project")
+        check(L.gstex_batch_project_keys(self.N, self.V, ptr(self.views_dev), ptr(s.means), ptr(s.scales),
+                                         float(s.glob_scale), ptr(s.quats), ptr(s.sh_coeffs), sh_dtype, s.sh_degree,
+                                         self.bw, ptr(self.colors), ptr(self.counts), ptr(self.dkeys),
+                                         ptr(self.pair_ids), ptr(self.rects), st), "batch_project_keys")
         VN = self.V * self.N
         main = torch.cuda.current_stream(self.dev)
         if self.records is not None:
@@ -237,17 +255,22 @@ class BatchRenderer:
                                         ptr(self.records_ws), self.records_ws.numel(), self.side.cuda_stream),
                   "batch_records")
             self.ev_join.record(self.side)
-        check(L.gstex_inclusive_scan_i32(VN, ptr(self.counts), ptr(self.cum), ptr(self.total), ptr(self.scan_ws),
+        # pairs in depth order, then their tiles in that order, then one stable
+        # sort by (global tile << 1 | real)
+        check(L.gstex_sort_pairs32(VN, None, 32, ptr(self.dkeys), ptr(self.pair_ids), ptr(self.dkeys_sorted),
+                                   ptr(self.order), ptr(self.dsort_ws), self.dsort_ws.numel(), st), "sort_pairs32")
+        check(L.gstex_batch_gather_counts(VN, ptr(self.order), ptr(self.counts), ptr(self.scounts), st),
+              "batch_gather_counts")
+        check(L.gstex_inclusive_scan_i32(VN, ptr(self.scounts), ptr(self.cum), ptr(self.total), ptr(self.scan_ws),
                                          self.scan_ws.numel(), st), "scan")
-        check(L.gstex_batch_emit(self.N, self.V, ptr(self.views_dev), ptr(s.means), ptr(s.scales),
-                                 float(s.glob_scale), ptr(s.quats), self.bw, ptr(self.cum), ptr(self.total),
-                                 self.capacity, ptr(self.keys), ptr(self.vals), ptr(self.count), ptr(self.overflow),
-                                 st), "batch_emit")
-        check(L.gstex_sort_pairs_dyn(self.capacity, ptr(self.count), self.end_bit(), ptr(self.keys), ptr(self.vals),
-                                     ptr(self.keys_sorted), ptr(self.gids_sorted), ptr(self.sort_ws),
-                                     self.sort_ws.numel(), st), "sort_pairs_dyn")
-        check(L.gstex_get_tile_bin_edges_dyn(self.capacity, ptr(self.count), ptr(self.keys_sorted), self.total_tiles,
-                                             ptr(self.bins), st), "tile_bin_edges_dyn")
+        check(L.gstex_batch_emit_sorted(self.N, self.V, ptr(self.views_dev), ptr(self.order), ptr(self.cum),
+                                        ptr(self.rects), ptr(self.total), self.capacity, ptr(self.keys),
+                                        ptr(self.vals), ptr(self.count), ptr(self.overflow), st), "batch_emit_sorted")
+        check(L.gstex_sort_pairs32(self.capacity, ptr(self.count), self.end_bit(), ptr(self.keys), ptr(self.vals),
+                                   ptr(self.keys_sorted), ptr(self.gids_sorted), ptr(self.sort_ws),
+                                   self.sort_ws.numel(), st), "sort_pairs32")
+        check(L.gstex_get_tile_bin_edges32_dyn(self.capacity, ptr(self.count), ptr(self.keys_sorted), 1,
+                                               self.total_tiles, ptr(self.bins), st), "tile_bin_edges32_dyn")
         if self.records is not None:
             main.wait_event(self.ev_join)
 

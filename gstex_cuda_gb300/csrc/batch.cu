@@ -26,7 +26,8 @@ template <typename SHT, int DEG>
 __global__ void batch_project_kernel(int N, int V, const BatchView* __restrict__ views, const float3* __restrict__ means,
                                      const float* __restrict__ scales, float glob, const float4* __restrict__ quats,
                                      const SHT* __restrict__ sh, int bw, float3* __restrict__ colors,
-                                     int32_t* __restrict__ counts) {
+                                     int32_t* __restrict__ counts, uint32_t* __restrict__ depth_keys,
+                                     int32_t* __restrict__ pair_ids, uint2* __restrict__ rects) {
     constexpr int B = (DEG + 1) * (DEG + 1);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
@@ -51,7 +52,22 @@ __global__ void batch_project_kernel(int N, int V, const BatchView* __restrict__
         float2 c, e;
         float z;
         aabb_2d(m, bv.V.fx, bv.V.fy, bv.V.cx, bv.V.cy, p, q, sx, sy, glob, c, e, z);
-        counts[(size_t)v * N + i] = tiles_hit(c, e, bv.tiles_x, bv.tiles_y, (float)bw);
+        const size_t j = (size_t)v * N + i;
+        const int cnt = tiles_hit(c, e, bv.tiles_x, bv.tiles_y, (float)bw);
+        counts[j] = cnt;
+        if (depth_keys) {
+            // depth-first binning: the pair's sort key (pairs without tiles last)
+            // and the tile rectangle its emission walks (empty: fillers only)
+            depth_keys[j] = cnt > 0 ? __float_as_uint(z) : 0xffffffffu;
+            pair_ids[j] = (int32_t)j;
+            uint2 rc = make_uint2(0u, 0u);
+            if (cnt > 0 && !((double)e.x <= 1e-4 && (double)e.y <= 1e-4)) {
+                int x0, y0, x1, y1;
+                tile_rect(c, e, bv.tiles_x, bv.tiles_y, bw, x0, y0, x1, y1);
+                rc = make_uint2((uint32_t)x0 | ((uint32_t)x1 << 16), (uint32_t)y0 | ((uint32_t)y1 << 16));
+            }
+            rects[j] = rc;
+        }
         float Y[25];
         sh_basis(DEG, make_float3(p.x - bv.campos[0], p.y - bv.campos[1], p.z - bv.campos[2]), Y);
         float3 col = make_float3(0.f, 0.f, 0.f);
@@ -112,6 +128,53 @@ __global__ void batch_emit_kernel(int N, int V, const BatchView* __restrict__ vi
             keys[cur] = (int64_t)((uint64_t)bv.tile_offset << 32);
             vals[cur] = 0;
         }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Depth-first binning.  The (view, Gaussian) pairs are sorted by the bits of
+// their camera depth (stable: ties keep (view, Gaussian) order), each pair
+// emits its tiles in that order, and one stable sort by
+// (global tile << 1 | real) orders every tile front to back.  This is the
+// order of the reference's sort by (tile << 32 | depth bits) with ties in
+// emission order, built from 32-bit keys: 4 passes over the pairs and 3 over
+// the intersections instead of 7 over 64-bit intersection keys.  Slots a
+// Gaussian does not write (filler bit 0) take the place the reference's zero
+// entries take: first in the view's tile 0, with Gaussian 0.
+// ---------------------------------------------------------------------------
+__global__ void gather_counts_kernel(int n, const int32_t* __restrict__ order, const int32_t* __restrict__ counts,
+                                     int32_t* __restrict__ out) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n) out[p] = counts[order[p]];
+}
+
+// Pair p of the depth order writes [cum[p-1], cum[p]) (clipped to the capacity).
+__global__ void batch_emit_sorted_kernel(int VN, int N, const BatchView* __restrict__ views,
+                                         const int32_t* __restrict__ order, const int32_t* __restrict__ cum,
+                                         const uint2* __restrict__ rects, long long capacity,
+                                         uint32_t* __restrict__ keys, int32_t* __restrict__ vals) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= VN) return;
+    long long lo = p == 0 ? 0 : (long long)(uint32_t)cum[p - 1];
+    long long hi = (long long)(uint32_t)cum[p];
+    if (hi > capacity) hi = capacity;
+    if (lo >= hi) return;
+    const int j = order[p];
+    const int v = j / N;
+    const int i = j - v * N;
+    const BatchView& bv = views[v];
+    const uint2 rc = rects[j];
+    const int x0 = (int)(rc.x & 0xffffu), x1 = (int)(rc.x >> 16), y0 = (int)(rc.y & 0xffffu), y1 = (int)(rc.y >> 16);
+    long long cur = lo;
+    for (int ty = y0; ty < y1 && cur < hi; ++ty)
+        for (int tx = x0; tx < x1 && cur < hi; ++tx) {
+            keys[cur] = ((uint32_t)(bv.tile_offset + ty * bv.tiles_x + tx) << 1) | 1u;
+            vals[cur] = i;
+            ++cur;
+        }
+    for (; cur < hi; ++cur) {
+        keys[cur] = (uint32_t)bv.tile_offset << 1;
+        vals[cur] = 0;
     }
 }
 
@@ -282,36 +345,79 @@ extern "C" int gstex_batch_prepare(int num_views, const gstex_view_desc* views, 
 template <typename SHT>
 static void project_launch(int deg, int N, int V, const BatchView* bv, const float* means, const float* scales,
                            float glob, const float* quats, const SHT* sh, int bw, float* colors, int32_t* counts,
-                           cudaStream_t stream) {
+                           uint32_t* dk, int32_t* ids, uint2* rects, cudaStream_t stream) {
     const dim3 grid(ceil_div(N, 128)), block(128);
     const float3* m = (const float3*)means;
     const float4* q = (const float4*)quats;
     float3* c = (float3*)colors;
     switch (deg) {
-        case 0: batch_project_kernel<SHT, 0><<<grid, block, 0, stream>>>(N, V, bv, m, scales, glob, q, sh, bw, c, counts); break;
-        case 1: batch_project_kernel<SHT, 1><<<grid, block, 0, stream>>>(N, V, bv, m, scales, glob, q, sh, bw, c, counts); break;
-        case 2: batch_project_kernel<SHT, 2><<<grid, block, 0, stream>>>(N, V, bv, m, scales, glob, q, sh, bw, c, counts); break;
-        case 3: batch_project_kernel<SHT, 3><<<grid, block, 0, stream>>>(N, V, bv, m, scales, glob, q, sh, bw, c, counts); break;
-        default: batch_project_kernel<SHT, 4><<<grid, block, 0, stream>>>(N, V, bv, m, scales, glob, q, sh, bw, c, counts); break;
+        case 0: batch_project_kernel<SHT, 0><<<grid, block, 0, stream>>>(N, V, bv, m, scales, glob, q, sh, bw, c, counts, dk, ids, rects); break;
+        case 1: batch_project_kernel<SHT, 1><<<grid, block, 0, stream>>>(N, V, bv, m, scales, glob, q, sh, bw, c, counts, dk, ids, rects); break;
+        case 2: batch_project_kernel<SHT, 2><<<grid, block, 0, stream>>>(N, V, bv, m, scales, glob, q, sh, bw, c, counts, dk, ids, rects); break;
+        case 3: batch_project_kernel<SHT, 3><<<grid, block, 0, stream>>>(N, V, bv, m, scales, glob, q, sh, bw, c, counts, dk, ids, rects); break;
+        default: batch_project_kernel<SHT, 4><<<grid, block, 0, stream>>>(N, V, bv, m, scales, glob, q, sh, bw, c, counts, dk, ids, rects); break;
     }
+}
+
+static int project_impl(int N, int V, const void* views_dev, const float* means, const float* scales,
+                        float glob_scale, const float* quats, const void* sh_coeffs, int sh_dtype, int sh_degree,
+                        int block_width, float* colors, int32_t* counts, uint32_t* depth_keys, int32_t* pair_ids,
+                        uint2* rects, cudaStream_t stream) {
+    GSTEX_REQUIRE(N >= 0 && V > 0 && views_dev && block_width >= 2 && block_width <= kMaxBlockWidth);
+    GSTEX_REQUIRE(sh_degree >= 0 && sh_degree <= 4 && (sh_dtype == 0 || sh_dtype == 1));
+    if (N == 0) return GSTEX_OK;
+    GSTEX_REQUIRE(means && scales && quats && sh_coeffs && colors && counts);
+    const BatchView* bv = (const BatchView*)views_dev;
+    if (sh_dtype == 1)
+        project_launch<__nv_bfloat16>(sh_degree, N, V, bv, means, scales, glob_scale, quats,
+                                      (const __nv_bfloat16*)sh_coeffs, block_width, colors, counts, depth_keys,
+                                      pair_ids, rects, stream);
+    else
+        project_launch<float>(sh_degree, N, V, bv, means, scales, glob_scale, quats, (const float*)sh_coeffs,
+                              block_width, colors, counts, depth_keys, pair_ids, rects, stream);
+    return check_launch("batch_project");
 }
 
 extern "C" int gstex_batch_project(int N, int V, const void* views_dev, const float* means, const float* scales,
                                    float glob_scale, const float* quats, const void* sh_coeffs, int sh_dtype,
                                    int sh_degree, int block_width, float* colors, int32_t* counts, gstex_stream_t s) {
-    GSTEX_REQUIRE(N >= 0 && V > 0 && views_dev && block_width >= 2 && block_width <= kMaxBlockWidth);
-    GSTEX_REQUIRE(sh_degree >= 0 && sh_degree <= 4 && (sh_dtype == 0 || sh_dtype == 1));
-    if (N == 0) return GSTEX_OK;
-    GSTEX_REQUIRE(means && scales && quats && sh_coeffs && colors && counts);
+    return project_impl(N, V, views_dev, means, scales, glob_scale, quats, sh_coeffs, sh_dtype, sh_degree,
+                        block_width, colors, counts, nullptr, nullptr, nullptr, (cudaStream_t)s);
+}
+
+extern "C" int gstex_batch_project_keys(int N, int V, const void* views_dev, const float* means, const float* scales,
+                                        float glob_scale, const float* quats, const void* sh_coeffs, int sh_dtype,
+                                        int sh_degree, int block_width, float* colors, int32_t* counts,
+                                        uint32_t* depth_keys, int32_t* pair_ids, uint32_t* rects, gstex_stream_t s) {
+    if ((unsigned long long)N * (unsigned long long)V > 0x7fffffffull) return GSTEX_ERR_UNSUPPORTED;
+    if (N > 0) GSTEX_REQUIRE(depth_keys && pair_ids && rects && ((uintptr_t)rects & 7) == 0);
+    return project_impl(N, V, views_dev, means, scales, glob_scale, quats, sh_coeffs, sh_dtype, sh_degree,
+                        block_width, colors, counts, depth_keys, pair_ids, (uint2*)rects, (cudaStream_t)s);
+}
+
+extern "C" int gstex_batch_gather_counts(int n, const int32_t* order, const int32_t* counts, int32_t* out,
+                                         gstex_stream_t s) {
+    GSTEX_REQUIRE(n >= 0);
+    if (n == 0) return GSTEX_OK;
+    GSTEX_REQUIRE(order && counts && out);
+    gather_counts_kernel<<<ceil_div(n, 256), 256, 0, (cudaStream_t)s>>>(n, order, counts, out);
+    return check_launch("batch_gather_counts");
+}
+
+extern "C" int gstex_batch_emit_sorted(int N, int V, const void* views_dev, const int32_t* order, const int32_t* cum,
+                                       const uint32_t* rects, const int64_t* total, long long capacity,
+                                       uint32_t* keys, int32_t* vals, int64_t* count, int* overflow,
+                                       gstex_stream_t s) {
+    GSTEX_REQUIRE(N >= 0 && V > 0 && views_dev && capacity >= 0 && total && count && overflow);
+    if ((unsigned long long)N * (unsigned long long)V > 0x7fffffffull) return GSTEX_ERR_UNSUPPORTED;
     cudaStream_t stream = (cudaStream_t)s;
-    const BatchView* bv = (const BatchView*)views_dev;
-    if (sh_dtype == 1)
-        project_launch<__nv_bfloat16>(sh_degree, N, V, bv, means, scales, glob_scale, quats,
-                                      (const __nv_bfloat16*)sh_coeffs, block_width, colors, counts, stream);
-    else
-        project_launch<float>(sh_degree, N, V, bv, means, scales, glob_scale, quats, (const float*)sh_coeffs,
-                              block_width, colors, counts, stream);
-    return check_launch("batch_project");
+    clamp_count_kernel<<<1, 1, 0, stream>>>(total, capacity, count, overflow);
+    if (N == 0 || capacity == 0) return check_launch("batch_emit_sorted");
+    GSTEX_REQUIRE(order && cum && rects && keys && vals && ((uintptr_t)rects & 7) == 0);
+    const int VN = N * V;
+    batch_emit_sorted_kernel<<<ceil_div(VN, 256), 256, 0, stream>>>(VN, N, (const BatchView*)views_dev, order, cum,
+                                                                     (const uint2*)rects, capacity, keys, vals);
+    return check_launch("batch_emit_sorted", 2);
 }
 
 extern "C" int gstex_batch_emit(int N, int V, const void* views_dev, const float* means, const float* scales,

@@ -61,7 +61,10 @@ __global__ void emit_kernel(int n, int num_isect, const float2* __restrict__ cen
 // Tile ranges (reference csrc/forward.cu:76-98); tiles outside [0, num_tiles)
 // are ignored.
 // ---------------------------------------------------------------------------
-__global__ void bin_edges_kernel(int n, const int64_t* __restrict__ n_dev, const int64_t* __restrict__ sorted,
+// Tile of a sorted key: bits [shift, ...) of a 64-bit (tile | depth) key or of
+// a 32-bit (tile | filler bit) key.
+template <typename K>
+__global__ void bin_edges_kernel(int n, const int64_t* __restrict__ n_dev, const K* __restrict__ sorted, int shift,
                                  int num_tiles, int2* __restrict__ bins) {
     if (n_dev) {
         const int64_t m = *n_dev;
@@ -69,12 +72,12 @@ __global__ void bin_edges_kernel(int n, const int64_t* __restrict__ n_dev, const
     }
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int cur = (int)(sorted[i] >> 32);
+    const int cur = (int)(sorted[i] >> shift);
     const bool ok = cur >= 0 && cur < num_tiles;
     if (i == 0 && ok) bins[cur].x = 0;
     if (i == n - 1 && ok) bins[cur].y = n;
     if (i == 0) return;
-    const int prev = (int)(sorted[i - 1] >> 32);
+    const int prev = (int)(sorted[i - 1] >> shift);
     if (prev != cur) {
         if (prev >= 0 && prev < num_tiles) bins[prev].y = i;
         if (ok) bins[cur].x = i;
@@ -122,7 +125,8 @@ __device__ __forceinline__ void resolve_count(const int64_t* n_dev, int& n, int&
     }
 }
 
-__global__ void __launch_bounds__(kSortThreads) radix_hist_kernel(const uint64_t* __restrict__ keys, int n, int chunk,
+template <typename K>
+__global__ void __launch_bounds__(kSortThreads) radix_hist_kernel(const K* __restrict__ keys, int n, int chunk,
                                                                   const int64_t* __restrict__ n_dev, int shift,
                                                                   uint32_t* __restrict__ hist) {
     __shared__ uint32_t h[kRadix];
@@ -195,16 +199,17 @@ __global__ void __launch_bounds__(kSortThreads) radix_scan_rows_kernel(uint32_t*
 // Stable scatter of one block's chunk, 2048 items at a time: items are ranked
 // by digit (warp match + per-warp counters, so equal digits keep their input
 // order), regrouped by digit in shared memory, and written out as runs of
-// consecutive positions.
+// consecutive positions.  K: 64- or 32-bit keys.
+template <typename K>
 __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
-    const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
+    const K* __restrict__ kin, const uint32_t* __restrict__ vin, K* __restrict__ kout,
     uint32_t* __restrict__ vout, int n, int chunk, const int64_t* __restrict__ n_dev, int shift,
     const uint32_t* __restrict__ offsets, const uint32_t* __restrict__ totals) {
     __shared__ uint32_t run_off[kRadix];
     __shared__ uint32_t tile_base[kRadix];
     __shared__ uint32_t wsum[kSortWarps];
     __shared__ uint32_t wcnt[kSortWarps][kRadix];
-    __shared__ uint64_t skey[kSortTile];
+    __shared__ K skey[kSortTile];
     __shared__ uint32_t sval[kSortTile];
     resolve_count(n_dev, n, chunk);
     const int tid = threadIdx.x, warp = tid >> 5;
@@ -220,7 +225,7 @@ __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
     for (int tbase = start; tbase < end; tbase += kSortTile) {
         for (int k = tid; k < kSortWarps * kRadix; k += blockDim.x) (&wcnt[0][0])[k] = 0;
         __syncthreads();
-        uint64_t key[kSortItems];
+        K key[kSortItems];
         uint32_t val[kSortItems];
         uint32_t rank[kSortItems];
 #pragma unroll
@@ -266,7 +271,7 @@ __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
         __syncthreads();
         const int tile_n = min(kSortTile, end - tbase);
         for (int l = tid; l < tile_n; l += kSortThreads) {
-            const uint64_t kk = skey[l];
+            const K kk = skey[l];
             const uint32_t d = (uint32_t)(kk >> shift) & (kRadix - 1);
             const uint32_t pos = run_off[d] + (uint32_t)l - tile_base[d];
             kout[pos] = kk;
@@ -301,47 +306,51 @@ extern "C" int gstex_map_gaussian_to_intersects(int n, int num_isect, const floa
     return check_launch("map_gaussian_to_intersects");
 }
 
-extern "C" size_t gstex_sort_workspace_bytes(int n) {
+static size_t sort_workspace_bytes(int n, size_t key_bytes) {
     if (n < 1) n = 1;
     const SortPlan p = sort_plan(n);
-    return align_up((size_t)n * 8, 256) + align_up((size_t)n * 4, 256) + (size_t)kRadix * p.blocks * 4 +
+    return align_up((size_t)n * key_bytes, 256) + align_up((size_t)n * 4, 256) + (size_t)kRadix * p.blocks * 4 +
            (size_t)kRadix * 4;
 }
 
-static int sort_impl(int n, const int64_t* n_dev, int end_bit, const int64_t* keys_in, const int32_t* vals_in,
-                     int64_t* keys_out, int32_t* vals_out, void* ws, size_t ws_bytes, cudaStream_t stream) {
-    GSTEX_REQUIRE(n >= 0 && end_bit >= 0 && end_bit <= 64);
+extern "C" size_t gstex_sort_workspace_bytes(int n) { return sort_workspace_bytes(n, 8); }
+extern "C" size_t gstex_sort32_workspace_bytes(int n) { return sort_workspace_bytes(n, 4); }
+
+template <typename K>
+static int sort_impl(int n, const int64_t* n_dev, int end_bit, const K* keys_in, const int32_t* vals_in,
+                     K* keys_out, int32_t* vals_out, void* ws, size_t ws_bytes, cudaStream_t stream) {
+    GSTEX_REQUIRE(n >= 0 && end_bit >= 0 && end_bit <= (int)(8 * sizeof(K)));
     if (n == 0) return GSTEX_OK;
     GSTEX_REQUIRE(keys_in && vals_in && keys_out && vals_out);
     const int passes = ceil_div(end_bit, 8);
     if (passes == 0 || (n == 1 && !n_dev)) {
-        cudaError_t e = cudaMemcpyAsync(keys_out, keys_in, (size_t)n * 8, cudaMemcpyDeviceToDevice, stream);
+        cudaError_t e = cudaMemcpyAsync(keys_out, keys_in, (size_t)n * sizeof(K), cudaMemcpyDeviceToDevice, stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(vals_out, vals_in, (size_t)n * 4, cudaMemcpyDeviceToDevice, stream);
         if (e != cudaSuccess) { set_cuda_error(e, "sort_pairs copy"); return GSTEX_ERR_CUDA; }
         return GSTEX_OK;
     }
     GSTEX_REQUIRE(ws);
-    if (ws_bytes < gstex_sort_workspace_bytes(n)) return GSTEX_ERR_CAPACITY;
+    if (ws_bytes < sort_workspace_bytes(n, sizeof(K))) return GSTEX_ERR_CAPACITY;
     const SortPlan p = sort_plan(n);
     char* w = (char*)ws;
-    uint64_t* kalt = (uint64_t*)w;
-    w += align_up((size_t)n * 8, 256);
+    K* kalt = (K*)w;
+    w += align_up((size_t)n * sizeof(K), 256);
     uint32_t* valt = (uint32_t*)w;
     w += align_up((size_t)n * 4, 256);
     uint32_t* hist = (uint32_t*)w;
     uint32_t* totals = hist + (size_t)kRadix * p.blocks;
     // Ping-pong so that the last pass lands in the output buffers.
-    const uint64_t* ksrc = (const uint64_t*)keys_in;
+    const K* ksrc = keys_in;
     const uint32_t* vsrc = (const uint32_t*)vals_in;
     for (int pass = 0; pass < passes; pass++) {
         const bool to_out = ((passes - 1 - pass) % 2) == 0;
-        uint64_t* kdst = to_out ? (uint64_t*)keys_out : kalt;
+        K* kdst = to_out ? keys_out : kalt;
         uint32_t* vdst = to_out ? (uint32_t*)vals_out : valt;
         const int shift = pass * 8;
-        radix_hist_kernel<<<p.blocks, kSortThreads, 0, stream>>>(ksrc, n, p.chunk, n_dev, shift, hist);
+        radix_hist_kernel<K><<<p.blocks, kSortThreads, 0, stream>>>(ksrc, n, p.chunk, n_dev, shift, hist);
         radix_scan_rows_kernel<<<kRadix, kSortThreads, 0, stream>>>(hist, p.blocks, totals);
-        radix_scatter_kernel<<<p.blocks, kSortThreads, 0, stream>>>(ksrc, vsrc, kdst, vdst, n, p.chunk, n_dev, shift,
-                                                                    hist, totals);
+        radix_scatter_kernel<K><<<p.blocks, kSortThreads, 0, stream>>>(ksrc, vsrc, kdst, vdst, n, p.chunk, n_dev,
+                                                                       shift, hist, totals);
         ksrc = kdst;
         vsrc = vdst;
     }
@@ -350,14 +359,23 @@ static int sort_impl(int n, const int64_t* n_dev, int end_bit, const int64_t* ke
 
 extern "C" int gstex_sort_pairs(int n, int end_bit, const int64_t* keys_in, const int32_t* vals_in,
                                 int64_t* keys_out, int32_t* vals_out, void* ws, size_t ws_bytes, gstex_stream_t s) {
-    return sort_impl(n, nullptr, end_bit, keys_in, vals_in, keys_out, vals_out, ws, ws_bytes, (cudaStream_t)s);
+    return sort_impl<uint64_t>(n, nullptr, end_bit, (const uint64_t*)keys_in, vals_in, (uint64_t*)keys_out, vals_out,
+                               ws, ws_bytes, (cudaStream_t)s);
 }
 
 extern "C" int gstex_sort_pairs_dyn(int capacity, const int64_t* count, int end_bit, const int64_t* keys_in,
                                     const int32_t* vals_in, int64_t* keys_out, int32_t* vals_out, void* ws,
                                     size_t ws_bytes, gstex_stream_t s) {
     GSTEX_REQUIRE(count);
-    return sort_impl(capacity, count, end_bit, keys_in, vals_in, keys_out, vals_out, ws, ws_bytes, (cudaStream_t)s);
+    return sort_impl<uint64_t>(capacity, count, end_bit, (const uint64_t*)keys_in, vals_in, (uint64_t*)keys_out,
+                               vals_out, ws, ws_bytes, (cudaStream_t)s);
+}
+
+extern "C" int gstex_sort_pairs32(int n, const int64_t* count, int end_bit, const uint32_t* keys_in,
+                                  const int32_t* vals_in, uint32_t* keys_out, int32_t* vals_out, void* ws,
+                                  size_t ws_bytes, gstex_stream_t s) {
+    return sort_impl<uint32_t>(n, count, end_bit, keys_in, vals_in, keys_out, vals_out, ws, ws_bytes,
+                               (cudaStream_t)s);
 }
 
 extern "C" int gstex_get_tile_bin_edges(int num_isect, const int64_t* sorted, int num_tiles, int32_t* bins,
@@ -368,8 +386,8 @@ extern "C" int gstex_get_tile_bin_edges(int num_isect, const int64_t* sorted, in
     if (e != cudaSuccess) { set_cuda_error(e, "tile_bin_edges memset"); return GSTEX_ERR_CUDA; }
     if (num_isect == 0) return GSTEX_OK;
     GSTEX_REQUIRE(sorted);
-    bin_edges_kernel<<<ceil_div(num_isect, 256), 256, 0, stream>>>(num_isect, nullptr, sorted, num_tiles,
-                                                                    (int2*)bins);
+    bin_edges_kernel<int64_t><<<ceil_div(num_isect, 256), 256, 0, stream>>>(num_isect, nullptr, sorted, 32,
+                                                                             num_tiles, (int2*)bins);
     return check_launch("get_tile_bin_edges");
 }
 
@@ -381,6 +399,20 @@ extern "C" int gstex_get_tile_bin_edges_dyn(int capacity, const int64_t* count, 
     if (e != cudaSuccess) { set_cuda_error(e, "tile_bin_edges memset"); return GSTEX_ERR_CUDA; }
     if (capacity == 0) return GSTEX_OK;
     GSTEX_REQUIRE(sorted);
-    bin_edges_kernel<<<ceil_div(capacity, 256), 256, 0, stream>>>(capacity, count, sorted, num_tiles, (int2*)bins);
+    bin_edges_kernel<int64_t><<<ceil_div(capacity, 256), 256, 0, stream>>>(capacity, count, sorted, 32, num_tiles,
+                                                                            (int2*)bins);
     return check_launch("get_tile_bin_edges_dyn");
+}
+
+extern "C" int gstex_get_tile_bin_edges32_dyn(int capacity, const int64_t* count, const uint32_t* sorted, int shift,
+                                              int num_tiles, int32_t* bins, gstex_stream_t s) {
+    GSTEX_REQUIRE(capacity >= 0 && num_tiles > 0 && bins && count && shift >= 0 && shift < 32);
+    cudaStream_t stream = (cudaStream_t)s;
+    cudaError_t e = cudaMemsetAsync(bins, 0, (size_t)num_tiles * 2 * sizeof(int32_t), stream);
+    if (e != cudaSuccess) { set_cuda_error(e, "tile_bin_edges32 memset"); return GSTEX_ERR_CUDA; }
+    if (capacity == 0) return GSTEX_OK;
+    GSTEX_REQUIRE(sorted);
+    bin_edges_kernel<uint32_t><<<ceil_div(capacity, 256), 256, 0, stream>>>(capacity, count, sorted, shift, num_tiles,
+                                                                             (int2*)bins);
+    return check_launch("get_tile_bin_edges32_dyn");
 }

@@ -131,6 +131,19 @@ int gstex_get_tile_bin_edges(int num_intersects, const int64_t* isect_ids_sorted
 int gstex_get_tile_bin_edges_dyn(int capacity, const int64_t* count, const int64_t* isect_ids_sorted,
                                  int num_tiles, int32_t* tile_bins, gstex_stream_t stream);
 
+/* Stable LSD radix sort of (uint32 key, int32 value) pairs on key bits
+ * [0, end_bit); with count non-NULL the number of items is read from device
+ * memory (clamped to n) and the call can be captured in a CUDA graph.
+ * Workspace: gstex_sort32_workspace_bytes(n).  Used by the depth-first
+ * batched binning (gstex_batch_emit_sorted). */
+size_t gstex_sort32_workspace_bytes(int n);
+int gstex_sort_pairs32(int n, const int64_t* count, int end_bit, const uint32_t* keys_in, const int32_t* vals_in,
+                       uint32_t* keys_out, int32_t* vals_out, void* workspace, size_t workspace_bytes,
+                       gstex_stream_t stream);
+/* Tile ranges of 32-bit sorted keys whose tile is key >> shift. */
+int gstex_get_tile_bin_edges32_dyn(int capacity, const int64_t* count, const uint32_t* keys_sorted, int shift,
+                                   int num_tiles, int32_t* tile_bins, gstex_stream_t stream);
+
 /* ---------------------------------------------------------------------
  * Textured compositor (texture_forward / texture_backward)
  * ------------------------------------------------------------------- */
@@ -300,6 +313,34 @@ int gstex_batch_emit(int num_points, int num_views, const void* views_dev, const
                      float glob_scale, const float* quats, int block_width, const int32_t* cum,
                      const int64_t* total, long long capacity, int64_t* keys, int32_t* gaussian_ids,
                      int64_t* count, int* overflow, gstex_stream_t stream);
+
+/* Depth-first binning, the order of gstex_batch_emit + a 64-bit sort from
+ * 32-bit sorts:
+ *   1. gstex_batch_project_keys: as gstex_batch_project, plus per pair j the
+ *      depth key (float bits of the camera depth; 0xffffffff without tiles),
+ *      pair_ids[j] = j and the tile rectangle rects [V*N, 2] (uint32 x0 | x1 << 16,
+ *      y0 | y1 << 16; 8-byte aligned);
+ *   2. gstex_sort_pairs32 of (depth_keys, pair_ids), end_bit 32 -> order;
+ *   3. gstex_batch_gather_counts(order) and gstex_inclusive_scan_i32 -> cum;
+ *   4. gstex_batch_emit_sorted: pair order[p] writes [cum[p-1], cum[p]) with
+ *      keys (global tile << 1 | 1) and its Gaussian id; slots it does not write
+ *      get (view's first tile << 1 | 0) and Gaussian 0, which sort first in that
+ *      tile like the reference's zero entries;
+ *   5. gstex_sort_pairs32 of (keys, gaussian_ids) with the emitted count,
+ *      end_bit 1 + bit_length(total_tiles), and gstex_get_tile_bin_edges32_dyn
+ *      with shift 1.
+ * The resulting gaussian_ids_sorted and tile_bins equal those of
+ * gstex_batch_emit + gstex_sort_pairs_dyn bit for bit; needs V * N < 2^31. */
+int gstex_batch_project_keys(int num_points, int num_views, const void* views_dev, const float* means,
+                             const float* scales, float glob_scale, const float* quats, const void* sh_coeffs,
+                             int sh_dtype, int sh_degree, int block_width, float* colors, int32_t* counts,
+                             uint32_t* depth_keys, int32_t* pair_ids, uint32_t* rects, gstex_stream_t stream);
+int gstex_batch_gather_counts(int n, const int32_t* order, const int32_t* counts, int32_t* out,
+                              gstex_stream_t stream);
+int gstex_batch_emit_sorted(int num_points, int num_views, const void* views_dev, const int32_t* order,
+                            const int32_t* cum, const uint32_t* rects, const int64_t* total, long long capacity,
+                            uint32_t* keys, int32_t* gaussian_ids, int64_t* count, int* overflow,
+                            gstex_stream_t stream);
 
 typedef struct gstex_batch_inputs {
     int num_points, num_views, block_width;

@@ -58,10 +58,55 @@ def test_batch_binning_bit_exact_per_view(setup):
         b = oracle.bin_and_sort(c, e, d, nt, cam.height, cam.width, 16)
         m = b["n_isect"]
         toff = int(sum(((cc.width + 15) // 16) * ((cc.height + 15) // 16) for cc in cams[:v]))
-        np.testing.assert_array_equal(ks[off:off + m] - (np.int64(toff) << 32), b["isect_ids_sorted"])
+        # keys are (global tile << 1 | real): the tile of every slot and the
+        # Gaussian order within each tile equal the reference's 64-bit sort
+        np.testing.assert_array_equal((ks[off:off + m].astype(np.int64) >> 1) - toff,
+                                      b["isect_ids_sorted"] >> 32)
         np.testing.assert_array_equal(gs[off:off + m], b["gaussian_ids_sorted"])
         off += m
     assert off == n
+
+
+def test_batch_binning_with_clipped_gaussians():
+    """A camera inside the cloud: Gaussians behind it whose mean projects into
+    the image get one tile and emit nothing, so their slots keep the
+    reference's zero entry (tile 0, Gaussian 0) and sort first in the view's
+    tile 0.  Tiles and Gaussian order of every view equal the oracle's."""
+    from gstex_cuda_gb300 import batch as B, synthetic
+    g = torch.Generator().manual_seed(17)
+    inside = synthetic.make_camera(torch.eye(4), 64, 48)
+    cams = synthetic.sphere_cameras(g, 2, radius=8.0, resolutions=[(64, 64), (80, 48)]) + [inside]
+    spec = synthetic._finish_with_area(g, torch.empty(1500, 3).uniform_(-3, 3, generator=g), 0.01, 0.1, 3, "normal",
+                                       cams, 15_000, "multi", {})
+    scene = B.Scene(means=spec.means.to(DEV), scales=spec.scales.to(DEV), quats=spec.quats.to(DEV),
+                    opacity=spec.opacity.to(DEV), sh_coeffs=spec.sh_coeffs.to(DEV), sh_degree=3,
+                    uv0=spec.uv0.to(DEV), umap=spec.umap.to(DEV), vmap=spec.vmap.to(DEV),
+                    texture_dims=spec.texture_dims.to(DEV), texture=spec.texture.to(DEV))
+    bcams = [B.Camera(c.viewmat, c.fx, c.fy, c.cx, c.cy, c.width, c.height) for c in cams]
+    r = B.BatchRenderer(bcams, spec.num_points, capacity=1 << 20)
+    r.bin(scene)
+    torch.cuda.synchronize()
+    ks = r.keys_sorted.cpu().numpy().astype(np.int64)
+    gs = r.gids_sorted.cpu().numpy()
+    n = int(r.count.item())
+    off = toff = 0
+    phantoms = 0
+    for v, cam in enumerate(cams):
+        c, e = oracle.get_aabb_2d(spec.means.numpy(), spec.scales.numpy(), 1.0, spec.quats.numpy(),
+                                  cam.viewmat.numpy(), cam.fx, cam.fy, cam.cx, cam.cy)
+        nt = oracle.num_tiles_hit(c, e, cam.height, cam.width, 16)
+        d = oracle.camera_depths(spec.means.numpy(), cam.viewmat.numpy())
+        b = oracle.bin_and_sort(c, e, d, nt, cam.height, cam.width, 16)
+        m = b["n_isect"]
+        phantoms += int(((nt > 0) & (e.max(-1) <= 1e-4)).sum())
+        np.testing.assert_array_equal((ks[off:off + m] >> 1) - toff, b["isect_ids_sorted"] >> 32)
+        np.testing.assert_array_equal(gs[off:off + m], b["gaussian_ids_sorted"])
+        ob = b["tile_bins"].reshape(-1, 2)
+        want = np.where((ob[:, 1] > ob[:, 0])[:, None], ob + off, 0)  # empty tiles stay (0, 0)
+        np.testing.assert_array_equal(r.bins.cpu().numpy()[toff:toff + len(ob)], want)
+        off += m
+        toff += ((cam.width + 15) // 16) * ((cam.height + 15) // 16)
+    assert off == n and phantoms > 0
 
 
 def test_batch_forward_backward_vs_oracle(setup):
