@@ -56,6 +56,8 @@ _BATCH_SIGS = {
     "gstex_sort32_workspace_bytes": (ctypes.c_size_t, [_I]),
     "gstex_sort_pairs32": (_I, [_I, _P, _I, _P, _P, _P, _P, _P, ctypes.c_size_t, _P]),
     "gstex_get_tile_bin_edges32_dyn": (_I, [_I, _P, _P, _I, _I, _P, _P]),
+    "gstex_batch_tile_order_workspace_bytes": (ctypes.c_size_t, [_I]),
+    "gstex_batch_tile_order": (_I, [_I, _P, _P, _P, ctypes.c_size_t, _P]),
     "gstex_batch_emit": (_I, [_I, _I, _P, _P, _P, _F, _P, _I, _P, _P, _LL, _P, _P, _P, _P, _P]),
     "gstex_sort_pairs_dyn": (_I, [_I, _P, _I, _P, _P, _P, _P, _P, ctypes.c_size_t, _P]),
     "gstex_get_tile_bin_edges_dyn": (_I, [_I, _P, _P, _I, _P, _P]),
@@ -121,7 +123,7 @@ class BatchRenderer:
     def __init__(self, cameras: Sequence[Camera], num_points: int, *, channels: int = 3, texture_dtype=torch.float32,
                  block_width: int = 16, settings: int = 1 << 8, background=(0.0, 0.0, 0.0), capacity: int = 0,
                  device="cuda:0", grid: int = 0, loss_weights: Optional[dict] = None, fwd_ppt: int = 1,
-                 bwd_ppt: int = 1, prebuilt_records: bool = True):
+                 bwd_ppt: int = 1, prebuilt_records: bool = True, heavy_first: bool = True):
         self.dev = torch.device(device)
         self.N = int(num_points)
         self.V = len(cameras)
@@ -184,6 +186,10 @@ class BatchRenderer:
         self.count = torch.zeros(1, **i64)
         self.overflow = torch.zeros(1, **i32)
         self.bins = torch.empty((self.total_tiles, 2), **i32)
+        # forward queue order: heaviest tiles first (the backward keeps tile order)
+        self.tile_order = torch.empty(self.total_tiles, **i32) if heavy_first else None
+        self.order_ws = (torch.empty(L.gstex_batch_tile_order_workspace_bytes(self.total_tiles), **u8)
+                         if heavy_first else None)
         self.queue = torch.zeros(1, **i32)
         self.bg = torch.tensor(list(background), **f32)
         # per-pixel outputs of all views
@@ -225,7 +231,8 @@ class BatchRenderer:
         bi.channels, bi.num_texels, bi.texture_dtype, bi.settings = self.C, s.texture.shape[0], self.texmode, \
             self.settings
         bi.total_tiles = self.total_tiles
-        bi.views, bi.tile_view, bi.tile_order = ptr(self.views_dev), ptr(self.tile_view), None
+        bi.views, bi.tile_view = ptr(self.views_dev), ptr(self.tile_view)
+        bi.tile_order = ptr(self.tile_order) if (self.tile_order is not None and not backward) else None
         bi.gaussian_ids_sorted, bi.tile_bins = ptr(self.gids_sorted), ptr(self.bins)
         bi.colors, bi.opacities, bi.means, bi.scales = ptr(self.colors), ptr(s.opacity), ptr(s.means), ptr(s.scales)
         bi.glob_scale = float(s.glob_scale)
@@ -271,6 +278,9 @@ class BatchRenderer:
                                    self.sort_ws.numel(), st), "sort_pairs32")
         check(L.gstex_get_tile_bin_edges32_dyn(self.capacity, ptr(self.count), ptr(self.keys_sorted), 1,
                                                self.total_tiles, ptr(self.bins), st), "tile_bin_edges32_dyn")
+        if self.tile_order is not None:
+            check(L.gstex_batch_tile_order(self.total_tiles, ptr(self.bins), ptr(self.tile_order), ptr(self.order_ws),
+                                           self.order_ws.numel(), st), "batch_tile_order")
         if self.records is not None:
             main.wait_event(self.ev_join)
 

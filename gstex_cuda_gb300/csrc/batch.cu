@@ -178,6 +178,18 @@ __global__ void batch_emit_sorted_kernel(int VN, int N, const BatchView* __restr
     }
 }
 
+// Queue order of the forward: tiles by decreasing intersection count (ties in
+// tile order), so the heaviest tiles do not start last and leave the end of
+// the persistent launch to a few CTAs.
+__global__ void tile_cost_keys_kernel(int T, const int2* __restrict__ bins, uint32_t* __restrict__ keys,
+                                      int32_t* __restrict__ ids) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= T) return;
+    const int2 b = bins[t];
+    keys[t] = ~(uint32_t)max(b.y - b.x, 0);
+    ids[t] = t;
+}
+
 // ---------------------------------------------------------------------------
 // Image losses of the reference demo (example.py:189-209) with their
 // gradients, over the concatenated pixels of all views:
@@ -393,6 +405,32 @@ extern "C" int gstex_batch_project_keys(int N, int V, const void* views_dev, con
     if (N > 0) GSTEX_REQUIRE(depth_keys && pair_ids && rects && ((uintptr_t)rects & 7) == 0);
     return project_impl(N, V, views_dev, means, scales, glob_scale, quats, sh_coeffs, sh_dtype, sh_degree,
                         block_width, colors, counts, depth_keys, pair_ids, (uint2*)rects, (cudaStream_t)s);
+}
+
+static size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+
+extern "C" size_t gstex_batch_tile_order_workspace_bytes(int total_tiles) {
+    const int n = total_tiles > 0 ? total_tiles : 1;
+    return 3 * align256((size_t)n * 4) + gstex_sort32_workspace_bytes(n);
+}
+
+extern "C" int gstex_batch_tile_order(int total_tiles, const int32_t* tile_bins, int32_t* order, void* workspace,
+                                      size_t workspace_bytes, gstex_stream_t s) {
+    GSTEX_REQUIRE(total_tiles >= 0);
+    if (total_tiles == 0) return GSTEX_OK;
+    GSTEX_REQUIRE(tile_bins && order && workspace && ((uintptr_t)workspace & 15) == 0);
+    if (workspace_bytes < gstex_batch_tile_order_workspace_bytes(total_tiles)) return GSTEX_ERR_CAPACITY;
+    const size_t a = align256((size_t)total_tiles * 4);
+    unsigned char* w = (unsigned char*)workspace;
+    uint32_t* keys = (uint32_t*)w;
+    int32_t* ids = (int32_t*)(w + a);
+    uint32_t* keys_sorted = (uint32_t*)(w + 2 * a);
+    tile_cost_keys_kernel<<<ceil_div(total_tiles, 256), 256, 0, (cudaStream_t)s>>>(total_tiles, (const int2*)tile_bins,
+                                                                                   keys, ids);
+    int rc = check_launch("batch_tile_order");
+    if (rc) return rc;
+    return gstex_sort_pairs32(total_tiles, nullptr, 32, keys, ids, keys_sorted, order, w + 3 * a,
+                              workspace_bytes - 3 * a, s);
 }
 
 extern "C" int gstex_batch_gather_counts(int n, const int32_t* order, const int32_t* counts, int32_t* out,

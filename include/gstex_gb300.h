@@ -342,6 +342,15 @@ int gstex_batch_emit_sorted(int num_points, int num_views, const void* views_dev
                             uint32_t* keys, int32_t* gaussian_ids, int64_t* count, int* overflow,
                             gstex_stream_t stream);
 
+/* Queue order of the global tiles by decreasing intersection count (ties in
+ * tile order) from tile_bins [total_tiles, 2]; pass it as in->tile_order to
+ * gstex_batch_forward so the heaviest tiles start first.  (The backward is
+ * faster in tile order: neighbouring tiles share splats in L2.)  Workspace:
+ * gstex_batch_tile_order_workspace_bytes(total_tiles), 16-byte aligned. */
+size_t gstex_batch_tile_order_workspace_bytes(int total_tiles);
+int gstex_batch_tile_order(int total_tiles, const int32_t* tile_bins, int32_t* order, void* workspace,
+                           size_t workspace_bytes, gstex_stream_t stream);
+
 typedef struct gstex_batch_inputs {
     int num_points, num_views, block_width;
     int channels, num_texels, texture_dtype, settings;

@@ -191,6 +191,26 @@ def test_plain_per_view_step_matches_batched_step(setup):
         assert np.abs(a - b).max() <= 1e-3 * (np.abs(b).max() + 1e-12), k
 
 
+def test_forward_tile_order_does_not_change_outputs(setup):
+    """The forward's heaviest-first queue order changes which CTA renders a
+    tile, not what it renders: outputs are bit-identical to tile order."""
+    from gstex_cuda_gb300 import batch as B
+    spec, cams, r, scene, _ = setup
+    bcams = [B.Camera(c.viewmat, c.fx, c.fy, c.cx, c.cy, c.width, c.height) for c in cams]
+    r2 = B.BatchRenderer(bcams, spec.num_points, capacity=1 << 20, fwd_ppt=r.fwd_ppt, bwd_ppt=r.bwd_ppt,
+                         heavy_first=False)
+    assert r.tile_order is not None and r2.tile_order is None
+    for x in (r, r2):
+        x.bin(scene)
+        x.forward(scene)
+    torch.cuda.synchronize()
+    order = r.tile_order.cpu().numpy()
+    cost = (r.bins[:, 1] - r.bins[:, 0]).cpu().numpy()
+    assert np.array_equal(np.sort(order), np.arange(r.total_tiles)) and np.all(np.diff(cost[order]) <= 0)
+    for k in ("img", "depth", "reg", "texture", "normal", "final_T", "final_idx", "depth_idx", "reg_s"):
+        assert np.array_equal(r.out[k].cpu().numpy(), r2.out[k].cpu().numpy()), k
+
+
 def test_batch_graph_replay_matches_eager(setup):
     spec, cams, r, scene, _ = setup
     P = r.total_pixels
