@@ -109,6 +109,45 @@ def test_batch_binning_with_clipped_gaussians():
     assert off == n and phantoms > 0
 
 
+def test_depth_first_binning_equals_64bit_binning(setup):
+    """The depth-first binning (32-bit sorts) and the 64-bit
+    (global tile << 32 | depth) emission + sort give the same
+    gaussian_ids_sorted and tile_bins, bit for bit."""
+    from gstex_cuda_gb300 import batch as B
+    from gstex_cuda_gb300._lib import check, ptr
+    spec, cams, r, scene, _ = setup
+    r.bin(scene)
+    L = B._L()
+    st = torch.cuda.current_stream().cuda_stream
+    VN, cap = r.V * r.N, r.capacity
+    i32 = dict(dtype=torch.int32, device=DEV)
+    i64 = dict(dtype=torch.int64, device=DEV)
+    cum = torch.empty(VN, **i32)
+    total = torch.zeros(1, **i64)
+    count = torch.zeros(1, **i64)
+    overflow = torch.zeros(1, **i32)
+    ws = torch.empty(L.gstex_scan_workspace_bytes(VN), dtype=torch.uint8, device=DEV)
+    keys = torch.empty(cap, **i64)
+    vals = torch.empty(cap, **i32)
+    ks = torch.empty(cap, **i64)
+    gs = torch.empty(cap, **i32)
+    sws = torch.empty(L.gstex_sort_workspace_bytes(cap), dtype=torch.uint8, device=DEV)
+    bins = torch.empty_like(r.bins)
+    check(L.gstex_inclusive_scan_i32(VN, ptr(r.counts), ptr(cum), ptr(total), ptr(ws), ws.numel(), st), "scan")
+    check(L.gstex_batch_emit(r.N, r.V, ptr(r.views_dev), ptr(scene.means), ptr(scene.scales), 1.0,
+                             ptr(scene.quats), r.bw, ptr(cum), ptr(total), cap, ptr(keys), ptr(vals), ptr(count),
+                             ptr(overflow), st), "emit")
+    check(L.gstex_sort_pairs_dyn(cap, ptr(count), 32 + int(r.total_tiles).bit_length(), ptr(keys), ptr(vals),
+                                 ptr(ks), ptr(gs), ptr(sws), sws.numel(), st), "sort")
+    check(L.gstex_get_tile_bin_edges_dyn(cap, ptr(count), ptr(ks), r.total_tiles, ptr(bins), st), "edges")
+    torch.cuda.synchronize()
+    n = int(count.item())
+    assert n == int(r.count.item())
+    assert torch.equal(gs[:n], r.gids_sorted[:n])
+    assert torch.equal(bins, r.bins)
+    assert torch.equal(ks[:n] >> 32, (r.keys_sorted[:n].to(torch.int64) >> 1))
+
+
 def test_batch_forward_backward_vs_oracle(setup):
     spec, cams, r, scene, loss = setup
     gs = r.gids_sorted.cpu().numpy()
