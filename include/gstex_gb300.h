@@ -134,13 +134,15 @@ int gstex_get_tile_bin_edges_dyn(int capacity, const int64_t* count, const int64
 /* Stable LSD radix sort of (uint32 key, int32 value) pairs on key bits
  * [0, end_bit); with count non-NULL the number of items is read from device
  * memory (clamped to n) and the call can be captured in a CUDA graph.
- * Workspace: gstex_sort32_workspace_bytes(n).  Used by the depth-first
- * batched binning (gstex_batch_emit_sorted). */
+ * Workspace: gstex_sort32_workspace_bytes(n).  The two sorts of the
+ * depth-first batched binning, which together replace the 64-bit sort of
+ * bin_and_sort_gaussians (gstex_cuda/utils.py:159-160). */
 size_t gstex_sort32_workspace_bytes(int n);
 int gstex_sort_pairs32(int n, const int64_t* count, int end_bit, const uint32_t* keys_in, const int32_t* vals_in,
                        uint32_t* keys_out, int32_t* vals_out, void* workspace, size_t workspace_bytes,
                        gstex_stream_t stream);
-/* Tile ranges of 32-bit sorted keys whose tile is key >> shift. */
+/* Tile ranges of 32-bit sorted keys whose tile is key >> shift; batched form
+ * of _C.get_tile_bin_edges (csrc/forward.cu:76-98). */
 int gstex_get_tile_bin_edges32_dyn(int capacity, const int64_t* count, const uint32_t* keys_sorted, int shift,
                                    int num_tiles, int32_t* tile_bins, gstex_stream_t stream);
 
@@ -315,7 +317,9 @@ int gstex_batch_emit(int num_points, int num_views, const void* views_dev, const
                      int64_t* count, int* overflow, gstex_stream_t stream);
 
 /* Depth-first binning, the order of gstex_batch_emit + a 64-bit sort from
- * 32-bit sorts:
+ * 32-bit sorts (batched form of get_aabb_2d + get_num_tiles_hit_2d +
+ * compute_cumulative_intersects + map_gaussian_to_intersects + the sort,
+ * gstex_cuda/utils.py:40-161, csrc/forward.cu:13-71):
  *   1. gstex_batch_project_keys: as gstex_batch_project, plus per pair j the
  *      depth key (float bits of the camera depth; 0xffffffff without tiles),
  *      pair_ids[j] = j and the tile rectangle rects [V*N, 2] (uint32 x0 | x1 << 16,
