@@ -86,3 +86,26 @@ def test_cpu_tensors_fail_loudly():
 def test_build_is_incremental():
     assert os.path.exists(build.build())
     assert not build._stale()
+
+
+def test_batch_layout_and_workspace_sizes_on_host():
+    """Host-only entry points of the batched path: the tile/pixel layout of a
+    camera set and the sizes of the caller-provided buffers."""
+    import ctypes
+    from gstex_cuda_gb300 import batch as B
+    L = B._L()
+    descs = (B.ViewDesc * 3)()
+    for d, (w, h) in zip(descs, [(1920, 1080), (512, 512), (33, 17)]):
+        d.width, d.height, d.fx, d.fy = w, h, w / 2.0, w / 2.0
+    tiles, pix = ctypes.c_int(0), ctypes.c_longlong(0)
+    assert L.gstex_batch_layout(3, descs, 16, ctypes.byref(tiles), ctypes.byref(pix)) == 0
+    assert tiles.value == 120 * 68 + 32 * 32 + 3 * 2
+    assert pix.value == 1920 * 1080 + 512 * 512 + 33 * 17
+    assert L.gstex_batch_layout(3, descs, 1, ctypes.byref(tiles), ctypes.byref(pix)) == 1  # block width < 2
+    descs[2].width = 0
+    assert L.gstex_batch_layout(3, descs, 16, ctypes.byref(tiles), ctypes.byref(pix)) == 1
+    # records: 224 bytes per (view, Gaussian); sorts: room for alternate keys and values
+    assert L.gstex_batch_records_bytes(1000, 4) == 1000 * 4 * 224
+    assert L.gstex_sort32_workspace_bytes(1 << 20) >= (1 << 20) * 8
+    assert L.gstex_sort_workspace_bytes(1 << 20) >= (1 << 20) * 12
+    assert L.gstex_batch_tile_order_workspace_bytes(96464) >= 96464 * 12 + L.gstex_sort32_workspace_bytes(96464)
