@@ -28,7 +28,7 @@ class RasterInputs(ctypes.Structure):
                 ("opacities", _P), ("means", _P), ("scales", _P), ("glob_scale", _F), ("quats", _P),
                 ("uv0", _P), ("umap", _P), ("vmap", _P), ("texture", _P), ("viewmat", _P),
                 ("fx", _F), ("fy", _F), ("cx", _F), ("cy", _F), ("settings", _I), ("background", _P),
-                ("pixels_per_thread", _I), ("records", _P)]
+                ("pixels_per_thread", _I), ("records", _P), ("group_lanes", _I)]
 
 
 class EditIO(ctypes.Structure):

@@ -42,7 +42,7 @@ class BatchInputs(ctypes.Structure):
                 ("views", _P), ("tile_view", _P), ("tile_order", _P), ("gaussian_ids_sorted", _P), ("tile_bins", _P),
                 ("colors", _P), ("opacities", _P), ("means", _P), ("scales", _P), ("glob_scale", _F), ("quats", _P),
                 ("uv0", _P), ("umap", _P), ("vmap", _P), ("texture_dims", _P), ("texture", _P), ("background", _P),
-                ("queue", _P), ("grid", _I), ("pixels_per_thread", _I), ("records", _P)]
+                ("queue", _P), ("grid", _I), ("pixels_per_thread", _I), ("records", _P), ("group_lanes", _I)]
 
 
 _BATCH_SIGS = {
@@ -123,7 +123,8 @@ class BatchRenderer:
     def __init__(self, cameras: Sequence[Camera], num_points: int, *, channels: int = 3, texture_dtype=torch.float32,
                  block_width: int = 16, settings: int = 1 << 8, background=(0.0, 0.0, 0.0), capacity: int = 0,
                  device="cuda:0", grid: int = 0, loss_weights: Optional[dict] = None, fwd_ppt: int = 1,
-                 bwd_ppt: int = 1, prebuilt_records: bool = True, heavy_first: bool = True):
+                 bwd_ppt: int = 1, fwd_group: int = 32, bwd_group: int = 32, prebuilt_records: bool = True,
+                 heavy_first: bool = True):
         self.dev = torch.device(device)
         self.N = int(num_points)
         self.V = len(cameras)
@@ -133,6 +134,7 @@ class BatchRenderer:
         self.texmode = 1 if texture_dtype == torch.bfloat16 else 0
         self.grid = int(grid)
         self.fwd_ppt, self.bwd_ppt = int(fwd_ppt), int(bwd_ppt)
+        self.fwd_group, self.bwd_group = int(fwd_group), int(bwd_group)
         self.lw = dict(LOSS_WEIGHTS if loss_weights is None else loss_weights)
         L = _L()
         descs = (ViewDesc * self.V)()
@@ -240,6 +242,7 @@ class BatchRenderer:
         bi.texture_dims, bi.texture, bi.background = ptr(s.texture_dims), ptr(s.texture), ptr(self.bg)
         bi.queue, bi.grid = ptr(self.queue), self.grid
         bi.pixels_per_thread = self.bwd_ppt if backward else self.fwd_ppt
+        bi.group_lanes = self.bwd_group if backward else self.fwd_group
         bi.records = ptr(self.records) if self.records is not None else None
         return bi
 
@@ -349,8 +352,9 @@ class BatchRenderer:
 
     # ------------------------------------------------------------------
     def autotune(self, s: Scene, tgt_img, tgt_tex, reps: int = 2) -> dict:
-        """Choose pixels-per-thread for the forward and the backward kernel by
-        timing each candidate on this scene and these cameras (CUDA events)."""
+        """Choose pixels-per-thread and lanes per splat walk (32, 16, 8, 4) of
+        the forward and of the backward kernel by timing each candidate on this
+        scene and these cameras (CUDA events)."""
         stream = torch.cuda.current_stream(self.dev)
         self.bin(s)
 
@@ -366,22 +370,23 @@ class BatchRenderer:
 
         result = {}
         best = None
-        for ppt in (1, 2):
-            self.fwd_ppt = ppt
+        for ppt, gs in ((1, 32), (2, 32), (1, 16), (1, 8), (1, 4)):
+            self.fwd_ppt, self.fwd_group = ppt, gs
             ms = timed(lambda: self.forward(s))
-            result[f"forward_ppt{ppt}_ms"] = ms
-            best = (ms, ppt) if best is None or ms < best[0] else best
-        self.fwd_ppt = best[1]
+            result[f"forward_ppt{ppt}_g{gs}_ms"] = ms
+            best = (ms, ppt, gs) if best is None or ms < best[0] else best
+        self.fwd_ppt, self.fwd_group = best[1], best[2]
         self.forward(s)
         self.image_loss(tgt_img, tgt_tex)
         best = None
-        for ppt in (1, 2):
-            self.bwd_ppt = ppt
+        for ppt, gs in ((1, 32), (2, 32), (1, 16), (1, 8), (1, 4)):
+            self.bwd_ppt, self.bwd_group = ppt, gs
             ms = timed(lambda: self.backward(s))
-            result[f"backward_ppt{ppt}_ms"] = ms
-            best = (ms, ppt) if best is None or ms < best[0] else best
-        self.bwd_ppt = best[1]
-        result.update(fwd_ppt=self.fwd_ppt, bwd_ppt=self.bwd_ppt)
+            result[f"backward_ppt{ppt}_g{gs}_ms"] = ms
+            best = (ms, ppt, gs) if best is None or ms < best[0] else best
+        self.bwd_ppt, self.bwd_group = best[1], best[2]
+        result.update(fwd_ppt=self.fwd_ppt, fwd_group=self.fwd_group, bwd_ppt=self.bwd_ppt,
+                      bwd_group=self.bwd_group)
         self.graph = None
         return result
 

@@ -538,7 +538,8 @@ extern "C" int gstex_batch_records(const gstex_batch_inputs* in, const int32_t* 
 
 static int grid_of(const gstex_batch_inputs* in, bool backward) {
     if (in->grid > 0) return in->grid;
-    int g = resident_ctas(in->block_width, backward, in->texture_dtype, in->channels, in->pixels_per_thread);
+    int g = resident_ctas(in->block_width, backward, in->texture_dtype, in->channels, in->pixels_per_thread,
+                          in->group_lanes);
     return g > 0 ? g : 152;
 }
 
@@ -555,8 +556,8 @@ extern "C" int gstex_batch_forward(const gstex_batch_inputs* in, const gstex_for
     if (e != cudaSuccess) { set_cuda_error(e, "batch_forward"); return GSTEX_ERR_CUDA; }
     FwdOut o{ (float3*)out->img, out->depth, out->reg, out->texture, (float3*)out->normal, out->final_T,
               out->final_idx, out->depth_idx, (float3*)out->reg_s };
-    return launch_fwd_batch(a, ba, o, in->block_width, in->texture_dtype, in->pixels_per_thread, grid_of(in, false),
-                            stream);
+    return launch_fwd_batch(a, ba, o, in->block_width, in->texture_dtype, in->pixels_per_thread, in->group_lanes,
+                            grid_of(in, false), stream);
 }
 
 extern "C" size_t gstex_batch_backward_workspace_bytes(int num_points) {
@@ -588,7 +589,7 @@ extern "C" int gstex_batch_backward(const gstex_batch_inputs* in, const gstex_ba
                io->v_depth, io->v_reg, io->v_alpha, io->v_texture, (const float3*)io->v_normal,
                (float*)io->workspace, io->v_tex_grad };
     if ((rc = launch_bwd_batch(a, ba, g, in->block_width, in->texture_dtype, in->pixels_per_thread,
-                               grid_of(in, true), stream)))
+                               in->group_lanes, grid_of(in, true), stream)))
         return rc;
     return launch_finalize(a, (const float*)io->workspace, io->v_opacity, io->v_means, io->v_scales, io->v_quats,
                            io->v_uv0, io->v_umap, io->v_vmap, stream);

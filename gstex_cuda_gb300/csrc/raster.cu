@@ -135,16 +135,44 @@ __device__ __forceinline__ void fetch3(const void* tex, const Bilerp& B, float c
 #ifndef GSTEX_WARP_BLOCK
 #define GSTEX_WARP_BLOCK 1
 #endif
-template <int PPT>
+//
+// Inside a warp's 8 x 4 block, GS < 32 splits the lanes into groups of GS
+// lanes, each covering a compact sub-block (16: two 4 x 4 halves; 8: four
+// 4 x 2 quarters; 4: eight 2 x 2 blocks).
+template <int PPT, int GS = 32>
 __device__ __forceinline__ int2 thread_pixel(int bw) {
 #if GSTEX_WARP_BLOCK
     if ((bw & 7) == 0) {
         const int tr = threadIdx.y * blockDim.x + threadIdx.x;
         const int lane = tr & 31, w = tr >> 5, wx = bw >> 3;
-        return make_int2(((w / wx) * 4 + (lane >> 3)) * PPT, (w % wx) * 8 + (lane & 7));
+        int col = lane & 7, row = lane >> 3;
+        if (GS == 4) {  // eight 2 x 2 blocks
+            const int g = lane >> 2, lg = lane & 3;
+            col = (g & 3) * 2 + (lg & 1);
+            row = (g >> 2) * 2 + (lg >> 1);
+        } else if (GS < 32) {
+            const int g = lane / GS, lg = lane % GS;
+            col = (g & 1) * 4 + (lg & 3);
+            row = (g >> 1) * (GS / 4) + (lg >> 2);
+        }
+        return make_int2(((w / wx) * 4 + row) * PPT, (w % wx) * 8 + col);
     }
 #endif
     return make_int2(threadIdx.y * PPT, threadIdx.x);
+}
+
+// Maximum / minimum over the GS-lane group of a full warp (GS a power of two).
+template <int GS>
+__device__ __forceinline__ int group_max(int v) {
+#pragma unroll
+    for (int o = GS / 2; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+template <int GS>
+__device__ __forceinline__ int group_min(int v) {
+#pragma unroll
+    for (int o = GS / 2; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
 }
 
 // Candidate list of one warp: the staged slots k in [k0, bsize), in order,
@@ -152,27 +180,29 @@ __device__ __forceinline__ int2 thread_pixel(int bw) {
 // splat left out is outside its alpha >= 1/255 box for every pixel of the
 // warp.  Returns the count; the entries are in wl[0, count).  The lanes of a
 // partial warp (tile widths that are not a multiple of 8) are its low lanes.
+__device__ __forceinline__ bool splat_meets_rect(const Recs& R, int kk, float rx0, float rx1, float ry0, float ry1) {
+    const float4 bx = R.hot[kk].box;
+    bool hit = !(bx.y < rx0 || bx.x > rx1 || bx.w < ry0 || bx.z > ry1);
+    if (hit && R.edge) {
+        // separating axes of the splat's quad: the rectangle's corner
+        // furthest inside each edge must be inside it
+        const RecEdge e = R.edge[kk];
+        const float ea[4] = { e.A.x, e.A.y, e.A.z, e.A.w }, eb[4] = { e.B.x, e.B.y, e.B.z, e.B.w };
+        const float ec[4] = { e.C.x, e.C.y, e.C.z, e.C.w };
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            hit = hit && ea[q] * (ea[q] > 0.f ? rx1 : rx0) + eb[q] * (eb[q] > 0.f ? ry1 : ry0) + ec[q] >= 0.f;
+    }
+    return hit;
+}
+
 __device__ __forceinline__ int build_list(uint8_t* wl, const Recs& R, int k0, int bsize, float rx0, float rx1,
                                           float ry0, float ry1, unsigned wmask, unsigned lane) {
     const int nl = __popc(wmask);
     int cnt = 0;
     for (int base = k0; base < bsize; base += nl) {
         const int kk = base + (int)lane;
-        bool hit = false;
-        if (kk < bsize) {
-            const float4 bx = R.hot[kk].box;
-            hit = !(bx.y < rx0 || bx.x > rx1 || bx.w < ry0 || bx.z > ry1);
-            if (hit && R.edge) {
-                // separating axes of the splat's quad: the rectangle's corner
-                // furthest inside each edge must be inside it
-                const RecEdge e = R.edge[kk];
-                const float ea[4] = { e.A.x, e.A.y, e.A.z, e.A.w }, eb[4] = { e.B.x, e.B.y, e.B.z, e.B.w };
-                const float ec[4] = { e.C.x, e.C.y, e.C.z, e.C.w };
-#pragma unroll
-                for (int q = 0; q < 4; q++)
-                    hit = hit && ea[q] * (ea[q] > 0.f ? rx1 : rx0) + eb[q] * (eb[q] > 0.f ? ry1 : ry0) + ec[q] >= 0.f;
-            }
-        }
+        const bool hit = kk < bsize && splat_meets_rect(R, kk, rx0, rx1, ry0, ry1);
         const unsigned m = __ballot_sync(wmask, hit);
         if (hit) wl[cnt + __popc(m & ((1u << lane) - 1u))] = (uint8_t)kk;
         cnt += __popc(m);
@@ -181,13 +211,44 @@ __device__ __forceinline__ int build_list(uint8_t* wl, const Recs& R, int k0, in
     return cnt;
 }
 
+// The same for the GS-lane group of a full warp that holds this lane: the
+// entries of the warp's list wl[0, cntw) (built with the warp's rectangle)
+// that are at or after slot k0 (k0 per group) and whose box and quad meet the
+// group's rectangle, in order.
+template <int GS>
+__device__ __forceinline__ int build_group_list(uint8_t* gl, const uint8_t* wl, int cntw, const Recs& R, int k0,
+                                                float rx0, float rx1, float ry0, float ry1, unsigned lane) {
+    const unsigned lg = lane & (GS - 1);
+    const unsigned gm = ((1u << GS) - 1u) << (lane & ~(unsigned)(GS - 1));
+    int cnt = 0;
+    for (int base = 0; base < cntw; base += GS) {
+        const int e = base + (int)lg;
+        const int kk = e < cntw ? wl[e] : 0;
+        const bool hit = e < cntw && kk >= k0 && splat_meets_rect(R, kk, rx0, rx1, ry0, ry1);
+        const unsigned m = __ballot_sync(0xffffffffu, hit) & gm;
+        if (hit) gl[cnt + __popc(m & ((1u << lane) - 1u))] = (uint8_t)kk;
+        cnt += __popc(m);
+    }
+    __syncwarp();
+    return cnt;
+}
+
 // ---------------------------------------------------------------------------
 // Forward body: one tile.  A block of bw x (bw / PPT) threads covers the
 // bw x bw tile; each thread owns PPT vertically adjacent pixels, so every
 // staged record read from shared memory is used for PPT pixels.
 // ---------------------------------------------------------------------------
-template <int TEXMODE, int CT, int PPT>
-__device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, const FwdOut& o, const Recs& R) {
+//
+// GS < 32 (full warps only): each group of GS lanes (a compact pixel block,
+// see thread_pixel) walks its own list of the staged slots whose screen box
+// meets the group's pixels, so a warp composites 32 / GS splats at once.  A
+// skipped splat can still end a pixel whose T is within 1/(1 - 1/255) of the
+// 1e-4 limit (texture.cu:213-221): a group with such a pixel walks every slot
+// of the batch from then on, in order, as the reference does.
+template <int TEXMODE, int CT, int PPT, int GS = 32>
+__device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, const FwdOut& o, const Recs& R,
+                                         uint8_t* lists) {
+    static_assert(GS == 32 || GS == 16 || GS == 8 || GS == 4, "group of 32, 16, 8 or 4 lanes");
     const int nthr = blockDim.x * blockDim.y;
     const int tr = threadIdx.y * blockDim.x + threadIdx.x;
     const int bw = blockDim.x;
@@ -209,8 +270,9 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
     const bool white_outline = a.settings & (1 << 24);
     const int C = CT >= 0 ? CT : a.C;
     constexpr int CA = CT > 0 ? CT : (CT == 0 ? 1 : kMaxChannels);
-    const int2 lp = thread_pixel<PPT>(bw);
+    const int2 lp = thread_pixel<PPT, GS>(bw);
     const int pj = J.tx * bw + lp.y;
+    const unsigned lane = tr & 31;
     PixelRay P[PPT];
     bool inside[PPT], done[PPT];
     float T[PPT], depth[PPT], reg[PPT];
@@ -234,6 +296,23 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
 #pragma unroll
         for (int k = 0; k < CA; k++) otex[p][k] = 0.f;
     }
+    // GS < 32: the warp's and the group's rectangles of pixel centres, lists
+    float rx0 = 0.f, rx1 = 0.f, ry0 = 0.f, ry1 = 0.f, qx0 = 0.f, qx1 = 0.f, qy0 = 0.f, qy1 = 0.f;
+    unsigned gmask = 0u;
+    uint8_t* wl = lists + (tr >> 5) * nthr;
+    uint8_t* gl = lists + ((size_t)ceil_div(nthr, 32) + tr / GS) * nthr;
+    if (GS < 32) {
+        const int pi0 = J.ty * bw + lp.x;
+        rx0 = (float)__reduce_min_sync(0xffffffffu, pj) + 0.5f;
+        rx1 = (float)__reduce_max_sync(0xffffffffu, pj) + 0.5f;
+        ry0 = (float)__reduce_min_sync(0xffffffffu, pi0) + 0.5f;
+        ry1 = (float)__reduce_max_sync(0xffffffffu, pi0 + PPT - 1) + 0.5f;
+        qx0 = (float)group_min<GS>(pj) + 0.5f;
+        qx1 = (float)group_max<GS>(pj) + 0.5f;
+        qy0 = (float)group_min<GS>(pi0) + 0.5f;
+        qy1 = (float)group_max<GS>(pi0 + PPT - 1) + 0.5f;
+        gmask = ((1u << GS) - 1u) << (lane & ~(unsigned)(GS - 1));
+    }
     const int2 range = J.range;
     const int nb = ceil_div(range.y - range.x, nthr);
 
@@ -245,16 +324,9 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
         __syncthreads();
         const int bsize = min(nthr, range.y - bstart);
         if (__all_sync(wmask, all_done)) continue;
-        // Every staged slot in order; each pixel tests the splat's box first.
-        for (int k = 0; k < bsize; ++k) {
-            const float4 bx = R.hot[k].box;
-            bool need = false;
-#pragma unroll
-            for (int p = 0; p < PPT; p++) {
-                const bool out_box = P[p].px < bx.x || P[p].px > bx.y || P[p].py < bx.z || P[p].py > bx.w;
-                need = need || (!done[p] && !(out_box && T[p] > 1.01e-4f));
-            }
-            if (need) {
+        // Composites staged slot k into this thread's pixels (those not done
+        // and, while T > 1.01e-4, inside the splat's alpha >= 1/255 box).
+        auto visit = [&](const int k) {
             const RecHot Hr = R.hot[k];
 #pragma unroll
             for (int p = 0; p < PPT; p++) {
@@ -323,12 +395,61 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
                 T[p] = next_T;
                 cur[p] = bstart + k;
             }
-            }
+        };
+        auto update_done = [&]() {
             bool ad = true;
 #pragma unroll
             for (int p = 0; p < PPT; p++) ad = ad && done[p];
             all_done = ad;
-            if (__all_sync(wmask, all_done)) break;
+        };
+        if (GS == 32) {
+            // Every staged slot in order; each pixel tests the splat's box first.
+            for (int k = 0; k < bsize; ++k) {
+                const float4 bx = R.hot[k].box;
+                bool need = false;
+#pragma unroll
+                for (int p = 0; p < PPT; p++) {
+                    const bool out_box = P[p].px < bx.x || P[p].px > bx.y || P[p].py < bx.z || P[p].py > bx.w;
+                    need = need || (!done[p] && !(out_box && T[p] > 1.01e-4f));
+                }
+                if (need) visit(k);
+                update_done();
+                if (__all_sync(wmask, all_done)) break;
+            }
+        } else {
+            // the group's slots whose box meets its pixels (warp list, then the
+            // group's filter of it), or every slot once a pixel is near 1e-4
+            auto near_done = [&]() {
+                bool nd = false;
+#pragma unroll
+                for (int p = 0; p < PPT; p++) nd = nd || (!done[p] && T[p] <= 1.01e-4f);
+                return nd;
+            };
+            const int cntw = build_list(wl, R, 0, bsize, rx0, rx1, ry0, ry1, 0xffffffffu, lane);
+            const int cnt = build_group_list<GS>(gl, wl, cntw, R, 0, qx0, qx1, qy0, qy1, lane);
+            bool dense = (__ballot_sync(0xffffffffu, near_done()) & gmask) != 0;
+            int j = 0, kd = -1;
+            while (true) {
+                int k;
+                bool act;
+                if (dense) {
+                    k = kd + 1;
+                    act = k < bsize;
+                } else {
+                    act = j < cnt;
+                    k = act ? gl[j] : 0;
+                }
+                if (!__any_sync(0xffffffffu, act)) break;
+                if (act) visit(k);
+                if (dense) kd = k;
+                else ++j;
+                update_done();
+                if (__all_sync(0xffffffffu, all_done)) break;
+                if (!dense && (__ballot_sync(0xffffffffu, act && near_done()) & gmask)) {
+                    dense = true;
+                    kd = k;
+                }
+            }
         }
     }
 #pragma unroll
@@ -355,11 +476,14 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
 // OFF, OFF/2, ..., 1: at each level a lane keeps the lower or the upper half
 // of its values (H = ceil(N/2) of them) and receives its partner's copy of
 // that half, one shuffle per kept value (N - 1 + log2 32 shuffles in all for
-// N <= 32).  Afterwards every lane holds one sum; slot() names the value
-// index it belongs to (N when the lane holds padding).
+// N <= 32).  Starting at OFF = 16 every lane ends with one sum; starting at
+// OFF = GS / 2 the reduction stays inside aligned groups of GS lanes and each
+// lane ends with OUT sums m[0, OUT).  slot(lane, j) names the value index
+// that m[j] belongs to (N when it holds padding).
 template <int N, int OFF>
 struct Ragged {
     static constexpr int H = (N + 1) / 2;
+    static constexpr int OUT = Ragged<H, OFF / 2>::OUT;
     static __device__ __forceinline__ void reduce(float* m, unsigned lane) {
         const bool upper = lane & OFF;
 #pragma unroll
@@ -372,8 +496,8 @@ struct Ragged {
         }
         Ragged<H, OFF / 2>::reduce(m, lane);
     }
-    static __device__ __forceinline__ int slot(unsigned lane) {
-        const int inner = Ragged<H, OFF / 2>::slot(lane);
+    static __device__ __forceinline__ int slot(unsigned lane, int j = 0) {
+        const int inner = Ragged<H, OFF / 2>::slot(lane, j);
         if (inner >= H) return N;
         const int idx = ((lane & OFF) ? H : 0) + inner;
         return idx < N ? idx : N;
@@ -381,10 +505,11 @@ struct Ragged {
 };
 template <int N>
 struct Ragged<N, 0> {
-    static_assert(N == 1, "five levels reduce at most 32 values to one");
+    static constexpr int OUT = N;
     static __device__ __forceinline__ void reduce(float*, unsigned) {}
-    static __device__ __forceinline__ int slot(unsigned) { return 0; }
+    static __device__ __forceinline__ int slot(unsigned, int j = 0) { return j; }
 };
+static_assert(Ragged<23, 16>::OUT == 1, "a full warp reduces 23 moments to one per lane");
 
 template <typename T>
 __device__ __forceinline__ T ld_or(const T* p, size_t i, T z) {
@@ -543,17 +668,28 @@ __device__ __forceinline__ void bwd_pair(const SceneArgs& a, const BwdArgs& g, c
     m[22] += kBlurFsq * v_sb * (Wm.uvs.w - P.py);
 }
 
-template <int TEXMODE, int CT, int PPT>
+// GS: lanes per splat walk.  32 = the warp walks one candidate list; 16, 8 or
+// 4 (full warps only) = each group of GS lanes (a compact pixel block, see
+// thread_pixel) walks its own list, so a warp works on 32 / GS splats at once
+// and a small splat occupies the lanes of the pixels it can reach, not a whole
+// warp.
+template <int TEXMODE, int CT, int PPT, int GS = 32>
 __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, const BwdArgs& g, const Recs& R,
                                          float* smom, uint8_t* lists, uint8_t* touched) {
+    static_assert(GS == 32 || GS == 16 || GS == 8 || GS == 4, "group of 32, 16, 8 or 4 lanes");
+    using Red = Ragged<kMoments, GS / 2>;
     const int nthr = blockDim.x * blockDim.y;
     const int tr = threadIdx.y * blockDim.x + threadIdx.x;
     const int bw = blockDim.x;
     const unsigned lane = tr & 31;
     const unsigned wmask = __activemask();
+    // candidate lists: one per warp, then (GS < 32) one per group
     uint8_t* wl = lists + (tr >> 5) * nthr;
+    uint8_t* gl = lists + ((size_t)ceil_div(nthr, 32) + tr / GS) * nthr;
     const bool full_warp = wmask == 0xffffffffu;
-    const int my_slot = Ragged<kMoments, 16>::slot(lane);
+    int my_slot[Red::OUT];
+#pragma unroll
+    for (int q = 0; q < Red::OUT; q++) my_slot[q] = Red::slot(lane, q);
     const View& V = J.V;
     const bool use_blur = a.settings & (1 << 9);
     const bool use_ndc = a.settings & (1 << 10);
@@ -562,7 +698,7 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
     const int C = CT >= 0 ? CT : a.C;
     constexpr int CA = CT > 0 ? CT : (CT == 0 ? 1 : kMaxChannels);
     const float3 z3 = make_float3(0.f, 0.f, 0.f);
-    const int2 lp = thread_pixel<PPT>(bw);
+    const int2 lp = thread_pixel<PPT, GS>(bw);
     const int pj = J.tx * bw + lp.y;
     BwdPix<CA> S[PPT];
     int my_bfin = -1;
@@ -586,12 +722,23 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
         s.vT_run = a.bg[0] * s.vout.x + a.bg[1] * s.vout.y + a.bg[2] * s.vout.z - valph;
         if (s.inside) my_bfin = max(my_bfin, s.bfin);
     }
-    const int warp_bfin = __reduce_max_sync(wmask, my_bfin);
-    // rectangle of the warp's pixel centres
-    const float rx0 = (float)__reduce_min_sync(wmask, pj) + 0.5f, rx1 = (float)__reduce_max_sync(wmask, pj) + 0.5f;
+    // last contributor and rectangle of the pixel centres of the warp, and
+    // (GS < 32) of the lane's group
     const int pi0 = J.ty * bw + lp.x;
+    const int warp_bfin = __reduce_max_sync(wmask, my_bfin);
+    const float rx0 = (float)__reduce_min_sync(wmask, pj) + 0.5f, rx1 = (float)__reduce_max_sync(wmask, pj) + 0.5f;
     const float ry0 = (float)__reduce_min_sync(wmask, pi0) + 0.5f;
     const float ry1 = (float)__reduce_max_sync(wmask, pi0 + PPT - 1) + 0.5f;
+    int group_bfin = warp_bfin;
+    float qx0 = rx0, qx1 = rx1, qy0 = ry0, qy1 = ry1;
+    if (GS < 32) {
+        group_bfin = group_max<GS>(my_bfin);
+        qx0 = (float)group_min<GS>(pj) + 0.5f;
+        qx1 = (float)group_max<GS>(pj) + 0.5f;
+        qy0 = (float)group_min<GS>(pi0) + 0.5f;
+        qy1 = (float)group_max<GS>(pi0 + PPT - 1) + 0.5f;
+    }
+    const unsigned gmask = (GS == 32) ? wmask : (((1u << GS) - 1u) << (lane & ~(unsigned)(GS - 1)));
 
     const int2 range = J.range;
     const int nb = ceil_div(range.y - range.x, nthr);
@@ -606,10 +753,18 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
         touched[tr] = 0;
         __syncthreads();
         // splats outside their alpha >= 1/255 box contribute nothing here:
-        // walk the warp's candidates, back to front
-        const int cnt = build_list(wl, R, max(0, bend - warp_bfin), bsize, rx0, rx1, ry0, ry1, wmask, lane);
-        for (int j = 0; j < cnt; ++j) {
-            const int k = wl[j];
+        // walk the candidates of the warp or group, back to front
+        const int cntw = build_list(wl, R, max(0, bend - warp_bfin), bsize, rx0, rx1, ry0, ry1, wmask, lane);
+        int cnt = cntw, cmax = cntw;
+        const uint8_t* list = wl;
+        if (GS < 32) {
+            cnt = build_group_list<GS>(gl, wl, cntw, R, max(0, bend - group_bfin), qx0, qx1, qy0, qy1, lane);
+            cmax = __reduce_max_sync(0xffffffffu, cnt);
+            list = gl;
+        }
+        for (int j = 0; j < cmax; ++j) {
+            const bool act = j < cnt;
+            const int k = act ? list[j] : 0;
             const int gidx = bend - k;
             {
                 const float4 bx = R.hot[k].box;
@@ -618,7 +773,7 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
                 for (int p = 0; p < PPT; p++)
                     need = need || (S[p].inside && gidx <= S[p].bfin &&
                                     !(S[p].P.px < bx.x || S[p].P.px > bx.y || S[p].P.py < bx.z || S[p].P.py > bx.w));
-                if (!__any_sync(wmask, need)) continue;
+                if (!__any_sync(wmask, act && need)) continue;
             }
             const RecHot Hr = R.hot[k];
             bool valid[PPT];
@@ -627,7 +782,7 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
             bool any = false;
 #pragma unroll
             for (int p = 0; p < PPT; p++) {
-                valid[p] = S[p].inside && gidx <= S[p].bfin && !outside_box(Hr, S[p].P);
+                valid[p] = act && S[p].inside && gidx <= S[p].bfin && !outside_box(Hr, S[p].P);
                 e[p] = eb[p] = alpha[p] = bf[p] = 0.f;
                 nbf[p] = 1.f;
                 if (valid[p]) {
@@ -658,13 +813,20 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
                     bwd_pair<TEXMODE, CT, CA>(a, g, R, k, gidx, Hr, H[p], alpha[p], e[p], eb[p], nbf[p], bf[p], S[p],
                                               C, use_ndc, prop_uv, bilinear, m);
             float* dst = smom + k * kMomSlot;
-            if (lane == 0) touched[k] = 1;
-            if (full_warp) {
-                Ragged<kMoments, 16>::reduce(m, lane);
-                if (my_slot < kMoments) atomicAdd(dst + my_slot, m[0]);
-            } else if (any) {
+            if (GS == 32 && !full_warp) {
+                if (lane == 0) touched[k] = 1;
+                if (any) {
 #pragma unroll
-                for (int q = 0; q < kMoments; q++) atomicAdd(dst + q, m[q]);
+                    for (int q = 0; q < kMoments; q++) atomicAdd(dst + q, m[q]);
+                }
+            } else {
+                Red::reduce(m, lane);
+                if (vmask & gmask) {
+                    if ((lane & (GS - 1)) == 0) touched[k] = 1;
+#pragma unroll
+                    for (int q = 0; q < Red::OUT; q++)
+                        if (my_slot[q] < kMoments) atomicAdd(dst + my_slot[q], m[q]);
+                }
             }
         }
         __syncthreads();
@@ -840,7 +1002,7 @@ __global__ void __launch_bounds__(256, 4) edit_view_kernel(SceneArgs a, ViewArgs
 #define FWD_BOUNDS(PPT) __launch_bounds__((PPT) == 2 ? 128 : 256, (PPT) == 2 ? GSTEX_FWD_MINB : GSTEX_FWD_MINB1)
 #define BWD_BOUNDS(PPT) __launch_bounds__((PPT) == 2 ? 128 : 256, (PPT) == 2 ? GSTEX_BWD_MINB : GSTEX_BWD_MINB1)
 
-template <int TEXMODE, int CT, int PPT>
+template <int TEXMODE, int CT, int PPT, int GS>
 __global__ void FWD_BOUNDS(PPT) fwd_view_kernel(SceneArgs a, ViewArgs va, FwdOut o) {
     extern __shared__ __align__(16) unsigned char smem[];
     TileJob J;
@@ -854,10 +1016,10 @@ __global__ void FWD_BOUNDS(PPT) fwd_view_kernel(SceneArgs a, ViewArgs va, FwdOut
     J.vc_stride = 3;
     J.recs = va.recs;
     const int nthr = blockDim.x * blockDim.y;
-    fwd_tile<TEXMODE, CT, PPT>(a, J, o, Recs::carve(smem, nthr, false));
+    fwd_tile<TEXMODE, CT, PPT, GS>(a, J, o, Recs::carve(smem, nthr, false), smem + (size_t)kRecBytes * nthr);
 }
 
-template <int TEXMODE, int CT, int PPT>
+template <int TEXMODE, int CT, int PPT, int GS>
 __global__ void BWD_BOUNDS(PPT) bwd_view_kernel(SceneArgs a, ViewArgs va, BwdArgs g) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int nthr = blockDim.x * blockDim.y;
@@ -872,9 +1034,9 @@ __global__ void BWD_BOUNDS(PPT) bwd_view_kernel(SceneArgs a, ViewArgs va, BwdArg
     J.vc_stride = 3;
     J.recs = va.recs;
     uint8_t* lists = smem + (size_t)(kRecBytes + kEdgeBytes + kMomSlot * sizeof(float)) * nthr;
-    bwd_tile<TEXMODE, CT, PPT>(a, J, g, Recs::carve(smem, nthr, true),
-                               reinterpret_cast<float*>(smem + (size_t)(kRecBytes + kEdgeBytes) * nthr), lists,
-                               lists + (size_t)ceil_div(nthr, 32) * nthr);
+    bwd_tile<TEXMODE, CT, PPT, GS>(a, J, g, Recs::carve(smem, nthr, true),
+                                   reinterpret_cast<float*>(smem + (size_t)(kRecBytes + kEdgeBytes) * nthr), lists,
+                                   lists + ((size_t)ceil_div(nthr, 32) + (GS < 32 ? ceil_div(nthr, GS) : 0)) * nthr);
 }
 
 __device__ __forceinline__ bool next_job(const BatchArgs& ba, int* s_tile, TileJob& J) {
@@ -900,17 +1062,18 @@ __device__ __forceinline__ bool next_job(const BatchArgs& ba, int* s_tile, TileJ
     return true;
 }
 
-template <int TEXMODE, int CT, int PPT>
+template <int TEXMODE, int CT, int PPT, int GS>
 __global__ void FWD_BOUNDS(PPT) fwd_batch_kernel(SceneArgs a, BatchArgs ba, FwdOut o) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_tile;
     TileJob J;
     const int nthr = blockDim.x * blockDim.y;
     const Recs R = Recs::carve(smem, nthr, false);
-    while (next_job(ba, &s_tile, J)) fwd_tile<TEXMODE, CT, PPT>(a, J, o, R);
+    uint8_t* lists = smem + (size_t)kRecBytes * nthr;
+    while (next_job(ba, &s_tile, J)) fwd_tile<TEXMODE, CT, PPT, GS>(a, J, o, R, lists);
 }
 
-template <int TEXMODE, int CT, int PPT>
+template <int TEXMODE, int CT, int PPT, int GS>
 __global__ void BWD_BOUNDS(PPT) bwd_batch_kernel(SceneArgs a, BatchArgs ba, BwdArgs g) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_tile;
@@ -919,8 +1082,8 @@ __global__ void BWD_BOUNDS(PPT) bwd_batch_kernel(SceneArgs a, BatchArgs ba, BwdA
     const Recs R = Recs::carve(smem, nthr, true);
     float* smom = reinterpret_cast<float*>(smem + (size_t)(kRecBytes + kEdgeBytes) * nthr);
     uint8_t* lists = smem + (size_t)(kRecBytes + kEdgeBytes + kMomSlot * sizeof(float)) * nthr;
-    uint8_t* touched = lists + (size_t)ceil_div(nthr, 32) * nthr;
-    while (next_job(ba, &s_tile, J)) bwd_tile<TEXMODE, CT, PPT>(a, J, g, R, smom, lists, touched);
+    uint8_t* touched = lists + ((size_t)ceil_div(nthr, 32) + (GS < 32 ? ceil_div(nthr, GS) : 0)) * nthr;
+    while (next_job(ba, &s_tile, J)) bwd_tile<TEXMODE, CT, PPT, GS>(a, J, g, R, smom, lists, touched);
 }
 
 // Writes the 32 records of a warp, assembled in shared memory (src), to
@@ -1118,44 +1281,68 @@ int fill_scene(const gstex_raster_inputs* in, SceneArgs& a, bool need_bins) {
 // Pixels per thread: 1 (block bw x bw) or 2 (block bw x bw/2, even bw only).
 int ppt_of(int bw, int requested) { return (requested == 2 && bw % 2 == 0) ? 2 : 1; }
 
-template <template <int, int, int> class Sel>
-static typename Sel<0, 0, 1>::type pick(int C, int texmode, int ppt) {
-    if (ppt == 2) {
-        if (C == 0) return Sel<0, 0, 2>::get();
-        if (C == 3) return texmode == 1 ? Sel<1, 3, 2>::get() : Sel<0, 3, 2>::get();
-        return Sel<0, -1, 2>::get();
+// Lanes per splat walk actually used: groups below 32 need block widths that
+// are multiples of 8 (full warps), one pixel per thread and 0 or 3 channels.
+int gs_of(int bw, int ppt, int C, int requested) {
+    if ((bw & 7) != 0 || ppt != 1 || (C != 0 && C != 3)) return 32;
+    return (requested == 16 || requested == 8 || requested == 4) ? requested : 32;
+}
+// Kernel variant of (channels, texel type, pixels per thread, lanes per splat
+// walk gs from gs_of): 1 or 2 pixels per thread with gs = 32; gs < 32 with
+// one pixel per thread and 0 or 3 channels.
+template <template <int, int, int, int> class Sel>
+static typename Sel<0, 0, 1, 32>::type pick(int C, int texmode, int ppt, int gs) {
+    if (gs == 16) {
+        if (C == 0) return Sel<0, 0, 1, 16>::get();
+        return texmode == 1 ? Sel<1, 3, 1, 16>::get() : Sel<0, 3, 1, 16>::get();
     }
-    if (C == 0) return Sel<0, 0, 1>::get();
-    if (C == 3) return texmode == 1 ? Sel<1, 3, 1>::get() : Sel<0, 3, 1>::get();
-    return Sel<0, -1, 1>::get();
+    if (gs == 8) {
+        if (C == 0) return Sel<0, 0, 1, 8>::get();
+        return texmode == 1 ? Sel<1, 3, 1, 8>::get() : Sel<0, 3, 1, 8>::get();
+    }
+    if (gs == 4) {
+        if (C == 0) return Sel<0, 0, 1, 4>::get();
+        return texmode == 1 ? Sel<1, 3, 1, 4>::get() : Sel<0, 3, 1, 4>::get();
+    }
+    if (ppt == 2) {
+        if (C == 0) return Sel<0, 0, 2, 32>::get();
+        if (C == 3) return texmode == 1 ? Sel<1, 3, 2, 32>::get() : Sel<0, 3, 2, 32>::get();
+        return Sel<0, -1, 2, 32>::get();
+    }
+    if (C == 0) return Sel<0, 0, 1, 32>::get();
+    if (C == 3) return texmode == 1 ? Sel<1, 3, 1, 32>::get() : Sel<0, 3, 1, 32>::get();
+    return Sel<0, -1, 1, 32>::get();
 }
 // Forward kernel: the alpha-visualisation variants (settings bit 16) come
-// with 1 pixel per thread and the generic fp32 or the bf16 texel path.
-template <template <int, int, int> class Sel>
-static typename Sel<0, 0, 1>::type pick_fwd(int C, int texmode, int& ppt, int settings) {
+// with 1 pixel per thread, gs = 32 and the generic fp32 or the bf16 texel path.
+template <template <int, int, int, int> class Sel>
+static typename Sel<0, 0, 1, 32>::type pick_fwd(int C, int texmode, int& ppt, int& gs, int settings) {
     if (settings & (1 << 16)) {
         ppt = 1;
-        return texmode == 1 ? Sel<3, 3, 1>::get() : Sel<2, -1, 1>::get();
+        gs = 32;
+        return texmode == 1 ? Sel<3, 3, 1, 32>::get() : Sel<2, -1, 1, 32>::get();
     }
-    return pick<Sel>(C, texmode, ppt);
+    return pick<Sel>(C, texmode, ppt, gs);
 }
-template <int M, int C, int P> struct FwdView { typedef void (*type)(SceneArgs, ViewArgs, FwdOut); static type get() { return fwd_view_kernel<M, C, P>; } };
-template <int M, int C, int P> struct BwdView { typedef void (*type)(SceneArgs, ViewArgs, BwdArgs); static type get() { return bwd_view_kernel<M, C, P>; } };
-template <int M, int C, int P> struct FwdBatch { typedef void (*type)(SceneArgs, BatchArgs, FwdOut); static type get() { return fwd_batch_kernel<M, C, P>; } };
-template <int M, int C, int P> struct BwdBatch { typedef void (*type)(SceneArgs, BatchArgs, BwdArgs); static type get() { return bwd_batch_kernel<M, C, P>; } };
+template <int M, int C, int P, int G> struct FwdView { typedef void (*type)(SceneArgs, ViewArgs, FwdOut); static type get() { return fwd_view_kernel<M, C, P, G>; } };
+template <int M, int C, int P, int G> struct BwdView { typedef void (*type)(SceneArgs, ViewArgs, BwdArgs); static type get() { return bwd_view_kernel<M, C, P, G>; } };
+template <int M, int C, int P, int G> struct FwdBatch { typedef void (*type)(SceneArgs, BatchArgs, FwdOut); static type get() { return fwd_batch_kernel<M, C, P, G>; } };
+template <int M, int C, int P, int G> struct BwdBatch { typedef void (*type)(SceneArgs, BatchArgs, BwdArgs); static type get() { return bwd_batch_kernel<M, C, P, G>; } };
 
 static dim3 block_of(int bw, int ppt) { return dim3(bw, bw / ppt); }
 static int threads_of(int bw, int ppt) { return bw * (bw / ppt); }
 // records, then (backward) the moment slots, then one candidate list per warp
-static size_t list_bytes(int bw, int ppt) {
+static size_t list_bytes(int bw, int ppt, int gs) {
     const int n = threads_of(bw, ppt);
-    return (size_t)ceil_div(n, 32) * n;
+    return ((size_t)ceil_div(n, 32) + (gs < 32 ? (size_t)ceil_div(n, gs) : 0)) * n;
 }
-size_t fwd_smem(int bw, int ppt) { return (size_t)kRecBytes * threads_of(bw, ppt); }
-size_t bwd_smem(int bw, int ppt) {
+size_t fwd_smem(int bw, int ppt, int gs) {
+    return (size_t)kRecBytes * threads_of(bw, ppt) + (gs < 32 ? list_bytes(bw, ppt, gs) : 0);
+}
+size_t bwd_smem(int bw, int ppt, int gs) {
     // ... then one "touched" flag per slot
     return ((size_t)kRecBytes + kEdgeBytes + kMomSlot * sizeof(float) + 1) * threads_of(bw, ppt) +
-           list_bytes(bw, ppt);
+           list_bytes(bw, ppt, gs);
 }
 
 int launch_finalize(const SceneArgs& a, const float* moments, float* v_opac, float* v_means, float* v_scales,
@@ -1167,38 +1354,45 @@ int launch_finalize(const SceneArgs& a, const float* moments, float* v_opac, flo
     return check_launch("finalize");
 }
 
-int launch_fwd_batch(const SceneArgs& a, const BatchArgs& ba, const FwdOut& o, int bw, int texmode, int ppt, int grid,
-                     cudaStream_t stream) {
+int launch_fwd_batch(const SceneArgs& a, const BatchArgs& ba, const FwdOut& o, int bw, int texmode, int ppt, int gs,
+                     int grid, cudaStream_t stream) {
     ppt = ppt_of(bw, ppt);
-    auto k = pick_fwd<FwdBatch>(a.C, texmode, ppt, a.settings);
-    int rc = set_smem(k, fwd_smem(bw, ppt), "batch forward");
+    gs = gs_of(bw, ppt, a.C, gs);
+    auto k = pick_fwd<FwdBatch>(a.C, texmode, ppt, gs, a.settings);
+    const size_t smem = fwd_smem(bw, ppt, gs);
+    int rc = set_smem(k, smem, "batch forward");
     if (rc) return rc;
-    k<<<grid, block_of(bw, ppt), fwd_smem(bw, ppt), stream>>>(a, ba, o);
+    k<<<grid, block_of(bw, ppt), smem, stream>>>(a, ba, o);
     return check_launch("batch forward");
 }
 
-int launch_bwd_batch(const SceneArgs& a, const BatchArgs& ba, const BwdArgs& g, int bw, int texmode, int ppt, int grid,
-                     cudaStream_t stream) {
+int launch_bwd_batch(const SceneArgs& a, const BatchArgs& ba, const BwdArgs& g, int bw, int texmode, int ppt, int gs,
+                     int grid, cudaStream_t stream) {
     ppt = ppt_of(bw, ppt);
-    auto k = pick<BwdBatch>(a.C, texmode, ppt);
-    int rc = set_smem(k, bwd_smem(bw, ppt), "batch backward");
+    gs = gs_of(bw, ppt, a.C, gs);
+    auto k = pick<BwdBatch>(a.C, texmode, ppt, gs);
+    const size_t smem = bwd_smem(bw, ppt, gs);
+    int rc = set_smem(k, smem, "batch backward");
     if (rc) return rc;
-    k<<<grid, block_of(bw, ppt), bwd_smem(bw, ppt), stream>>>(a, ba, g);
+    k<<<grid, block_of(bw, ppt), smem, stream>>>(a, ba, g);
     return check_launch("batch backward");
 }
 
-int resident_ctas(int bw, bool backward, int texmode, int C, int ppt) {
+int resident_ctas(int bw, bool backward, int texmode, int C, int ppt, int gs) {
     int n = 0;
     cudaError_t e;
     ppt = ppt_of(bw, ppt);
+    gs = gs_of(bw, ppt, C, gs);
     if (backward) {
-        auto k = pick<BwdBatch>(C, texmode, ppt);
-        if (set_smem(k, bwd_smem(bw, ppt), "occupancy")) return 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, threads_of(bw, ppt), bwd_smem(bw, ppt));
+        auto k = pick<BwdBatch>(C, texmode, ppt, gs);
+        const size_t smem = bwd_smem(bw, ppt, gs);
+        if (set_smem(k, smem, "occupancy")) return 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, threads_of(bw, ppt), smem);
     } else {
-        auto k = pick<FwdBatch>(C, texmode, ppt);
-        if (set_smem(k, fwd_smem(bw, ppt), "occupancy")) return 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, threads_of(bw, ppt), fwd_smem(bw, ppt));
+        auto k = pick<FwdBatch>(C, texmode, ppt, gs);
+        const size_t smem = fwd_smem(bw, ppt, gs);
+        if (set_smem(k, smem, "occupancy")) return 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, threads_of(bw, ppt), smem);
     }
     if (e != cudaSuccess) return 0;
     int dev = 0, sms = 0;
@@ -1267,9 +1461,11 @@ extern "C" int gstex_texture_forward(const gstex_raster_inputs* in, const gstex_
     cudaStream_t stream = (cudaStream_t)s;
     const dim3 grid(va.tiles_x, ceil_div(va.H, bw));
     int ppt = ppt_of(bw, in->pixels_per_thread);
-    auto k = pick_fwd<FwdView>(a.C, in->texture_dtype, ppt, a.settings);
-    if ((rc = set_smem(k, fwd_smem(bw, ppt), "texture_forward"))) return rc;
-    k<<<grid, block_of(bw, ppt), fwd_smem(bw, ppt), stream>>>(a, va, o);
+    int gs = gs_of(bw, ppt, a.C, in->group_lanes);
+    auto k = pick_fwd<FwdView>(a.C, in->texture_dtype, ppt, gs, a.settings);
+    const size_t smem = fwd_smem(bw, ppt, gs);
+    if ((rc = set_smem(k, smem, "texture_forward"))) return rc;
+    k<<<grid, block_of(bw, ppt), smem, stream>>>(a, va, o);
     return check_launch("texture_forward");
 }
 
@@ -1351,9 +1547,11 @@ extern "C" int gstex_texture_backward(const gstex_raster_inputs* in, const gstex
     va.vcolors = io->v_colors;
     const dim3 grid(va.tiles_x, ceil_div(va.H, bw));
     const int ppt = ppt_of(bw, in->pixels_per_thread);
-    auto k = pick<BwdView>(a.C, in->texture_dtype, ppt);
-    if ((rc = set_smem(k, bwd_smem(bw, ppt), "texture_backward"))) return rc;
-    k<<<grid, block_of(bw, ppt), bwd_smem(bw, ppt), stream>>>(a, va, g);
+    const int gs = gs_of(bw, ppt, a.C, in->group_lanes);
+    auto k = pick<BwdView>(a.C, in->texture_dtype, ppt, gs);
+    const size_t smem = bwd_smem(bw, ppt, gs);
+    if ((rc = set_smem(k, smem, "texture_backward"))) return rc;
+    k<<<grid, block_of(bw, ppt), smem, stream>>>(a, va, g);
     if ((rc = check_launch("texture_backward"))) return rc;
     return launch_finalize(a, (const float*)io->workspace, io->v_opacity, io->v_means, io->v_scales, io->v_quats,
                            io->v_uv0, io->v_umap, io->v_vmap, stream);

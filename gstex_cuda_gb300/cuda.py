@@ -180,6 +180,12 @@ def _texture_mode(texture, channels):
 
 
 PIXELS_PER_THREAD = 1  # 1 or 2 (2 halves the threads per tile; even block widths only)
+# Lanes that walk one list of staged splats in texture_forward /
+# texture_backward: 32 (a warp's 8x4 pixel block), 16 (4x4), 8 (4x2) or 4
+# (2x2); below 32 only for block widths that are multiples of 8, one pixel per
+# thread and 0 or 3 channels (else 32).
+FORWARD_GROUP_LANES = 32
+BACKWARD_GROUP_LANES = 32
 # texture_forward / texture_backward build one splat record per Gaussian of the
 # view first (gstex_view_records) and the tiles copy them; False: every tile
 # derives the records of its Gaussians itself.
@@ -247,6 +253,7 @@ def texture_forward(tile_bounds, block, img_size, texture_info, texture_dims, ga
     ri, C = _raster_inputs(W, H, bw, texture_info, texture_dims, gaussian_ids_sorted, tile_bins, colors, opacities,
                            means, scales, glob_scale, quats, uv0, umap, vmap, texture, viewmat, fx, fy, cx, cy,
                            settings, background)
+    ri.group_lanes = int(FORWARD_GROUP_LANES)
     dev = means.device
     f32 = dict(dtype=torch.float32, device=dev)
     out_img = torch.empty((H, W, 3), **f32)
@@ -274,6 +281,7 @@ def texture_backward(img_height, img_width, block_width, texture_info, texture_d
     ri, C = _raster_inputs(img_width, img_height, block_width, texture_info, texture_dims, gaussian_ids_sorted,
                            tile_bins, colors, opacities, means, scales, glob_scale, quats, uv0, umap, vmap, texture,
                            viewmat, fx, fy, cx, cy, settings, background)
+    ri.group_lanes = int(BACKWARD_GROUP_LANES)
     ups = [("final_Ts", final_Ts), ("final_idx", final_idx), ("depth_idx", depth_idx), ("final_s", final_s),
            ("v_output", v_output), ("v_output_depth", v_output_depth), ("v_output_reg", v_output_reg),
            ("v_output_alpha", v_output_alpha), ("v_output_texture", v_output_texture),

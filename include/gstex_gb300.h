@@ -180,6 +180,13 @@ typedef struct gstex_raster_inputs {
      * of its Gaussians itself.  Read by texture_forward / texture_backward,
      * not by texture_edit. */
     const void* records;
+    /* Lanes of the launched compositor kernel (texture_forward or
+     * texture_backward) that walk one list of staged splats: 32 (a warp's
+     * 8x4 pixel block), 16 (4x4), 8 (4x2) or 4 (2x2); 0 = 32.  Values below
+     * 32 apply to block widths that are multiples of 8, one pixel per thread
+     * and 0 or 3 channels; elsewhere 32 is used.  Results do not depend on
+     * it beyond float summation order. */
+    int group_lanes;
 } gstex_raster_inputs;
 
 /* Bytes of the records buffer of one view: 224 per Gaussian plus the list
@@ -381,6 +388,8 @@ typedef struct gstex_batch_inputs {
     int pixels_per_thread;              /* 0 = default (1); 2 needs an even block width */
     const void* records;                /* optional: gstex_batch_records output (16-byte aligned);
                                            null = each tile derives the records it stages */
+    int group_lanes;                    /* lanes per splat walk of the launched kernel
+                                           (see gstex_raster_inputs) */
 } gstex_batch_inputs;
 
 /* Bytes of the per-(view, Gaussian) splat records of gstex_batch_records

@@ -10,7 +10,8 @@ pytestmark = pytest.mark.gpu
 DEV = "cuda:0"
 
 
-@pytest.fixture(scope="module", params=[(1, 1), (2, 2)], ids=["1px", "2px"])
+@pytest.fixture(scope="module", params=[(1, 1, 32), (2, 2, 32), (1, 1, 16), (1, 1, 8), (1, 1, 4)],
+                ids=["1px", "2px", "1px_g16", "1px_g8", "1px_g4"])
 def setup(request):
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
@@ -25,7 +26,7 @@ def setup(request):
                     texture_dims=spec.texture_dims.to(DEV), texture=spec.texture.to(DEV))
     bcams = [B.Camera(c.viewmat, c.fx, c.fy, c.cx, c.cy, c.width, c.height) for c in cams]
     r = B.BatchRenderer(bcams, spec.num_points, capacity=1 << 20, fwd_ppt=request.param[0],
-                        bwd_ppt=request.param[1])
+                        bwd_ppt=request.param[1], fwd_group=request.param[2], bwd_group=request.param[2])
     P = r.total_pixels
     gen = torch.Generator().manual_seed(1)
     tgt_img = torch.rand(P, 3, generator=gen).to(DEV)
@@ -237,7 +238,7 @@ def test_forward_tile_order_does_not_change_outputs(setup):
     spec, cams, r, scene, _ = setup
     bcams = [B.Camera(c.viewmat, c.fx, c.fy, c.cx, c.cy, c.width, c.height) for c in cams]
     r2 = B.BatchRenderer(bcams, spec.num_points, capacity=1 << 20, fwd_ppt=r.fwd_ppt, bwd_ppt=r.bwd_ppt,
-                         heavy_first=False)
+                         fwd_group=r.fwd_group, bwd_group=r.bwd_group, heavy_first=False)
     assert r.tile_order is not None and r2.tile_order is None
     for x in (r, r2):
         x.bin(scene)
@@ -248,6 +249,27 @@ def test_forward_tile_order_does_not_change_outputs(setup):
     assert np.array_equal(np.sort(order), np.arange(r.total_tiles)) and np.all(np.diff(cost[order]) <= 0)
     for k in ("img", "depth", "reg", "texture", "normal", "final_T", "final_idx", "depth_idx", "reg_s"):
         assert np.array_equal(r.out[k].cpu().numpy(), r2.out[k].cpu().numpy()), k
+
+
+def test_forward_group_walk_does_not_change_outputs(setup):
+    """Lanes per splat walk of the forward (32: every slot in order, each
+    pixel testing the splat's box; 16 / 8 / 4: each lane group walks the
+    slots whose box meets its pixels, or every slot once a pixel's T nears
+    1e-4) change which lanes run together, not what a pixel composites: the
+    outputs are bit-identical."""
+    from gstex_cuda_gb300 import batch as B
+    spec, cams, r, scene, _ = setup
+    bcams = [B.Camera(c.viewmat, c.fx, c.fy, c.cx, c.cy, c.width, c.height) for c in cams]
+    outs = {}
+    for gs in (32, 16, 8, 4):
+        x = B.BatchRenderer(bcams, spec.num_points, capacity=1 << 20, fwd_group=gs)
+        x.bin(scene)
+        x.forward(scene)
+        torch.cuda.synchronize()
+        outs[gs] = {k: v.cpu().numpy() for k, v in x.out.items()}
+    for gs in (16, 8, 4):
+        for k in outs[32]:
+            assert np.array_equal(outs[gs][k], outs[32][k]), (gs, k)
 
 
 def test_batch_graph_replay_matches_eager(setup):
@@ -275,7 +297,7 @@ def test_prebuilt_records_match_per_tile_records(setup):
     spec, cams, r, scene, loss = setup
     bcams = [B.Camera(c.viewmat, c.fx, c.fy, c.cx, c.cy, c.width, c.height) for c in cams]
     r2 = B.BatchRenderer(bcams, spec.num_points, capacity=1 << 20, fwd_ppt=r.fwd_ppt, bwd_ppt=r.bwd_ppt,
-                         prebuilt_records=False)
+                         fwd_group=r.fwd_group, bwd_group=r.bwd_group, prebuilt_records=False)
     gen = torch.Generator().manual_seed(1)
     tgt_img = torch.rand(r.total_pixels, 3, generator=gen).to(DEV)
     tgt_tex = torch.rand(r.total_pixels, 3, generator=gen).to(DEV)

@@ -211,13 +211,16 @@ def test_raster_tiny_matches_reference_golden():
         assert err < 2e-4, (k, err)
 
 
-@pytest.fixture(params=[1, 2], ids=["1px", "2px"])
+@pytest.fixture(params=[(1, 32), (2, 32), (1, 16), (1, 8), (1, 4)], ids=["1px", "2px", "1px_g16", "1px_g8", "1px_g4"])
 def pixels_per_thread(request):
+    """Pixels per thread, and lanes per splat walk of both compositor kernels
+    (group sizes below 32 apply to block widths that are multiples of 8)."""
     import gstex_cuda_gb300.cuda as C
-    old = C.PIXELS_PER_THREAD
-    C.PIXELS_PER_THREAD = request.param
-    yield request.param
-    C.PIXELS_PER_THREAD = old
+    old = C.PIXELS_PER_THREAD, C.FORWARD_GROUP_LANES, C.BACKWARD_GROUP_LANES
+    ppt, gs = request.param
+    C.PIXELS_PER_THREAD, C.FORWARD_GROUP_LANES, C.BACKWARD_GROUP_LANES = ppt, gs, gs
+    yield ppt
+    C.PIXELS_PER_THREAD, C.FORWARD_GROUP_LANES, C.BACKWARD_GROUP_LANES = old
 
 
 @pytest.mark.parametrize("w,h,bw", [(64, 64, 16), (48, 32, 16), (70, 45, 8), (33, 29, 5), (40, 30, 10)])
