@@ -57,7 +57,13 @@ def parse():
     p.add_argument("--no-plain", action="store_true", help="skip the plain per-view fp32 comparison")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-refkern", action="store_true", help="skip timing the reference's kernels per view")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--no-autotune", action="store_true",
+                   help="use the kernel variants given by --fwd-group/--bwd-group (profiling runs)")
+    p.add_argument("--fwd-group", type=int, default=32)
+    p.add_argument("--bwd-group", type=int, default=32)
+    p.add_argument("--no-graph", action="store_true")
     return p.parse_args()
 
 
@@ -164,37 +170,61 @@ def job_frames_per_s(world: int, views: int, steps: int, elapsed_max: float) -> 
     return world * views * steps / elapsed_max
 
 
-def traffic_per_intersection():
-    """DRAM bytes per intersection of the compositor kernels, measured with ncu
-    on a smaller case of the same workload (the committed profile summary); the full
-    launch's traffic is that times its intersections."""
-    import re
-    out = {}
-    try:
-        with open(os.path.join(HERE, "profiles", "compositor_dram_traffic_4views.txt")) as f:
-            for line in f:
-                m = re.match(r"^\| (forward|backward) \|.*\| ([0-9.]+) \|$", line.strip())
-                if m:
-                    out[m.group(1)] = float(m.group(2))
-    except OSError:
-        pass
-    return out
+def reference_kernels_leg(spec, dev, steps, warmup=1):
+    """frames/s of the reference's own kernels run the way its callers run
+    them (one view after another in fp32: SH colours, AABBs, tile counts,
+    the host-synchronising intersection count, emission, torch.sort, tile
+    ranges, texture_forward, the demo's image losses by elementwise torch,
+    texture_backward, the SH adjoint) on the same scene, timed by wall clock
+    around whole steps.  The kernels are the reference's, compiled from its
+    sources into cubins (oracle/refkern); None when those are absent."""
+    import torch
+    from oracle import refkern as R
+    from gstex_cuda_gb300.batch import LOSS_WEIGHTS
+    if not R.available():
+        return None
+    t = {k: getattr(spec, k2).contiguous().to(dev) for k, k2 in
+         (("means", "means"), ("scales", "scales"), ("quats", "quats"), ("opacity", "opacity"), ("uv0", "uv0"),
+          ("umap", "umap"), ("vmap", "vmap"), ("dims", "texture_dims"))}
+    t["texture"] = spec.texture.float().contiguous().to(dev)
+    t["sh"] = spec.sh_coeffs.float().contiguous().to(dev)
+    gen = torch.Generator().manual_seed(11)
+    tgts = [(torch.rand(c.height, c.width, 3, generator=gen).to(dev),
+             torch.rand(c.height, c.width, 3, generator=gen).to(dev)) for c in spec.cameras]
+
+    def step():
+        for v, cam in enumerate(spec.cameras):
+            f = R.view_forward(t, cam, spec.sh_degree)
+            ups = R.image_loss_grads(f["out"], tgts[v][0], tgts[v][1], LOSS_WEIGHTS)
+            R.view_backward(t, cam, spec.sh_degree, f, ups)
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    torch.cuda.synchronize(dev)
+    el = time.perf_counter() - t0
+    del t, tgts
+    torch.cuda.empty_cache()
+    return len(spec.cameras) * steps / el
 
 
-def reference_kernels_plain_fps():
-    """frames/s of the reference's own kernels run per view in fp32 on the
-    batched scene, from the committed measurement (the reference's kernels
-    are test infrastructure and do not run inside this benchmark)."""
-    import re
-    try:
-        with open(os.path.join(HERE, "profiles", "reference_kernels_plain_32views.md")) as f:
-            for line in f:
-                m = re.match(r"^\| reference kernels, plain per-view fp32 \| ([0-9.]+) \|", line.strip())
-                if m:
-                    return float(m.group(1))
-    except OSError:
-        pass
-    return None
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one compositor
+# launch on the full 32-view workload, from a single-pass ncu capture of that
+# launch (profiles/compositor_dram_traffic_32views.md gives the command and
+# the raw figures).  Keyed by kernel; used only for the default workload.
+DRAM_BYTES_PER_LAUNCH = {}
+TRAFFIC_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch, 32-view workload"
+
+
+def dram_traffic_model(kernel, workload="batched", views=32):
+    """Measured DRAM bytes of one launch of `kernel` on the default workload,
+    or None (other workloads, or no capture of this build)."""
+    if workload != "batched" or views != 32:
+        return None
+    return DRAM_BYTES_PER_LAUNCH.get(kernel)
 
 
 def algorithmic_bytes(I, tiles, T, P, C, N, tex_bytes_per_texel, grad_texel_bytes, backward):
@@ -322,7 +352,12 @@ def main():
         torch.cuda.synchronize(dev)
     I = r.intersections()
     log(f"intersections {I}, pixels {P}, tiles {r.total_tiles}, capacity {r.capacity}")
-    tuned = r.autotune(scene, tgt_img, tgt_tex)
+    if args.no_autotune:
+        r.fwd_group, r.bwd_group = args.fwd_group, args.bwd_group
+        tuned = {"fixed": True, "fwd_ppt": r.fwd_ppt, "fwd_group": r.fwd_group, "bwd_ppt": r.bwd_ppt,
+                 "bwd_group": r.bwd_group}
+    else:
+        tuned = r.autotune(scene, tgt_img, tgt_tex)
     log(f"autotune: {tuned}")
 
     # timed region: eager steps (one launch per stage), CUDA events around the
@@ -366,6 +401,8 @@ def main():
     # graph replay of the same step (launch overhead removed)
     graph_fps = None
     try:
+        if args.no_graph:
+            raise RuntimeError("skipped (--no-graph)")
         r.capture(scene, tgt_img, tgt_tex)
         for _ in range(2):
             r.replay()
@@ -419,6 +456,15 @@ def main():
             plain = f"unavailable: {type(ex).__name__}: {ex}"
         log(f"plain fp32 per-view: {plain}")
 
+    # the reference's own kernels on the same scene, plain per view in fp32
+    ref_plain = None
+    if not args.no_refkern:
+        try:
+            ref_plain = reference_kernels_leg(spec, dev, max(1, args.steps // 5))
+        except Exception as ex:
+            ref_plain = f"unavailable: {type(ex).__name__}: {ex}"
+        log(f"reference kernels plain fp32 per-view: {ref_plain}")
+
     # roofline of the dominant compositor kernel
     T = spec.num_texels
     N = spec.num_points
@@ -428,11 +474,7 @@ def main():
     peak, peak_kind = measured_peak_hbm()
     dom = ("backward", bb, bwd_ms) if bwd_ms >= fwd_ms else ("forward", fb, fwd_ms)
     achieved = dom[1] / (dom[2] / 1000.0) / 1e9
-    # the measured bytes per intersection belong to the batched scene
-    tpi = traffic_per_intersection().get(dom[0]) if args.workload == "batched" else None
-    traffic = tpi * I if tpi else None
-
-    ref_plain = reference_kernels_plain_fps() if args.workload == "batched" and nviews == 32 else None
+    traffic = dram_traffic_model(dom[0], args.workload, nviews)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -459,16 +501,18 @@ def main():
                 "e2e": e2e, "gpu_launches": int(launches),
                 "roofline": {"bound": "hbm", "kernel": dom[0], "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
-                             "traffic_source": "ncu dram bytes per intersection (4-view case) x intersections",
+                             "traffic_source": TRAFFIC_SOURCE if traffic is not None else None,
                              "algorithmic_bytes_per_launch": dom[1], "kernel_ms": dom[2]},
                 "kernels_ms": {"forward": fwd_ms, "backward": bwd_ms},
                 "graph_frames_per_s": graph_fps,
                 "plain_fp32_frames_per_s": plain,
                 "speedup_vs_plain_fp32": (value / plain) if isinstance(plain, float) else None,
                 "reference_kernels_plain_fp32_frames_per_s": ref_plain,
-                "speedup_vs_reference_kernels_plain_fp32": (value / ref_plain) if ref_plain else None,
-                "reference_kernels_source": "profiles/reference_kernels_plain_32views.md (same scene, same GPU model, "
-                                            "oracle/refkern/time_plain.py)" if ref_plain else None,
+                "speedup_vs_reference_kernels_plain_fp32": (value / ref_plain) if isinstance(ref_plain, float)
+                else None,
+                "reference_kernels_source": ("the reference's texture_forward/backward, AABB, binning and SH kernels "
+                                             "(cubins from its sources), one fp32 view after another, measured in "
+                                             "this run after the timed region") if ref_plain is not None else None,
                 "cpu_baseline": cpu, "clocks": clk}
         print(json.dumps(line), flush=True)
     if world > 1:

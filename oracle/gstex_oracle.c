@@ -635,8 +635,9 @@ int FN(texture_backward)(int tiles_x, int tiles_y, int bw, int img_w, int img_h,
             const REAL* vt = v_tex + pix * C;
             v3 bgv = { bg[0], bg[1], bg[2] };
             REAL vT_run = dot3(bgv, vout) - valpha;
-            for (int idx = re - 1; idx >= rs; idx--) {
-                if (idx > bfin) continue;
+            /* entries after the pixel's last contributor are skipped
+               (texture.cu:483-487): start the walk at it */
+            for (int idx = (bfin < re - 1 ? bfin : re - 1); idx >= rs; idx--) {
                 const int g = gids[idx];
                 v3 mean = { means[3 * g], means[3 * g + 1], means[3 * g + 2] };
                 REAL sx = scales[3 * g], sy = scales[3 * g + 1];

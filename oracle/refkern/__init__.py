@@ -335,3 +335,77 @@ def bin_and_sort(num_points, centers, extents, depths, counts, tile_bounds, bloc
     gids_sorted = torch.gather(gids, 0, order)
     bins = get_tile_bin_edges(n, isect_sorted, tile_bounds)
     return n, isect_sorted, gids_sorted, bins
+
+
+# ---------------------------------------------------------------------------
+# One view the way a caller of the reference renders it (restated glue of
+# example.py:121-209: SH colours, AABBs, depths, tile counts, host-synchronising
+# binning, texture_forward; texture_backward and the SH adjoint), used by the
+# full-size batched parity test and by the benchmark's timing of the
+# reference's plain per-view fp32 path.
+# ---------------------------------------------------------------------------
+def view_forward(t, cam, sh_degree, block_width=16, settings=1 << 8, background=None, binning=None):
+    """t: dict of float32 / int32 CUDA tensors means, scales, quats, opacity,
+    uv0, umap, vmap, dims, texture [T, C], sh [N, B, 3]; cam: a camera with
+    viewmat, c2w (CPU [4, 4]), fx, fy, cx, cy, width, height.  Returns a dict
+    with the view's colours, binning (n, gids_sorted, bins, tile_bounds),
+    inputs of texture_backward and the nine forward outputs.  binning =
+    (gaussian_ids_sorted, tile_bins) replaces the reference's own binning
+    (the compositor kernels then run on the given lists)."""
+    dev = t["means"].device
+    N = t["means"].shape[0]
+    H, W, bw = cam.height, cam.width, block_width
+    vm = cam.viewmat.contiguous().to(dev)
+    c2w = cam.c2w.contiguous().to(dev)
+    dirs = (t["means"] - c2w[:3, 3][None]).contiguous()
+    colors = compute_sh_forward(N, sh_degree, sh_degree, dirs, t["sh"])
+    intr = (cam.fx, cam.fy, cam.cx, cam.cy)
+    tb = ((W + bw - 1) // bw, (H + bw - 1) // bw, 1)
+    if binning is None:
+        centers, extents = get_aabb_2d(t["means"], t["scales"], 1.0, t["quats"], vm, *intr)
+        depths = (t["means"] @ vm.T[:3, :3] + vm.T[3:, :3])[:, 2].contiguous()
+        counts = num_tiles_hit(centers, extents, H, W, bw)
+        n, isect_sorted, gids, bins = bin_and_sort(N, centers, extents, depths, counts, tb, bw)
+    else:
+        gids, bins = binning
+        n, isect_sorted = int(gids.numel()), None
+    bg = background if background is not None else torch.zeros(3, device=dev)
+    C = t["texture"].shape[1]
+    common = ((N, 1, C), t["dims"], gids, bins, colors, t["opacity"], t["means"], t["scales"], 1.0, t["quats"],
+              t["uv0"], t["umap"], t["vmap"], t["texture"], vm, c2w, *intr, settings, bg)
+    names = ("img", "depth", "reg", "texture", "normal", "final_T", "final_idx", "depth_idx", "reg_s")
+    outs = dict(zip(names, texture_forward(tb, (bw, bw, 1), (W, H, 1), *common)))
+    return dict(colors=colors, dirs=dirs, n=n, isect_sorted=isect_sorted, gids_sorted=gids, bins=bins,
+                tile_bounds=tb, common=common, out=outs)
+
+
+def view_backward(t, cam, sh_degree, fwd, ups, block_width=16):
+    """texture_backward and the SH adjoint of one view rendered by
+    view_forward, for upstream gradients ups (dict of CUDA tensors img,
+    texture, normal, reg; depth and alpha optional).  Returns the nine
+    gradients of texture_backward plus 'sh_coeffs'."""
+    o = fwd["out"]
+    z = torch.zeros_like(o["reg"])
+    g = texture_backward(cam.height, cam.width, block_width, *fwd["common"], o["final_T"], o["final_idx"],
+                         o["depth_idx"].clone(), o["reg_s"], ups["img"].contiguous(),
+                         ups.get("depth", z).contiguous(), ups["reg"].contiguous(), ups.get("alpha", z).contiguous(),
+                         ups["texture"].contiguous(), ups["normal"].contiguous())
+    names = ("colors", "opacity", "means", "scales", "quats", "uv0", "umap", "vmap", "texture")
+    grads = dict(zip(names, g))
+    N = t["means"].shape[0]
+    grads["sh_coeffs"] = compute_sh_backward(N, sh_degree, sh_degree, fwd["dirs"], grads["colors"])
+    return grads
+
+
+def image_loss_grads(out, tgt_img, tgt_tex, weights):
+    """Upstream gradients of the demo's image losses (example.py:189-209:
+    w_img MSE(img) + w_tex MSE(texture) + w_reg mean(reg) + w_normal
+    mean |n - (0, 0, 1)|^2), by elementwise torch as the reference's autograd
+    computes them."""
+    H, W = out["reg"].shape
+    inv = 1.0 / (H * W)
+    z = torch.tensor([0.0, 0.0, 1.0], device=out["img"].device)
+    return dict(img=(2 * weights["img"] * inv / 3) * (out["img"] - tgt_img),
+                texture=(2 * weights["texture"] * inv / 3) * (out["texture"] - tgt_tex),
+                reg=torch.full_like(out["reg"], weights["reg"] * inv),
+                normal=(2 * weights["normal"] * inv) * (out["normal"] - z))

@@ -27,7 +27,11 @@ from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(os.path.dirname(HERE), "_ref")
-DEFAULT_SRC = "/root/reference/gstex_cuda/cuda/csrc"
+# The reference checkout: GSTEX_REFERENCE if set, else a directory named
+# "reference" beside this repository's root.
+_REPO = os.path.dirname(os.path.dirname(HERE))
+REFERENCE = os.environ.get("GSTEX_REFERENCE", os.path.join(os.path.dirname(_REPO), "reference"))
+DEFAULT_SRC = os.path.join(REFERENCE, "gstex_cuda", "cuda", "csrc")
 
 # cubin name -> reference source file (each holds the kernels named beside it)
 UNITS = {

@@ -1,7 +1,7 @@
 """Generate golden vectors from the reference's own Python code.
 
-Run in a container that has the reference checkout (default
-``/root/reference``; override with ``GSTEX_REFERENCE``):
+Run where the reference checkout is present (``GSTEX_REFERENCE``, else a
+directory named ``reference`` beside this repository's root):
 
     python tests/golden/make_golden.py
 
@@ -30,7 +30,7 @@ import torch
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("GSTEX_REFERENCE", "/root/reference")
+REF = os.environ.get("GSTEX_REFERENCE", os.path.join(os.path.dirname(REPO), "reference"))
 
 
 def _import_reference():

@@ -145,4 +145,9 @@ def upstream(H, W, C, seed=7):
 
 
 def np_(t):
-    return t.detach().float().cpu().numpy() if isinstance(t, torch.Tensor) else np.asarray(t)
+    """numpy copy of a tensor: floating types as float32, integer types kept
+    (a float32 copy would round indices above 2^24)."""
+    if not isinstance(t, torch.Tensor):
+        return np.asarray(t)
+    t = t.detach()
+    return (t if not t.is_floating_point() else t.float()).cpu().numpy()
