@@ -9,7 +9,9 @@
 // caller passes only its inputs and outputs.
 //
 // The array is sized for GSTEX_SORT_STATIC_MAX_ITEMS pairs (13.1 MB) and
-// exists on every GPU that loads the library until the process exits.  All
+// exists on every GPU that loads the library until the process exits.  The
+// first call in each CUDA context looks up the array's device address, so it
+// should come before any stream capture.  All
 // calls on a device share it and it keeps the last call's contents; the sort
 // writes every scratch word before reading it, so nothing has to be cleared
 // between calls.  Calls that overlap on the GPU (other streams or host
@@ -30,30 +32,74 @@ constexpr size_t kStaticScratchBytes = (size_t)GSTEX_SORT_STATIC_MAX_ITEMS * 8 +
 static __device__ __align__(256) unsigned char g_sort_scratch[kStaticScratchBytes];
 
 namespace {
-constexpr int kMaxDevices = 64;
+// The array's device address belongs to the CUDA context the module was
+// loaded into, so it is cached per context: keyed by the context's unique id
+// (cuCtxGetId, which is never reused, unlike a context handle after a device
+// reset), resolved through the runtime so that the library does not link the
+// driver library.  Without those entry points the address is looked up on
+// every call.
+typedef int (*CtxGetCurrentFn)(void** ctx);
+typedef int (*CtxGetIdFn)(void* ctx, unsigned long long* id);
+constexpr int kCacheSlots = 64;
 std::mutex g_scratch_mutex;
-void* g_scratch_ptr[kMaxDevices] = {};
+bool g_driver_resolved = false;
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+unsigned long long g_cache_ctx[kCacheSlots] = {};
+void* g_cache_ptr[kCacheSlots] = {};
+int g_cache_next = 0;
+
+// Id of the calling thread's current context; false when there is none yet
+// or the driver entry points are unavailable.  Called with the mutex held.
+bool current_context_id(unsigned long long* id) {
+    if (!g_driver_resolved) {
+        g_driver_resolved = true;
+        cudaDriverEntryPointQueryResult q1, q2;
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+            q1 == cudaDriverEntryPointSuccess && q2 == cudaDriverEntryPointSuccess) {
+            g_ctx_get_current = (CtxGetCurrentFn)f1;
+            g_ctx_get_id = (CtxGetIdFn)f2;
+        }
+        cudaGetLastError();  // a failed lookup leaves no sticky error
+    }
+    if (!g_ctx_get_current || !g_ctx_get_id) return false;
+    void* ctx = nullptr;
+    if (g_ctx_get_current(&ctx) != 0 || !ctx) return false;
+    return g_ctx_get_id(ctx, id) == 0;
+}
 }  // namespace
 
-// Device address of g_sort_scratch on the current device.  In host code the
-// array's name is only a host-side stand-in, so the address is looked up once
-// per device (with that device current) and cached.
+// Device address of g_sort_scratch in the current context.  In host code the
+// array's name is only a host-side stand-in, so the address is looked up
+// (which also makes the runtime's context current) the first time a context
+// calls, and cached under that context's id.
 static int static_scratch(void** out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) { set_cuda_error(e, "sort_pairs_static: cudaGetDevice"); return GSTEX_ERR_CUDA; }
-    if (dev < 0 || dev >= kMaxDevices) return GSTEX_ERR_UNSUPPORTED;
     std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (!g_scratch_ptr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_sort_scratch);
-        if (e != cudaSuccess || !p) {
-            set_cuda_error(e, "sort_pairs_static: cudaGetSymbolAddress");
-            return GSTEX_ERR_CUDA;
-        }
-        g_scratch_ptr[dev] = p;
+    unsigned long long id = 0;
+    bool have_id = current_context_id(&id);
+    if (have_id) {
+        for (int i = 0; i < kCacheSlots; i++)
+            if (g_cache_ptr[i] && g_cache_ctx[i] == id) {
+                *out = g_cache_ptr[i];
+                return GSTEX_OK;
+            }
     }
-    *out = g_scratch_ptr[dev];
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_sort_scratch);
+    if (e != cudaSuccess || !p) {
+        set_cuda_error(e, "sort_pairs_static: cudaGetSymbolAddress");
+        return GSTEX_ERR_CUDA;
+    }
+    if (!have_id) have_id = current_context_id(&id);
+    if (have_id) {
+        g_cache_ctx[g_cache_next] = id;
+        g_cache_ptr[g_cache_next] = p;
+        g_cache_next = (g_cache_next + 1) % kCacheSlots;
+    }
+    *out = p;
     return GSTEX_OK;
 }
 

@@ -107,8 +107,8 @@ int gstex_sort_pairs(int n, int end_bit, const int64_t* keys_in, const int32_t* 
  * torch inside each op.  Scratch is one file-scope device array of 13.1 MB
  * sized for GSTEX_SORT_STATIC_MAX_ITEMS pairs, held by every GPU that loads
  * the library until exit; larger n returns GSTEX_ERR_CAPACITY.  The first
- * call on a device looks up the array's device address (do it before any
- * stream capture).  All calls on a device share the array: calls that
+ * call in each CUDA context (per device, and again after a device reset)
+ * looks up the array's device address (do it before any stream capture).  All calls on a device share the array: calls that
  * overlap on the GPU race and must be serialised by the caller; nothing in it
  * needs clearing between calls.  Allocates nothing and calls no allocating
  * routine. */

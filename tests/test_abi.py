@@ -109,3 +109,18 @@ def test_batch_layout_and_workspace_sizes_on_host():
     assert L.gstex_sort32_workspace_bytes(1 << 20) >= (1 << 20) * 8
     assert L.gstex_sort_workspace_bytes(1 << 20) >= (1 << 20) * 12
     assert L.gstex_batch_tile_order_workspace_bytes(96464) >= 96464 * 12 + L.gstex_sort32_workspace_bytes(96464)
+
+
+def test_static_scratch_sort_rejects_bad_arguments_without_gpu():
+    """gstex_sort_pairs_static checks its arguments before touching the GPU:
+    a negative count or end_bit outside [0, 64] is an invalid argument, more
+    pairs than its fixed scratch array holds is a capacity error."""
+    import ctypes
+    L = _lib.lib()
+    f = L.gstex_sort_pairs_static
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 5
+    assert f(-1, 45, None, None, None, None, None) == 1
+    assert f(10, 65, None, None, None, None, None) == 1
+    assert f(10, -1, None, None, None, None, None) == 1
+    assert f((1 << 20) + 1, 45, None, None, None, None, None) == 2

@@ -53,6 +53,29 @@ def test_static_scratch_sort_matches_workspace_sort_twice():
         assert torch.equal(vo, ref_v)
 
 
+@pytest.mark.parametrize("n", [0, 1, 2049])
+@pytest.mark.parametrize("end_bit", [0, 8, 64])
+def test_static_scratch_sort_small_cases(n, end_bit):
+    """The branches of the sort through the static entry point: no pairs, one
+    pair and end_bit 0 (plain copies), 8 bits (one pass), 64 bits (eight
+    passes), each equal to gstex_sort_pairs."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import gstex_cuda_gb300 as G
+    lib = _lib()
+    stream = torch.cuda.current_stream().cuda_stream
+    k, v = _pairs(max(n, 1), 7 + n + end_bit)
+    k, v = k[:n].contiguous(), v[:n].contiguous()
+    ref_k, ref_v = G.cuda.sort_pairs(k, v, end_bit=end_bit)
+    ko = torch.full_like(k, -1)
+    vo = torch.full_like(v, -1)
+    rc = lib.gstex_sort_pairs_static(n, end_bit, k.data_ptr() if n else None, v.data_ptr() if n else None,
+                                     ko.data_ptr() if n else None, vo.data_ptr() if n else None, stream)
+    assert rc == 0, lib.gstex_status_string(rc)
+    torch.cuda.synchronize()
+    assert torch.equal(ko, ref_k) and torch.equal(vo, ref_v)
+
+
 def test_static_scratch_sort_rejects_sizes_beyond_its_array():
     lib = _lib()
     rc = lib.gstex_sort_pairs_static(MAX_ITEMS + 1, 45, None, None, None, None, None)
