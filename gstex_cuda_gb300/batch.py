@@ -45,12 +45,20 @@ class BatchInputs(ctypes.Structure):
                 ("queue", _P), ("grid", _I), ("pixels_per_thread", _I), ("records", _P), ("group_lanes", _I)]
 
 
+class RawGrads(ctypes.Structure):
+    _fields_ = [("raw_quats", _P), ("v_raw_scales", _P), ("v_raw_quats", _P), ("v_mapping", _P),
+                ("v_raw_opacity", _P)]
+
+
 _BATCH_SIGS = {
     "gstex_batch_layout": (_I, [_I, ctypes.POINTER(ViewDesc), _I, ctypes.POINTER(_I), ctypes.POINTER(_LL)]),
     "gstex_batch_views_bytes": (ctypes.c_size_t, [_I]),
     "gstex_batch_prepare": (_I, [_I, ctypes.POINTER(ViewDesc), _I, _P, _P, _P, _P]),
     "gstex_batch_project": (_I, [_I, _I, _P, _P, _P, _F, _P, _P, _I, _I, _I, _P, _P, _P]),
     "gstex_batch_project_keys": (_I, [_I, _I, _P, _P, _P, _F, _P, _P, _I, _I, _I, _P, _P, _P, _P, _P, _P]),
+    "gstex_batch_project_keys_raw": (_I, [_I, _I, _P, _P, _P, _P, _P, _P, _F, _P, _I, _I, _I] + [_P] * 11),
+    "gstex_batch_backward_raw": (_I, [ctypes.POINTER(BatchInputs), ctypes.POINTER(_lib.BackwardIO),
+                                      ctypes.POINTER(RawGrads), _P]),
     "gstex_batch_gather_counts": (_I, [_I, _P, _P, _P, _P]),
     "gstex_batch_emit_sorted": (_I, [_I, _I, _P, _P, _P, _P, _P, _LL, _P, _P, _P, _P, _P]),
     "gstex_sort32_workspace_bytes": (ctypes.c_size_t, [_I]),
@@ -108,6 +116,27 @@ class Scene:
     uv0: torch.Tensor
     umap: torch.Tensor
     vmap: torch.Tensor
+    texture_dims: torch.Tensor
+    texture: torch.Tensor
+    channels: int = 3
+    glob_scale: float = 1.0
+
+
+@dataclass
+class RawScene:
+    """A scene as a GStex trainer holds it (example.py:126-143, 155-171 of the
+    reference): means [N,3]; raw_scales [N,3] log-scales (first two used);
+    raw_quats [N,4] wxyz of any norm; mapping [N,1,4] (uv0 x, uv0 y, log
+    uv-scale, theta); raw_opacity [N] logits; SH coefficients and texels as in
+    Scene.  BatchRenderer.step_raw activates them on the device inside the
+    projection and returns gradients w.r.t. these raw tensors."""
+    means: torch.Tensor
+    raw_scales: torch.Tensor
+    raw_quats: torch.Tensor
+    mapping: torch.Tensor
+    raw_opacity: torch.Tensor
+    sh_coeffs: torch.Tensor
+    sh_degree: int
     texture_dims: torch.Tensor
     texture: torch.Tensor
     channels: int = 3
@@ -256,6 +285,43 @@ class BatchRenderer:
                                          float(s.glob_scale), ptr(s.quats), ptr(s.sh_coeffs), sh_dtype, s.sh_degree,
                                          self.bw, ptr(self.colors), ptr(self.counts), ptr(self.dkeys),
                                          ptr(self.pair_ids), ptr(self.rects), st), "batch_project_keys")
+        self._bin_rest(s)
+
+    def activated(self, raw: RawScene) -> Scene:
+        """The device buffers that bin_raw fills with the activated parameters
+        of `raw` (allocated once; the texels, SH coefficients and means are
+        raw's own tensors)."""
+        if getattr(self, "_act", None) is None or self._act.means is not raw.means:
+            f32 = dict(dtype=torch.float32, device=self.dev)
+            N = self.N
+            self._act = Scene(means=raw.means, scales=torch.empty((N, 3), **f32), quats=torch.empty((N, 4), **f32),
+                              opacity=torch.empty((N, 1), **f32), sh_coeffs=raw.sh_coeffs, sh_degree=raw.sh_degree,
+                              uv0=torch.empty((N, 1, 2), **f32), umap=torch.empty((N, 1, 3), **f32),
+                              vmap=torch.empty((N, 1, 3), **f32), texture_dims=raw.texture_dims,
+                              texture=raw.texture, channels=raw.channels, glob_scale=raw.glob_scale)
+        return self._act
+
+    def bin_raw(self, raw: RawScene) -> Scene:
+        """bin() from the trainer's raw parameters: the projection activates
+        every Gaussian (writing the activated parameters into activated(raw))
+        and the rest of binning reads those.  Returns the activated Scene."""
+        L = _L()
+        st = torch.cuda.current_stream(self.dev).cuda_stream
+        a = self.activated(raw)
+        sh_dtype = 1 if raw.sh_coeffs.dtype == torch.bfloat16 else 0
+        check(L.gstex_batch_project_keys_raw(self.N, self.V, ptr(self.views_dev), ptr(raw.means),
+                                             ptr(raw.raw_scales), ptr(raw.raw_quats), ptr(raw.mapping),
+                                             ptr(raw.raw_opacity), float(raw.glob_scale), ptr(raw.sh_coeffs),
+                                             sh_dtype, raw.sh_degree, self.bw, ptr(a.scales), ptr(a.quats),
+                                             ptr(a.uv0), ptr(a.umap), ptr(a.vmap), ptr(a.opacity), ptr(self.colors),
+                                             ptr(self.counts), ptr(self.dkeys), ptr(self.pair_ids), ptr(self.rects),
+                                             st), "batch_project_keys_raw")
+        self._bin_rest(a)
+        return a
+
+    def _bin_rest(self, s: Scene):
+        L = _L()
+        st = torch.cuda.current_stream(self.dev).cuda_stream
         VN = self.V * self.N
         main = torch.cuda.current_stream(self.dev)
         if self.records is not None:
@@ -350,6 +416,48 @@ class BatchRenderer:
         self.backward(s)
         return loss
 
+    def backward_raw(self, raw: RawScene, upstream: Optional[dict] = None):
+        """backward() carried on through the parameter activation: gradients
+        w.r.t. raw's tensors (keys means, raw_scales, raw_quats, mapping,
+        raw_opacity, texture, sh_coeffs; vcolors per view)."""
+        L = _L()
+        st = torch.cuda.current_stream(self.dev).cuda_stream
+        a = self.activated(raw)
+        g = self._grad_buffers(a)
+        if "raw_scales" not in g:
+            f32 = dict(dtype=torch.float32, device=self.dev)
+            N = self.N
+            g.update(raw_scales=torch.empty((N, 3), **f32), raw_quats=torch.empty((N, 4), **f32),
+                     mapping=torch.empty((N, 1, 4), **f32), raw_opacity=torch.empty((N,), **f32))
+        u = self.ups if upstream is None else upstream
+        g["texture"].zero_()
+        o = self.out
+        bio = _lib.BackwardIO(ptr(o["final_T"]), ptr(o["final_idx"]), ptr(o["depth_idx"]), ptr(o["reg_s"]),
+                              ptr(u.get("img")), ptr(u.get("depth")), ptr(u.get("reg")), ptr(u.get("alpha")),
+                              ptr(u.get("texture")), ptr(u.get("normal")), ptr(g["vcolors"]), None,
+                              ptr(g["means"]), None, None, None, None, None, ptr(g["texture"]), ptr(self.moments),
+                              self.moments.numel())
+        rg = RawGrads(ptr(raw.raw_quats), ptr(g["raw_scales"]), ptr(g["raw_quats"]), ptr(g["mapping"]),
+                      ptr(g["raw_opacity"]) if raw.raw_opacity is not None else None)
+        bi = self._inputs(a, backward=True)
+        check(L.gstex_batch_backward_raw(ctypes.byref(bi), ctypes.byref(bio), ctypes.byref(rg), st),
+              "batch_backward_raw")
+        check(L.gstex_batch_sh_backward(self.N, self.V, ptr(self.views_dev), ptr(raw.means), raw.sh_degree,
+                                        ptr(g["vcolors"]), ptr(g["sh_coeffs"]), st), "batch_sh_backward")
+        return {k: g[k] for k in ("vcolors", "means", "raw_scales", "raw_quats", "mapping", "raw_opacity",
+                                  "texture", "sh_coeffs")}
+
+    def step_raw(self, raw: RawScene, tgt_img, tgt_tex):
+        """One training step from the trainer's raw parameters: activation
+        fused into the projection, forward, image losses, backward carried on
+        to the raw parameters.  Returns the device loss; gradients are in
+        self.raw_grads."""
+        a = self.bin_raw(raw)
+        self.forward(a)
+        loss = self.image_loss(tgt_img, tgt_tex)
+        self.raw_grads = self.backward_raw(raw)
+        return loss
+
     # ------------------------------------------------------------------
     def autotune(self, s: Scene, tgt_img, tgt_tex, reps: int = 2) -> dict:
         """Choose pixels-per-thread and lanes per splat walk (32, 16, 8, 4) of
@@ -390,18 +498,19 @@ class BatchRenderer:
         self.graph = None
         return result
 
-    def capture(self, s: Scene, tgt_img, tgt_tex):
-        """Capture ``step`` for these (static) tensors in a CUDA graph."""
-        self._grad_buffers(s)
+    def capture(self, s, tgt_img, tgt_tex):
+        """Capture ``step`` (``step_raw`` for a RawScene) for these (static)
+        tensors in a CUDA graph."""
+        step = self.step_raw if isinstance(s, RawScene) else self.step
         side = torch.cuda.Stream(self.dev)
         side.wait_stream(torch.cuda.current_stream(self.dev))
         with torch.cuda.stream(side):
             for _ in range(2):
-                self.step(s, tgt_img, tgt_tex)
+                step(s, tgt_img, tgt_tex)
         torch.cuda.current_stream(self.dev).wait_stream(side)
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g):
-            self.step(s, tgt_img, tgt_tex)
+            step(s, tgt_img, tgt_tex)
         self.graph = g
         return g
 

@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "preprocess.cuh"
 #include "project.cuh"
 #include "raster.cuh"
 
@@ -21,19 +22,28 @@ namespace gstex {
 // coefficients are read once.
 // ---------------------------------------------------------------------------
 // SH degree DEG is a template parameter so that the coefficient and basis
-// arrays stay in registers.
+// arrays stay in registers.  With raw.raw_scales set, each Gaussian is first
+// activated from the trainer's raw parameters (preprocess.cuh) and its
+// activated parameters are written for the later stages.
 template <typename SHT, int DEG>
 __global__ void batch_project_kernel(int N, int V, const BatchView* __restrict__ views, const float3* __restrict__ means,
                                      const float* __restrict__ scales, float glob, const float4* __restrict__ quats,
                                      const SHT* __restrict__ sh, int bw, float3* __restrict__ colors,
                                      int32_t* __restrict__ counts, uint32_t* __restrict__ depth_keys,
-                                     int32_t* __restrict__ pair_ids, uint2* __restrict__ rects) {
+                                     int32_t* __restrict__ pair_ids, uint2* __restrict__ rects, RawParams raw) {
     constexpr int B = (DEG + 1) * (DEG + 1);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     const float3 p = means[i];
-    const float4 q = quats[i];
-    const float sx = scales[3 * i], sy = scales[3 * i + 1];
+    float4 q;
+    float sx, sy;
+    if (raw.raw_scales) {
+        activate(raw, i, sx, sy, q);
+    } else {
+        q = quats[i];
+        sx = scales[3 * i];
+        sy = scales[3 * i + 1];
+    }
     float k[B][3];
 #pragma unroll
     for (int b = 0; b < B; b++)
@@ -357,24 +367,24 @@ extern "C" int gstex_batch_prepare(int num_views, const gstex_view_desc* views, 
 template <typename SHT>
 static void project_launch(int deg, int N, int V, const BatchView* bv, const float* means, const float* scales,
                            float glob, const float* quats, const SHT* sh, int bw, float* colors, int32_t* counts,
-                           uint32_t* dk, int32_t* ids, uint2* rects, cudaStream_t stream) {
+                           uint32_t* dk, int32_t* ids, uint2* rects, const RawParams& raw, cudaStream_t stream) {
     const dim3 grid(ceil_div(N, 128)), block(128);
     const float3* m = (const float3*)means;
     const float4* q = (const float4*)quats;
     float3* c = (float3*)colors;
     switch (deg) {
-        case 0: batch_project_kernel<SHT, 0><<<grid, block, 0, stream>>>(N, V, bv, m, scales, glob, q, sh, bw, c, counts, dk, ids, rects); break;
-        case 1: batch_project_kernel<SHT, 1><<<grid, block, 0, stream>>>(N, V, bv, m, scales, glob, q, sh, bw, c, counts, dk, ids, rects); break;
-        case 2: batch_project_kernel<SHT, 2><<<grid, block, 0, stream>>>(N, V, bv, m, scales, glob, q, sh, bw, c, counts, dk, ids, rects); break;
-        case 3: batch_project_kernel<SHT, 3><<<grid, block, 0, stream>>>(N, V, bv, m, scales, glob, q, sh, bw, c, counts, dk, ids, rects); break;
-        default: batch_project_kernel<SHT, 4><<<grid, block, 0, stream>>>(N, V, bv, m, scales, glob, q, sh, bw, c, counts, dk, ids, rects); break;
+        case 0: batch_project_kernel<SHT, 0><<<grid, block, 0, stream>>>(N, V, bv, m, scales, glob, q, sh, bw, c, counts, dk, ids, rects, raw); break;
+        case 1: batch_project_kernel<SHT, 1><<<grid, block, 0, stream>>>(N, V, bv, m, scales, glob, q, sh, bw, c, counts, dk, ids, rects, raw); break;
+        case 2: batch_project_kernel<SHT, 2><<<grid, block, 0, stream>>>(N, V, bv, m, scales, glob, q, sh, bw, c, counts, dk, ids, rects, raw); break;
+        case 3: batch_project_kernel<SHT, 3><<<grid, block, 0, stream>>>(N, V, bv, m, scales, glob, q, sh, bw, c, counts, dk, ids, rects, raw); break;
+        default: batch_project_kernel<SHT, 4><<<grid, block, 0, stream>>>(N, V, bv, m, scales, glob, q, sh, bw, c, counts, dk, ids, rects, raw); break;
     }
 }
 
 static int project_impl(int N, int V, const void* views_dev, const float* means, const float* scales,
                         float glob_scale, const float* quats, const void* sh_coeffs, int sh_dtype, int sh_degree,
                         int block_width, float* colors, int32_t* counts, uint32_t* depth_keys, int32_t* pair_ids,
-                        uint2* rects, cudaStream_t stream) {
+                        uint2* rects, cudaStream_t stream, const RawParams& raw = RawParams{}) {
     GSTEX_REQUIRE(N >= 0 && V > 0 && views_dev && block_width >= 2 && block_width <= kMaxBlockWidth);
     GSTEX_REQUIRE(sh_degree >= 0 && sh_degree <= 4 && (sh_dtype == 0 || sh_dtype == 1));
     if (N == 0) return GSTEX_OK;
@@ -383,10 +393,10 @@ static int project_impl(int N, int V, const void* views_dev, const float* means,
     if (sh_dtype == 1)
         project_launch<__nv_bfloat16>(sh_degree, N, V, bv, means, scales, glob_scale, quats,
                                       (const __nv_bfloat16*)sh_coeffs, block_width, colors, counts, depth_keys,
-                                      pair_ids, rects, stream);
+                                      pair_ids, rects, raw, stream);
     else
         project_launch<float>(sh_degree, N, V, bv, means, scales, glob_scale, quats, (const float*)sh_coeffs,
-                              block_width, colors, counts, depth_keys, pair_ids, rects, stream);
+                              block_width, colors, counts, depth_keys, pair_ids, rects, raw, stream);
     return check_launch("batch_project");
 }
 
@@ -405,6 +415,28 @@ extern "C" int gstex_batch_project_keys(int N, int V, const void* views_dev, con
     if (N > 0) GSTEX_REQUIRE(depth_keys && pair_ids && rects && ((uintptr_t)rects & 7) == 0);
     return project_impl(N, V, views_dev, means, scales, glob_scale, quats, sh_coeffs, sh_dtype, sh_degree,
                         block_width, colors, counts, depth_keys, pair_ids, (uint2*)rects, (cudaStream_t)s);
+}
+
+extern "C" int gstex_batch_project_keys_raw(int N, int V, const void* views_dev, const float* means,
+                                            const float* raw_scales, const float* raw_quats, const float* mapping,
+                                            const float* raw_opacity, float glob_scale, const void* sh_coeffs,
+                                            int sh_dtype, int sh_degree, int block_width, float* scales, float* quats,
+                                            float* uv0, float* umap, float* vmap, float* opacity, float* colors,
+                                            int32_t* counts, uint32_t* depth_keys, int32_t* pair_ids, uint32_t* rects,
+                                            gstex_stream_t s) {
+    if ((unsigned long long)N * (unsigned long long)V > 0x7fffffffull) return GSTEX_ERR_UNSUPPORTED;
+    if (N > 0) {
+        GSTEX_REQUIRE(depth_keys && pair_ids && rects && ((uintptr_t)rects & 7) == 0);
+        GSTEX_REQUIRE(raw_scales && raw_quats && mapping && scales && quats && uv0 && umap && vmap);
+        GSTEX_REQUIRE(((uintptr_t)raw_quats & 15) == 0 && ((uintptr_t)mapping & 15) == 0 &&
+                      ((uintptr_t)quats & 15) == 0 && ((uintptr_t)uv0 & 7) == 0);
+        if (raw_opacity) GSTEX_REQUIRE(opacity);
+    }
+    const RawParams raw{ raw_scales, (const float4*)raw_quats, (const float4*)mapping, raw_opacity, 1, scales,
+                         (float4*)quats, (float2*)uv0, umap, vmap, opacity };
+    // the kernel reads means and writes the activated scales and quats itself
+    return project_impl(N, V, views_dev, means, scales, glob_scale, quats, sh_coeffs, sh_dtype, sh_degree,
+                        block_width, colors, counts, depth_keys, pair_ids, (uint2*)rects, (cudaStream_t)s, raw);
 }
 
 static size_t align256(size_t x) { return (x + 255) / 256 * 256; }
@@ -564,7 +596,8 @@ extern "C" size_t gstex_batch_backward_workspace_bytes(int num_points) {
     return (size_t)(num_points > 0 ? num_points : 1) * kMomStride * sizeof(float);
 }
 
-extern "C" int gstex_batch_backward(const gstex_batch_inputs* in, const gstex_backward_io* io, gstex_stream_t s) {
+static int batch_backward_impl(const gstex_batch_inputs* in, const gstex_backward_io* io, const gstex_raw_grads* raw,
+                               gstex_stream_t s) {
     SceneArgs a;
     BatchArgs ba;
     int rc = batch_scene(in, a, ba);
@@ -573,8 +606,17 @@ extern "C" int gstex_batch_backward(const gstex_batch_inputs* in, const gstex_ba
     GSTEX_REQUIRE(io);
     if (a.N == 0) return GSTEX_OK;  // no Gaussian, no gradient
     GSTEX_REQUIRE(io->final_T && io->final_idx && io->depth_idx && io->reg_s && io->workspace);
-    GSTEX_REQUIRE(io->v_colors && io->v_opacity && io->v_means && io->v_scales && io->v_quats && io->v_uv0 &&
-                  io->v_umap && io->v_vmap);
+    GSTEX_REQUIRE(io->v_colors && io->v_means);
+    RawGradArgs rg{};
+    if (raw) {
+        GSTEX_REQUIRE(raw->raw_quats && raw->v_raw_scales && raw->v_raw_quats && raw->v_mapping);
+        GSTEX_REQUIRE(((uintptr_t)raw->raw_quats & 15) == 0 && ((uintptr_t)raw->v_raw_quats & 15) == 0 &&
+                      ((uintptr_t)raw->v_mapping & 15) == 0);
+        rg = RawGradArgs{ (const float4*)raw->raw_quats, in->scales, in->opacities, raw->v_raw_scales,
+                          (float4*)raw->v_raw_quats, (float4*)raw->v_mapping, raw->v_raw_opacity };
+    } else {
+        GSTEX_REQUIRE(io->v_opacity && io->v_scales && io->v_quats && io->v_uv0 && io->v_umap && io->v_vmap);
+    }
     if (a.C > 0) GSTEX_REQUIRE(io->v_tex_grad);
     if (io->workspace_bytes < gstex_batch_backward_workspace_bytes(a.N)) return GSTEX_ERR_CAPACITY;
     if (a.N == 0) return GSTEX_OK;
@@ -592,7 +634,17 @@ extern "C" int gstex_batch_backward(const gstex_batch_inputs* in, const gstex_ba
                                in->group_lanes, grid_of(in, true), stream)))
         return rc;
     return launch_finalize(a, (const float*)io->workspace, io->v_opacity, io->v_means, io->v_scales, io->v_quats,
-                           io->v_uv0, io->v_umap, io->v_vmap, stream);
+                           io->v_uv0, io->v_umap, io->v_vmap, stream, rg);
+}
+
+extern "C" int gstex_batch_backward(const gstex_batch_inputs* in, const gstex_backward_io* io, gstex_stream_t s) {
+    return batch_backward_impl(in, io, nullptr, s);
+}
+
+extern "C" int gstex_batch_backward_raw(const gstex_batch_inputs* in, const gstex_backward_io* io,
+                                        const gstex_raw_grads* raw, gstex_stream_t s) {
+    GSTEX_REQUIRE(raw);
+    return batch_backward_impl(in, io, raw, s);
 }
 
 extern "C" int gstex_batch_sh_backward(int N, int V, const void* views_dev, const float* means, int sh_degree,

@@ -1,52 +1,18 @@
 // Per-step parameter activation of a GStex training loop on the device: the
 // preprocessing of the reference's demo trainer (example.py:126-143 and the
-// sigmoids of example.py:155-171) as one forward and one backward kernel.
-//
-//   scales[:, :2] = exp(raw_scales[:, :2]); scales[:, 2] = 1e-5 * mean(scales[:, :2]) (no gradient)
-//   quats         = raw_quats / |raw_quats|
-//   uv0           = mapping[..., 0:2]
-//   umap          = exp(mapping[..., 2]) * ( ax1 cos(theta) + ax2 sin(theta))
-//   vmap          = exp(mapping[..., 2]) * (-ax1 sin(theta) + ax2 cos(theta)),  theta = mapping[..., 3]
-//   opacity       = sigmoid(raw_opacity)
-//
-// with ax1, ax2 the first two columns of R(quats).  One thread per Gaussian;
-// P charts per Gaussian.
-#include "common.cuh"
+// sigmoids of example.py:155-171) as one forward and one backward kernel;
+// the formulas are in preprocess.cuh.  One thread per Gaussian; P charts per
+// Gaussian.
+#include "preprocess.cuh"
 
 namespace gstex {
 
-__device__ __forceinline__ float sigmoidf(float x) { return 1.f / (1.f + expf(-x)); }
-
-__global__ void preprocess_fwd_kernel(int N, int P, const float* __restrict__ raw_scales,
-                                      const float4* __restrict__ raw_quats, const float4* __restrict__ mapping,
-                                      const float* __restrict__ raw_opacity, float* __restrict__ scales,
-                                      float4* __restrict__ quats, float2* __restrict__ uv0,
-                                      float* __restrict__ umap, float* __restrict__ vmap,
-                                      float* __restrict__ opacity) {
+__global__ void preprocess_fwd_kernel(int N, RawParams r) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
-    const float s0 = expf(raw_scales[3 * i]), s1 = expf(raw_scales[3 * i + 1]);
-    scales[3 * i] = s0;
-    scales[3 * i + 1] = s1;
-    scales[3 * i + 2] = 1e-5f * (0.5f * (s0 + s1));
-    const float4 r = raw_quats[i];
-    const float in = 1.f / sqrtf(r.x * r.x + r.y * r.y + r.z * r.z + r.w * r.w);
-    const float4 q = make_float4(r.x * in, r.y * in, r.z * in, r.w * in);
-    quats[i] = q;
-    const Axes A = quat_axes(q);
-    for (int p = 0; p < P; p++) {
-        const size_t k = (size_t)i * P + p;
-        const float4 m = mapping[k];
-        uv0[k] = make_float2(m.x, m.y);
-        const float us = expf(m.z);
-        float sn, cs;
-        sincosf(m.w, &sn, &cs);
-        const float3 u = us * (cs * A.a1 + sn * A.a2);
-        const float3 v = us * (cs * A.a2 - sn * A.a1);
-        umap[3 * k] = u.x; umap[3 * k + 1] = u.y; umap[3 * k + 2] = u.z;
-        vmap[3 * k] = v.x; vmap[3 * k + 1] = v.y; vmap[3 * k + 2] = v.z;
-    }
-    if (raw_opacity) opacity[i] = sigmoidf(raw_opacity[i]);
+    float s0, s1;
+    float4 q;
+    activate(r, i, s0, s1, q);
 }
 
 __global__ void preprocess_bwd_kernel(int N, int P, const float* __restrict__ raw_scales,
@@ -114,9 +80,9 @@ extern "C" int gstex_preprocess_forward(int N, int P, const float* raw_scales, c
     GSTEX_REQUIRE(raw_scales && raw_quats && scales && quats);
     if (P > 0) GSTEX_REQUIRE(mapping && uv0 && umap && vmap);
     if (raw_opacity) GSTEX_REQUIRE(opacity);
-    preprocess_fwd_kernel<<<ceil_div(N, 256), 256, 0, (cudaStream_t)s>>>(
-        N, P, raw_scales, (const float4*)raw_quats, (const float4*)mapping, raw_opacity, scales, (float4*)quats,
-        (float2*)uv0, umap, vmap, opacity);
+    const RawParams r{ raw_scales, (const float4*)raw_quats, (const float4*)mapping, raw_opacity, P, scales,
+                       (float4*)quats, (float2*)uv0, umap, vmap, opacity };
+    preprocess_fwd_kernel<<<ceil_div(N, 256), 256, 0, (cudaStream_t)s>>>(N, r);
     return check_launch("preprocess_forward");
 }
 

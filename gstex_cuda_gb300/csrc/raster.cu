@@ -1202,11 +1202,18 @@ int launch_records(const SceneArgs& a, const BatchArgs& ba, int num_views, const
 }
 
 // Moments -> parameter gradients (one thread per Gaussian).  Colour gradients
-// are written by the tile flushes directly.
+// are written by the tile flushes directly.  With rg.raw_quats set the
+// gradients are carried on through the parameter activation (preprocess.cuh)
+// to the trainer's raw parameters, from the activated values the projection
+// wrote: exp' = scale, sigmoid' = o (1 - o); the chart maps umap = us (cs a1 +
+// sn a2), vmap = us (cs a2 - sn a1) give d/d log-scale = vu.u + vv.v,
+// d/d theta = vu.v - vv.u and, with us cs = u.a1 and us sn = u.a2, the
+// gradients into the axes a1, a2 that join the quaternion's; the
+// normalisation adds (I - q q^T) / |raw q|.
 __global__ void finalize_kernel(int N, const float* __restrict__ mom, const float4* __restrict__ quats,
                                 const float3* __restrict__ umap, const float3* __restrict__ vmap, float* v_opac,
                                 float3* v_means, float3* v_scales, float4* v_quats, float2* v_uv0, float3* v_umap,
-                                float3* v_vmap) {
+                                float3* v_vmap, RawGradArgs rg) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     float M[kMomStride];
@@ -1221,18 +1228,40 @@ __global__ void finalize_kernel(int N, const float* __restrict__ mom, const floa
     const float4 q = quats[i];
     const Axes A = quat_axes(q);
     const float3 um = umap[i], vm = vmap[i];
-    v_opac[i] = M[0];
-    v_scales[i] = make_float3(M[1], M[2], 0.f);
-    v_uv0[i] = make_float2(M[15], M[16]);
-    v_umap[i] = M[17] * A.a1 + M[18] * A.a2;
-    v_vmap[i] = M[19] * A.a1 + M[20] * A.a2;
+    const float3 vu = M[17] * A.a1 + M[18] * A.a2;  // v_umap
+    const float3 vv = M[19] * A.a1 + M[20] * A.a2;  // v_vmap
     const float3 vdiff = M[15] * um + M[16] * vm;
     const float3 vmean = (M[5] * A.a3) - (M[3] * A.a1 + M[4] * A.a2) - vdiff;
     v_means[i] = vmean + make_float3(M[21], M[22], M[23]);
-    const float3 c0 = M[6] * A.a1 + M[7] * A.a2;
-    const float3 c1 = M[8] * A.a1 + M[9] * A.a2;
+    float3 c0 = M[6] * A.a1 + M[7] * A.a2;
+    float3 c1 = M[8] * A.a1 + M[9] * A.a2;
     const float3 c2 = make_float3(M[12], M[13], M[14]) - (M[10] * A.a1 + M[11] * A.a2);
-    v_quats[i] = quat_axes_vjp(q, c0, c1, c2);
+    if (!rg.raw_quats) {
+        v_opac[i] = M[0];
+        v_scales[i] = make_float3(M[1], M[2], 0.f);
+        v_uv0[i] = make_float2(M[15], M[16]);
+        v_umap[i] = vu;
+        v_vmap[i] = vv;
+        v_quats[i] = quat_axes_vjp(q, c0, c1, c2);
+        return;
+    }
+    if (rg.v_raw_opacity) {
+        const float o = rg.opacity[i];
+        rg.v_raw_opacity[i] = M[0] * o * (1.f - o);
+    }
+    rg.v_raw_scales[3 * i] = M[1] * rg.scales[3 * i];
+    rg.v_raw_scales[3 * i + 1] = M[2] * rg.scales[3 * i + 1];
+    rg.v_raw_scales[3 * i + 2] = 0.f;
+    const float usc = dot3(um, A.a1), uss = dot3(um, A.a2);
+    rg.v_mapping[i] = make_float4(M[15], M[16], dot3(vu, um) + dot3(vv, vm), dot3(vu, vm) - dot3(vv, um));
+    c0 = c0 + (usc * vu - uss * vv);
+    c1 = c1 + (uss * vu + usc * vv);
+    const float4 vq = quat_axes_vjp(q, c0, c1, c2);
+    const float4 r = rg.raw_quats[i];
+    const float in = 1.f / sqrtf(r.x * r.x + r.y * r.y + r.z * r.z + r.w * r.w);
+    const float qv = q.x * vq.x + q.y * vq.y + q.z * vq.z + q.w * vq.w;
+    rg.v_raw_quats[i] = make_float4((vq.x - q.x * qv) * in, (vq.y - q.y * qv) * in, (vq.z - q.z * qv) * in,
+                                    (vq.w - q.w * qv) * in);
 }
 
 template <typename K>
@@ -1346,11 +1375,12 @@ size_t bwd_smem(int bw, int ppt, int gs) {
 }
 
 int launch_finalize(const SceneArgs& a, const float* moments, float* v_opac, float* v_means, float* v_scales,
-                    float* v_quats, float* v_uv0, float* v_umap, float* v_vmap, cudaStream_t stream) {
+                    float* v_quats, float* v_uv0, float* v_umap, float* v_vmap, cudaStream_t stream,
+                    const RawGradArgs& rg) {
     if (a.N == 0) return GSTEX_OK;
     finalize_kernel<<<ceil_div(a.N, 256), 256, 0, stream>>>(a.N, moments, a.quats, a.umap, a.vmap, v_opac,
                                                            (float3*)v_means, (float3*)v_scales, (float4*)v_quats,
-                                                           (float2*)v_uv0, (float3*)v_umap, (float3*)v_vmap);
+                                                           (float2*)v_uv0, (float3*)v_umap, (float3*)v_vmap, rg);
     return check_launch("finalize");
 }
 

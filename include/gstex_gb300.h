@@ -424,6 +424,39 @@ int gstex_batch_forward(const gstex_batch_inputs* in, const gstex_forward_output
 size_t gstex_batch_backward_workspace_bytes(int num_points);
 int gstex_batch_backward(const gstex_batch_inputs* in, const gstex_backward_io* io, gstex_stream_t stream);
 
+/* A training step from the trainer's raw parameters (the demo trainer's
+ * per-step activation, example.py:126-143 and 155-171, fused into the
+ * batched step instead of a dozen PyTorch ops; no native counterpart in the
+ * reference).  gstex_batch_project_keys_raw is gstex_batch_project_keys that
+ * first activates each Gaussian from raw_scales [N,3] (log, first two
+ * used), raw_quats [N,4] (wxyz, any norm, 16-byte aligned), mapping [N,1,4]
+ * (uv0 x, uv0 y, log uv-scale, theta; 16-byte aligned) and raw_opacity [N]
+ * (logits, or null to keep opacity) and writes the activated scales [N,3],
+ * quats [N,4], uv0 [N,1,2], umap / vmap [N,1,3] and opacity [N], which the
+ * later stages of the step read (pass them in gstex_batch_inputs). */
+int gstex_batch_project_keys_raw(int num_points, int num_views, const void* views_dev, const float* means,
+                                 const float* raw_scales, const float* raw_quats, const float* mapping,
+                                 const float* raw_opacity, float glob_scale, const void* sh_coeffs, int sh_dtype,
+                                 int sh_degree, int block_width, float* scales, float* quats, float* uv0,
+                                 float* umap, float* vmap, float* opacity, float* colors, int32_t* counts,
+                                 uint32_t* depth_keys, int32_t* pair_ids, uint32_t* rects, gstex_stream_t stream);
+
+/* Gradients w.r.t. the raw parameters of gstex_batch_project_keys_raw. */
+typedef struct gstex_raw_grads {
+    const float* raw_quats;  /* [N,4] the step's raw quaternions (16-byte aligned) */
+    float* v_raw_scales;     /* [N,3] (third entry 0: the third scale is tied) */
+    float* v_raw_quats;      /* [N,4] (16-byte aligned) */
+    float* v_mapping;        /* [N,1,4] (16-byte aligned) */
+    float* v_raw_opacity;    /* [N], or null when opacity was not activated */
+} gstex_raw_grads;
+
+/* gstex_batch_backward carried on through the activation: writes io->v_means,
+ * io->v_colors and the raw gradients (io->v_opacity, v_scales, v_quats,
+ * v_uv0, v_umap, v_vmap are not written and may be null).  The activated
+ * scales and opacities in `in` are the ones the projection wrote. */
+int gstex_batch_backward_raw(const gstex_batch_inputs* in, const gstex_backward_io* io, const gstex_raw_grads* raw,
+                             gstex_stream_t stream);
+
 /* SH coefficient gradients [N, bases(degree), 3] summed over views, from
  * the [V, N, 4] colour gradients of gstex_batch_backward.  Batched
  * compute_sh_backward. */

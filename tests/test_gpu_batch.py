@@ -414,3 +414,64 @@ def test_bf16_storage_accuracy_vs_fp64_oracle():
     assert (img_b > 2e-3).mean() <= 1e-3, float((img_b > 2e-3).mean())
     for k, (mx, _, fr2) in g_b.items():
         assert fr2 <= 5e-3 and mx < 1e-1, ("fp32 values", k, mx, fr2)
+
+
+def _raw_from(spec, seed=23):
+    """Trainer-side raw parameters near the spec's scene: log-scales, quaternions
+    of random norm, charts (uv0, log uv-scale, theta), opacity logits."""
+    g = torch.Generator().manual_seed(seed)
+    N = spec.num_points
+    raw_scales = torch.log(spec.scales.clone())
+    raw_scales[:, 2] = torch.randn(N, generator=g)  # not used (the third scale is tied)
+    raw_quats = spec.quats * torch.empty(N, 1).uniform_(0.5, 2.0, generator=g)
+    mapping = torch.zeros(N, 1, 4)
+    mapping[:, 0, :2] = 0.5
+    mapping[:, 0, 2] = torch.log(1.0 / (6.0 * spec.scales[:, :2].mean(-1)))
+    mapping[:, 0, 3] = torch.empty(N).uniform_(-3.0, 3.0, generator=g)
+    raw_opacity = torch.logit(spec.opacity.reshape(-1).clamp(1e-4, 1 - 1e-4))
+    return raw_scales, raw_quats, mapping, raw_opacity
+
+
+def test_raw_parameter_step_matches_preprocess_then_step(setup):
+    """The training step from raw parameters (activation fused into the
+    projection, its adjoint into the gradient finalize) against the two-kernel
+    path: the standalone preprocess kernel, the step on the activated scene,
+    and the preprocess adjoint on the activated gradients.  Same loss and raw
+    gradients up to float rounding; the activated parameters it wrote equal
+    the preprocess kernel's to a few ulp."""
+    from gstex_cuda_gb300 import batch as B
+    from gstex_cuda_gb300.preprocess import preprocess
+    spec, cams, r, scene, _ = setup
+    rs, rq, mp, ro = (x.to(DEV) for x in _raw_from(spec))
+    raw = B.RawScene(means=scene.means, raw_scales=rs.contiguous(), raw_quats=rq.contiguous(),
+                     mapping=mp.contiguous(), raw_opacity=ro.contiguous(), sh_coeffs=scene.sh_coeffs, sh_degree=3,
+                     texture_dims=scene.texture_dims, texture=scene.texture)
+    gen = torch.Generator().manual_seed(1)
+    tgt_img = torch.rand(r.total_pixels, 3, generator=gen).to(DEV)
+    tgt_tex = torch.rand(r.total_pixels, 3, generator=gen).to(DEV)
+    l_raw = float(r.step_raw(raw, tgt_img, tgt_tex).item())
+    g_raw = {k: v.clone() for k, v in r.raw_grads.items()}
+    act = {k: getattr(r.activated(raw), k).clone() for k in ("scales", "quats", "uv0", "umap", "vmap", "opacity")}
+    # two-kernel path
+    leaves = [t.clone().requires_grad_(True) for t in (rs, rq, mp, ro)]
+    sc, qu, u0, um, vm, op = preprocess(*leaves)
+    for k, v in zip(("scales", "quats", "uv0", "umap", "vmap", "opacity"), (sc, qu, u0, um, vm, op)):
+        ref = v.detach().reshape(act[k].shape)
+        assert torch.allclose(act[k], ref, rtol=2e-6, atol=1e-6), k
+    s2 = B.Scene(means=scene.means, scales=sc.detach().contiguous(), quats=qu.detach().contiguous(),
+                 opacity=op.detach().contiguous(), sh_coeffs=scene.sh_coeffs, sh_degree=3,
+                 uv0=u0.detach().contiguous(), umap=um.detach().contiguous(), vmap=vm.detach().contiguous(),
+                 texture_dims=scene.texture_dims, texture=scene.texture)
+    l2 = float(r.step(s2, tgt_img, tgt_tex).item())
+    g2 = r.grads
+    torch.autograd.backward([sc, qu, u0, um, vm, op], [g2["scales"], g2["quats"], g2["uv0"], g2["umap"], g2["vmap"],
+                                                       g2["opacity"]])
+    assert abs(l_raw - l2) <= 1e-5 * abs(l2)
+    refs = dict(raw_scales=leaves[0].grad, raw_quats=leaves[1].grad, mapping=leaves[2].grad,
+                raw_opacity=leaves[3].grad, means=g2["means"], texture=g2["texture"], sh_coeffs=g2["sh_coeffs"])
+    for k, ref in refs.items():
+        got = g_raw[k].reshape(ref.shape)
+        if k == "raw_scales":
+            got, ref = got[:, :2], ref[:, :2]
+        err = float((got - ref).abs().max() / (ref.abs().max() + 1e-12))
+        assert err < 1e-3, (k, err)
