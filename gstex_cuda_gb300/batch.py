@@ -42,7 +42,8 @@ class BatchInputs(ctypes.Structure):
                 ("views", _P), ("tile_view", _P), ("tile_order", _P), ("gaussian_ids_sorted", _P), ("tile_bins", _P),
                 ("colors", _P), ("opacities", _P), ("means", _P), ("scales", _P), ("glob_scale", _F), ("quats", _P),
                 ("uv0", _P), ("umap", _P), ("vmap", _P), ("texture_dims", _P), ("texture", _P), ("background", _P),
-                ("queue", _P), ("grid", _I), ("pixels_per_thread", _I), ("records", _P), ("group_lanes", _I)]
+                ("queue", _P), ("grid", _I), ("pixels_per_thread", _I), ("records", _P), ("group_lanes", _I),
+                ("stage_bulk", _I)]
 
 
 class RawGrads(ctypes.Structure):
@@ -152,8 +153,8 @@ class BatchRenderer:
     def __init__(self, cameras: Sequence[Camera], num_points: int, *, channels: int = 3, texture_dtype=torch.float32,
                  block_width: int = 16, settings: int = 1 << 8, background=(0.0, 0.0, 0.0), capacity: int = 0,
                  device="cuda:0", grid: int = 0, loss_weights: Optional[dict] = None, fwd_ppt: int = 1,
-                 bwd_ppt: int = 1, fwd_group: int = 32, bwd_group: int = 32, prebuilt_records: bool = True,
-                 heavy_first: bool = True):
+                 bwd_ppt: int = 1, fwd_group: int = 32, bwd_group: int = 32, stage_bulk: bool = False,
+                 prebuilt_records: bool = True, heavy_first: bool = True):
         self.dev = torch.device(device)
         self.N = int(num_points)
         self.V = len(cameras)
@@ -164,6 +165,7 @@ class BatchRenderer:
         self.grid = int(grid)
         self.fwd_ppt, self.bwd_ppt = int(fwd_ppt), int(bwd_ppt)
         self.fwd_group, self.bwd_group = int(fwd_group), int(bwd_group)
+        self.stage_bulk = bool(stage_bulk)
         self.lw = dict(LOSS_WEIGHTS if loss_weights is None else loss_weights)
         L = _L()
         descs = (ViewDesc * self.V)()
@@ -272,6 +274,7 @@ class BatchRenderer:
         bi.queue, bi.grid = ptr(self.queue), self.grid
         bi.pixels_per_thread = self.bwd_ppt if backward else self.fwd_ppt
         bi.group_lanes = self.bwd_group if backward else self.fwd_group
+        bi.stage_bulk = 0 if backward else int(self.stage_bulk)
         bi.records = ptr(self.records) if self.records is not None else None
         return bi
 

@@ -541,6 +541,7 @@ static int batch_scene(const gstex_batch_inputs* in, SceneArgs& a, BatchArgs& ba
     ba.vcolors = nullptr;
     ba.queue = in->queue;
     ba.recs = (const RecAll*)in->records;
+    ba.stage_bulk = in->stage_bulk;
     return GSTEX_OK;
 }
 

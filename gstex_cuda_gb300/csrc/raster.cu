@@ -61,6 +61,66 @@ __device__ __forceinline__ void stage_job(const Recs& R, int slot, const SceneAr
     }
 }
 
+// ---------------------------------------------------------------------------
+// Bulk staging: the hot, warm and cold parts of a prebuilt record copied into
+// their shared-memory slots by the copy engine (cp.async.bulk, no registers or
+// load/store instructions per 16 bytes), completing on a CTA mbarrier that the
+// batch waits on.  The barrier expects one arrival per thread; each thread
+// announces the bytes of its own copies (arrive.expect_tx) before issuing
+// them, so the barrier's transaction count never runs ahead of its
+// expectation.  Every wait is bounded: non-blocking polls with a short sleep,
+// at most kStageSpins of them (about 0.2 s); then the kernel counts the
+// time-out in g_wait_timeouts and stops (no tile is rendered from a batch that
+// did not arrive).
+// ---------------------------------------------------------------------------
+__device__ unsigned int g_wait_timeouts;
+constexpr int kStageSpins = 1 << 21;
+constexpr unsigned kStageBytes = sizeof(RecHot) + sizeof(RecWarm) + sizeof(RecCold);
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
+    for (int i = 0; i < kStageSpins; ++i) {
+        if (mbar_test_wait(bar, parity)) return true;
+        if (i >= 32) __nanosleep(100);
+    }
+    return false;
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Issues the copies of the prebuilt record of Gaussian gid into slot.
+__device__ __forceinline__ void stage_bulk(const Recs& R, int slot, const TileJob& J, int gid, uint64_t* bar) {
+    const unsigned char* src = reinterpret_cast<const unsigned char*>(J.recs + gid);
+    bulk_g2s(R.hot + slot, src, sizeof(RecHot), bar);
+    bulk_g2s(R.warm + slot, src + sizeof(RecHot), sizeof(RecWarm), bar);
+    bulk_g2s(R.cold + slot, src + sizeof(RecHot) + sizeof(RecWarm), sizeof(RecCold), bar);
+}
+
 // Completes a Hit in the direct form, rebuilding the Gaussian's camera-space
 // frame from its parameters (rare: splats at the camera plane and pixels within
 // the reference's denominator clamp).
@@ -245,9 +305,14 @@ __device__ __forceinline__ int build_group_list(uint8_t* gl, const uint8_t* wl, 
 // skipped splat can still end a pixel whose T is within 1/(1 - 1/255) of the
 // 1e-4 limit (texture.cu:213-221): a group with such a pixel walks every slot
 // of the batch from then on, in order, as the reference does.
+//
+// With bar (a CTA mbarrier expecting one arrival per thread; phase its
+// current parity) and prebuilt records, each batch is staged by bulk copies;
+// returns false when a batch did not arrive within the bounded wait (the tile
+// is then not written).
 template <int TEXMODE, int CT, int PPT, int GS = 32>
-__device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, const FwdOut& o, const Recs& R,
-                                         uint8_t* lists) {
+__device__ __forceinline__ bool fwd_tile(const SceneArgs& a, const TileJob& J, const FwdOut& o, const Recs& R,
+                                         uint8_t* lists, uint64_t* bar = nullptr, unsigned* phase = nullptr) {
     static_assert(GS == 32 || GS == 16 || GS == 8 || GS == 4, "group of 32, 16, 8 or 4 lanes");
     const int nthr = blockDim.x * blockDim.y;
     const int tr = threadIdx.y * blockDim.x + threadIdx.x;
@@ -316,13 +381,28 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
     const int2 range = J.range;
     const int nb = ceil_div(range.y - range.x, nthr);
 
+    const bool bulk = bar != nullptr && J.recs != nullptr;
     for (int b = 0; b < nb; ++b) {
         if (__syncthreads_count(all_done) >= nthr) break;
         const int bstart = range.x + nthr * b;
         const int idx = bstart + tr;
-        if (idx < range.y) stage_job(R, tr, a, J, a.gids[idx], use_blur);
-        __syncthreads();
         const int bsize = min(nthr, range.y - bstart);
+        if (bulk) {
+            // the slots were last read before the barrier above
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_arrive_expect_tx(bar, idx < range.y ? kStageBytes : 0u);
+            if (idx < range.y) stage_bulk(R, tr, J, a.gids[idx], bar);
+            const bool ok = mbar_wait_bounded(bar, *phase);
+            if (__syncthreads_or(!ok)) {
+                if (tr == 0) atomicAdd(&g_wait_timeouts, 1u);
+                mbar_wait_bounded(bar, *phase);  // copies still in flight: one more bounded wait
+                return false;
+            }
+            *phase ^= 1u;
+        } else {
+            if (idx < range.y) stage_job(R, tr, a, J, a.gids[idx], use_blur);
+            __syncthreads();
+        }
         if (__all_sync(wmask, all_done)) continue;
         // Composites staged slot k into this thread's pixels (those not done
         // and, while T > 1.01e-4, inside the splat's alpha >= 1/255 box).
@@ -445,7 +525,9 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
                 else ++j;
                 update_done();
                 if (__all_sync(0xffffffffu, all_done)) break;
-                if (!dense && (__ballot_sync(0xffffffffu, act && near_done()) & gmask)) {
+                // every lane takes part in the ballot (dense differs between groups)
+                const unsigned nd = __ballot_sync(0xffffffffu, act && near_done());
+                if (!dense && (nd & gmask)) {
                     dense = true;
                     kd = k;
                 }
@@ -467,6 +549,7 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
         o.reg_s[pix] = ts[p];
         for (int ch = 0; ch < C; ch++) o.tex[pix * C + ch] = otex[p][ch];
     }
+    return true;
 }
 
 // ---------------------------------------------------------------------------
@@ -1016,7 +1099,14 @@ __global__ void FWD_BOUNDS(PPT) fwd_view_kernel(SceneArgs a, ViewArgs va, FwdOut
     J.vc_stride = 3;
     J.recs = va.recs;
     const int nthr = blockDim.x * blockDim.y;
-    fwd_tile<TEXMODE, CT, PPT, GS>(a, J, o, Recs::carve(smem, nthr, false), smem + (size_t)kRecBytes * nthr);
+    __shared__ uint64_t s_bar;
+    unsigned phase = 0;
+    if (va.stage_bulk && J.recs) {
+        if (threadIdx.x == 0 && threadIdx.y == 0) mbar_init(&s_bar, nthr);
+        __syncthreads();
+    }
+    fwd_tile<TEXMODE, CT, PPT, GS>(a, J, o, Recs::carve(smem, nthr, false), smem + (size_t)kRecBytes * nthr,
+                                   va.stage_bulk ? &s_bar : nullptr, &phase);
 }
 
 template <int TEXMODE, int CT, int PPT, int GS>
@@ -1070,7 +1160,15 @@ __global__ void FWD_BOUNDS(PPT) fwd_batch_kernel(SceneArgs a, BatchArgs ba, FwdO
     const int nthr = blockDim.x * blockDim.y;
     const Recs R = Recs::carve(smem, nthr, false);
     uint8_t* lists = smem + (size_t)kRecBytes * nthr;
-    while (next_job(ba, &s_tile, J)) fwd_tile<TEXMODE, CT, PPT, GS>(a, J, o, R, lists);
+    __shared__ uint64_t s_bar;
+    unsigned phase = 0;
+    const bool bulk = ba.stage_bulk && ba.recs;
+    if (bulk) {
+        if (threadIdx.x == 0 && threadIdx.y == 0) mbar_init(&s_bar, nthr);
+        __syncthreads();
+    }
+    while (next_job(ba, &s_tile, J))
+        if (!fwd_tile<TEXMODE, CT, PPT, GS>(a, J, o, R, lists, bulk ? &s_bar : nullptr, &phase)) break;
 }
 
 template <int TEXMODE, int CT, int PPT, int GS>
@@ -1445,11 +1543,22 @@ static ViewArgs view_args(const gstex_raster_inputs* in) {
     va.colors = (const float3*)in->colors;
     va.vcolors = nullptr;
     va.recs = (const RecAll*)in->records;
+    va.stage_bulk = in->stage_bulk;
     return va;
 }
 
 // records [N], then the count and list of deferred near-edge-on records
 static size_t view_records_fix_offset(int n) { return (size_t)n * sizeof(RecAll); }
+
+extern "C" unsigned int gstex_wait_timeouts(void) {
+    unsigned int n = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(&n, g_wait_timeouts, sizeof(n));
+    if (e != cudaSuccess) {
+        set_cuda_error(e, "wait_timeouts");
+        return 0xffffffffu;
+    }
+    return n;
+}
 
 extern "C" size_t gstex_view_records_bytes(int num_points) {
     const int n = num_points > 0 ? num_points : 0;

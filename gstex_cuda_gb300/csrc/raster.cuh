@@ -36,6 +36,7 @@ struct ViewArgs {
     const float3* colors;
     float* vcolors;       // [N,3] colour gradients (backward)
     const RecAll* recs;   // optional [N] prebuilt records of the view; null: built per tile
+    int stage_bulk;       // forward: stage prebuilt records with bulk copies
 };
 
 // Per-view constants of a batched launch (device array).
@@ -58,6 +59,7 @@ struct BatchArgs {
     float* vcolors;            // [V, N, 4] (rgb + pad: one vector atomic per flush)
     int* queue;                // tile counter, zero before each launch
     const RecAll* recs;        // optional [V, N] prebuilt records; null: built per tile
+    int stage_bulk;            // forward: stage prebuilt records with bulk copies
 };
 
 // What one CTA needs to render one tile.

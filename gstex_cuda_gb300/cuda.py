@@ -186,6 +186,10 @@ PIXELS_PER_THREAD = 1  # 1 or 2 (2 halves the threads per tile; even block width
 # thread and 0 or 3 channels (else 32).
 FORWARD_GROUP_LANES = 32
 BACKWARD_GROUP_LANES = 32
+# texture_forward with prebuilt records: stage each batch of records into
+# shared memory with bulk copies (cp.async.bulk on an mbarrier) instead of
+# per-thread 16-byte loads.
+STAGE_BULK = False
 # texture_forward / texture_backward build one splat record per Gaussian of the
 # view first (gstex_view_records) and the tiles copy them; False: every tile
 # derives the records of its Gaussians itself.
@@ -254,6 +258,7 @@ def texture_forward(tile_bounds, block, img_size, texture_info, texture_dims, ga
                            means, scales, glob_scale, quats, uv0, umap, vmap, texture, viewmat, fx, fy, cx, cy,
                            settings, background)
     ri.group_lanes = int(FORWARD_GROUP_LANES)
+    ri.stage_bulk = int(bool(STAGE_BULK))
     dev = means.device
     f32 = dict(dtype=torch.float32, device=dev)
     out_img = torch.empty((H, W, 3), **f32)

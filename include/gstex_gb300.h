@@ -41,6 +41,12 @@ const char* gstex_last_cuda_error(void);
 const char* gstex_version(void);
 /* Number of kernels this library has launched since it was loaded. */
 unsigned long long gstex_launch_count(void);
+/* Number of bounded device-side waits (bulk-copy staging) that gave up on
+ * the current device since the library was loaded; a kernel whose wait gives
+ * up stops without writing the tiles it had not finished.  Synchronous
+ * (reads device memory); 0xffffffff if the read fails.  No counterpart in the
+ * reference, whose kernels have no waits. */
+unsigned int gstex_wait_timeouts(void);
 
 /* ---------------------------------------------------------------------
  * Projection
@@ -187,6 +193,10 @@ typedef struct gstex_raster_inputs {
      * and 0 or 3 channels; elsewhere 32 is used.  Results do not depend on
      * it beyond float summation order. */
     int group_lanes;
+    /* texture_forward with records: 1 stages each batch of records into
+     * shared memory with bulk copies (cp.async.bulk completing on a CTA
+     * mbarrier, bounded wait), 0 with per-thread 16-byte loads. */
+    int stage_bulk;
 } gstex_raster_inputs;
 
 /* Bytes of the records buffer of one view: 224 per Gaussian plus the list
@@ -390,6 +400,7 @@ typedef struct gstex_batch_inputs {
                                            null = each tile derives the records it stages */
     int group_lanes;                    /* lanes per splat walk of the launched kernel
                                            (see gstex_raster_inputs) */
+    int stage_bulk;                     /* forward: bulk-copy record staging (see gstex_raster_inputs) */
 } gstex_batch_inputs;
 
 /* Bytes of the per-(view, Gaussian) splat records of gstex_batch_records

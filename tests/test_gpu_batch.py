@@ -272,6 +272,41 @@ def test_forward_group_walk_does_not_change_outputs(setup):
             assert np.array_equal(outs[gs][k], outs[32][k]), (gs, k)
 
 
+def test_forward_group_walk_dense_tiles():
+    """The forward's lane groups on tiles with several batches of splats and
+    pixels that saturate, where a group falls back to walking every slot
+    while other groups of the same warp still walk their lists: outputs
+    bit-identical to the 32-lane walk for every group size, with per-thread
+    loads and with bulk-copy staging, and no bounded wait gave up."""
+    from gstex_cuda_gb300 import _lib, batch as B, synthetic
+    g = torch.Generator().manual_seed(29)
+    cams = synthetic.sphere_cameras(g, 2, radius=8.0, resolutions=[(128, 96), (96, 128)])
+    means = (0.3 * torch.randn(20_000, 3, generator=g))
+    spec = synthetic._finish_with_area(g, means, 0.05, 0.3, 3, "normal", cams, 60_000, "dense", {})
+    scene = B.Scene(means=spec.means.to(DEV), scales=spec.scales.to(DEV), quats=spec.quats.to(DEV),
+                    opacity=spec.opacity.to(DEV), sh_coeffs=spec.sh_coeffs.to(DEV), sh_degree=3,
+                    uv0=spec.uv0.to(DEV), umap=spec.umap.to(DEV), vmap=spec.vmap.to(DEV),
+                    texture_dims=spec.texture_dims.to(DEV), texture=spec.texture.to(DEV))
+    bcams = [B.Camera(c.viewmat, c.fx, c.fy, c.cx, c.cy, c.width, c.height) for c in cams]
+    outs = {}
+    for gs, bulk in ((32, False), (16, False), (8, False), (4, False), (32, True), (8, True)):
+        x = B.BatchRenderer(bcams, spec.num_points, capacity=4_000_000, fwd_group=gs, stage_bulk=bulk)
+        x.bin(scene)
+        x.forward(scene)
+        torch.cuda.synchronize()
+        assert x.check_capacity()
+        outs[gs, bulk] = {k: v.cpu().numpy() for k, v in x.out.items()}
+        if gs == 32 and not bulk:
+            cost = (x.bins[:, 1] - x.bins[:, 0]).cpu().numpy()
+            assert cost.max() > 3 * 256  # several batches per tile
+            # pixels whose T came within 1.01e-4 (the in-order fallback of their group)
+            assert (outs[gs, bulk]["final_T"] <= 1.01e-4).sum() >= 5
+    for key in outs:
+        for k in outs[32, False]:
+            assert np.array_equal(outs[key][k], outs[32, False][k]), (key, k)
+    assert _lib.lib().gstex_wait_timeouts() == 0
+
+
 def test_batch_graph_replay_matches_eager(setup):
     spec, cams, r, scene, _ = setup
     P = r.total_pixels

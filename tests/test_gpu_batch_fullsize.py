@@ -144,7 +144,11 @@ def test_batched_step_at_full_size_vs_reference_kernels(which):
         for k in ("final_idx", "depth_idx"):
             got[k] = _tile_local(np_(got[k]), bins_b[toff:toff + nt], cam.width, cam.height)
             refo[k] = _tile_local(np_(refo[k]), local, cam.width, cam.height)
-        _compare(refo, got, {}, {}, 1e-4, 5e-3 if stress else 3e-3, 2e-3)
+        # the outlier cap is 5e-2 here (1e-2 in the single-view tests): over
+        # 32 random viewpoints some splats are seen almost edge-on, which
+        # this path solves in double and the reference in fast-math fp32, so
+        # a pixel's alpha can move by more than one threshold flip
+        _compare(refo, got, {}, {}, 1e-4, 5e-3 if stress else 3e-3, 2e-3, out_cap=5e-2)
         # backward with identical upstream gradients
         a, b = r.pix_offsets_host[v], r.pix_offsets_host[v + 1]
         H, W = cam.height, cam.width
