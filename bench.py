@@ -63,6 +63,7 @@ def parse():
                    help="use the kernel variants given by --fwd-group/--bwd-group (profiling runs)")
     p.add_argument("--fwd-group", type=int, default=32)
     p.add_argument("--bwd-group", type=int, default=32)
+    p.add_argument("--stage-bulk", action="store_true")
     p.add_argument("--no-graph", action="store_true")
     return p.parse_args()
 
@@ -353,9 +354,9 @@ def main():
     I = r.intersections()
     log(f"intersections {I}, pixels {P}, tiles {r.total_tiles}, capacity {r.capacity}")
     if args.no_autotune:
-        r.fwd_group, r.bwd_group = args.fwd_group, args.bwd_group
-        tuned = {"fixed": True, "fwd_ppt": r.fwd_ppt, "fwd_group": r.fwd_group, "bwd_ppt": r.bwd_ppt,
-                 "bwd_group": r.bwd_group}
+        r.fwd_group, r.bwd_group, r.stage_bulk = args.fwd_group, args.bwd_group, args.stage_bulk
+        tuned = {"fixed": True, "fwd_ppt": r.fwd_ppt, "fwd_group": r.fwd_group, "stage_bulk": r.stage_bulk,
+                 "bwd_ppt": r.bwd_ppt, "bwd_group": r.bwd_group}
     else:
         tuned = r.autotune(scene, tgt_img, tgt_tex)
     log(f"autotune: {tuned}")

@@ -464,8 +464,9 @@ class BatchRenderer:
     # ------------------------------------------------------------------
     def autotune(self, s: Scene, tgt_img, tgt_tex, reps: int = 2) -> dict:
         """Choose pixels-per-thread and lanes per splat walk (32, 16, 8, 4) of
-        the forward and of the backward kernel by timing each candidate on this
-        scene and these cameras (CUDA events)."""
+        the forward and of the backward kernel, and whether the forward stages
+        records by bulk copies, by timing each candidate on this scene and
+        these cameras (CUDA events)."""
         stream = torch.cuda.current_stream(self.dev)
         self.bin(s)
 
@@ -487,6 +488,12 @@ class BatchRenderer:
             result[f"forward_ppt{ppt}_g{gs}_ms"] = ms
             best = (ms, ppt, gs) if best is None or ms < best[0] else best
         self.fwd_ppt, self.fwd_group = best[1], best[2]
+        # record staging by bulk copies, on the chosen forward variant
+        if self.records is not None:
+            self.stage_bulk = True
+            ms = timed(lambda: self.forward(s))
+            result["forward_bulk_staging_ms"] = ms
+            self.stage_bulk = ms < best[0]
         self.forward(s)
         self.image_loss(tgt_img, tgt_tex)
         best = None
@@ -496,8 +503,8 @@ class BatchRenderer:
             result[f"backward_ppt{ppt}_g{gs}_ms"] = ms
             best = (ms, ppt, gs) if best is None or ms < best[0] else best
         self.bwd_ppt, self.bwd_group = best[1], best[2]
-        result.update(fwd_ppt=self.fwd_ppt, fwd_group=self.fwd_group, bwd_ppt=self.bwd_ppt,
-                      bwd_group=self.bwd_group)
+        result.update(fwd_ppt=self.fwd_ppt, fwd_group=self.fwd_group, stage_bulk=self.stage_bulk,
+                      bwd_ppt=self.bwd_ppt, bwd_group=self.bwd_group)
         self.graph = None
         return result
 

@@ -321,3 +321,26 @@ def test_alpha_visualisation_forward_vs_oracle(extra):
     with pytest.raises(Exception):
         ups = upstream(case.cam.height, case.cam.width, case.spec.texture.shape[1])
         case.backward_cuda(out, b["gaussian_ids_sorted"], b["tile_bins"], ups, bw, settings, bgt)
+
+
+def test_forward_bulk_staging_bit_identical():
+    """texture_forward with the view's records staged by bulk copies (one
+    cp.async.bulk per record part, completing on a CTA mbarrier) gives the
+    same bits as per-thread loads, at block widths 16 and 8."""
+    import gstex_cuda_gb300.cuda as CU
+    from gstex_cuda_gb300 import _lib
+    case = Case(small_scene(n=500, width=96, height=80, seed=43))
+    old = CU.STAGE_BULK
+    try:
+        for bw in (16, 8):
+            b = case.binning_cuda(bw)
+            res = {}
+            for bulk in (False, True):
+                CU.STAGE_BULK = bulk
+                res[bulk], _ = case.forward_cuda(b["gaussian_ids_sorted"], b["tile_bins"], bw, 1 << 8)
+            torch.cuda.synchronize()
+            for k in res[False]:
+                assert torch.equal(res[True][k], res[False][k]), (bw, k)
+    finally:
+        CU.STAGE_BULK = old
+    assert _lib.lib().gstex_wait_timeouts() == 0
