@@ -60,10 +60,8 @@ def parse():
     p.add_argument("--no-refkern", action="store_true", help="skip timing the reference's kernels per view")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-autotune", action="store_true",
-                   help="use the kernel variants given by --fwd-group/--bwd-group (profiling runs)")
-    p.add_argument("--fwd-group", type=int, default=32)
-    p.add_argument("--bwd-group", type=int, default=32)
-    p.add_argument("--stage-bulk", action="store_true")
+                   help="use the backward variant given by --bwd-group (profiling runs)")
+    p.add_argument("--bwd-group", type=int, default=8)
     p.add_argument("--no-graph", action="store_true")
     return p.parse_args()
 
@@ -354,9 +352,8 @@ def main():
     I = r.intersections()
     log(f"intersections {I}, pixels {P}, tiles {r.total_tiles}, capacity {r.capacity}")
     if args.no_autotune:
-        r.fwd_group, r.bwd_group, r.stage_bulk = args.fwd_group, args.bwd_group, args.stage_bulk
-        tuned = {"fixed": True, "fwd_ppt": r.fwd_ppt, "fwd_group": r.fwd_group, "stage_bulk": r.stage_bulk,
-                 "bwd_ppt": r.bwd_ppt, "bwd_group": r.bwd_group}
+        r.bwd_group = args.bwd_group
+        tuned = {"fixed": True, "fwd_ppt": r.fwd_ppt, "bwd_ppt": r.bwd_ppt, "bwd_group": r.bwd_group}
     else:
         tuned = r.autotune(scene, tgt_img, tgt_tex)
     log(f"autotune: {tuned}")

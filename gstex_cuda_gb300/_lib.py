@@ -28,7 +28,7 @@ class RasterInputs(ctypes.Structure):
                 ("opacities", _P), ("means", _P), ("scales", _P), ("glob_scale", _F), ("quats", _P),
                 ("uv0", _P), ("umap", _P), ("vmap", _P), ("texture", _P), ("viewmat", _P),
                 ("fx", _F), ("fy", _F), ("cx", _F), ("cy", _F), ("settings", _I), ("background", _P),
-                ("pixels_per_thread", _I), ("records", _P), ("group_lanes", _I), ("stage_bulk", _I)]
+                ("pixels_per_thread", _I), ("records", _P), ("group_lanes", _I)]
 
 
 class EditIO(ctypes.Structure):
@@ -55,7 +55,6 @@ _SIGS = {
     "gstex_last_cuda_error": (ctypes.c_char_p, []),
     "gstex_version": (ctypes.c_char_p, []),
     "gstex_launch_count": (ctypes.c_ulonglong, []),
-    "gstex_wait_timeouts": (ctypes.c_uint, []),
     "gstex_get_aabb_2d": (_I, [_I, _P, _P, _F, _P, _P, _F, _F, _F, _F, _P, _P, _P]),
     "gstex_num_tiles_hit": (_I, [_I, _P, _P, _I, _I, _I, _P, _P]),
     "gstex_view_records_bytes": (ctypes.c_size_t, [_I]),

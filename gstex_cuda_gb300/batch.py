@@ -42,8 +42,7 @@ class BatchInputs(ctypes.Structure):
                 ("views", _P), ("tile_view", _P), ("tile_order", _P), ("gaussian_ids_sorted", _P), ("tile_bins", _P),
                 ("colors", _P), ("opacities", _P), ("means", _P), ("scales", _P), ("glob_scale", _F), ("quats", _P),
                 ("uv0", _P), ("umap", _P), ("vmap", _P), ("texture_dims", _P), ("texture", _P), ("background", _P),
-                ("queue", _P), ("grid", _I), ("pixels_per_thread", _I), ("records", _P), ("group_lanes", _I),
-                ("stage_bulk", _I)]
+                ("queue", _P), ("grid", _I), ("pixels_per_thread", _I), ("records", _P), ("group_lanes", _I)]
 
 
 class RawGrads(ctypes.Structure):
@@ -153,8 +152,7 @@ class BatchRenderer:
     def __init__(self, cameras: Sequence[Camera], num_points: int, *, channels: int = 3, texture_dtype=torch.float32,
                  block_width: int = 16, settings: int = 1 << 8, background=(0.0, 0.0, 0.0), capacity: int = 0,
                  device="cuda:0", grid: int = 0, loss_weights: Optional[dict] = None, fwd_ppt: int = 1,
-                 bwd_ppt: int = 1, fwd_group: int = 32, bwd_group: int = 32, stage_bulk: bool = False,
-                 prebuilt_records: bool = True, heavy_first: bool = True):
+                 bwd_ppt: int = 1, bwd_group: int = 32, prebuilt_records: bool = True, heavy_first: bool = True):
         self.dev = torch.device(device)
         self.N = int(num_points)
         self.V = len(cameras)
@@ -164,8 +162,7 @@ class BatchRenderer:
         self.texmode = 1 if texture_dtype == torch.bfloat16 else 0
         self.grid = int(grid)
         self.fwd_ppt, self.bwd_ppt = int(fwd_ppt), int(bwd_ppt)
-        self.fwd_group, self.bwd_group = int(fwd_group), int(bwd_group)
-        self.stage_bulk = bool(stage_bulk)
+        self.bwd_group = int(bwd_group)
         self.lw = dict(LOSS_WEIGHTS if loss_weights is None else loss_weights)
         L = _L()
         descs = (ViewDesc * self.V)()
@@ -273,8 +270,7 @@ class BatchRenderer:
         bi.texture_dims, bi.texture, bi.background = ptr(s.texture_dims), ptr(s.texture), ptr(self.bg)
         bi.queue, bi.grid = ptr(self.queue), self.grid
         bi.pixels_per_thread = self.bwd_ppt if backward else self.fwd_ppt
-        bi.group_lanes = self.bwd_group if backward else self.fwd_group
-        bi.stage_bulk = 0 if backward else int(self.stage_bulk)
+        bi.group_lanes = self.bwd_group if backward else 32
         bi.records = ptr(self.records) if self.records is not None else None
         return bi
 
@@ -463,10 +459,9 @@ class BatchRenderer:
 
     # ------------------------------------------------------------------
     def autotune(self, s: Scene, tgt_img, tgt_tex, reps: int = 2) -> dict:
-        """Choose pixels-per-thread and lanes per splat walk (32, 16, 8, 4) of
-        the forward and of the backward kernel, and whether the forward stages
-        records by bulk copies, by timing each candidate on this scene and
-        these cameras (CUDA events)."""
+        """Choose pixels-per-thread of the forward kernel, and pixels-per-thread
+        and lanes per splat walk (32, 16, 8, 4) of the backward kernel, by
+        timing each candidate on this scene and these cameras (CUDA events)."""
         stream = torch.cuda.current_stream(self.dev)
         self.bin(s)
 
@@ -482,18 +477,12 @@ class BatchRenderer:
 
         result = {}
         best = None
-        for ppt, gs in ((1, 32), (2, 32), (1, 16), (1, 8), (1, 4)):
-            self.fwd_ppt, self.fwd_group = ppt, gs
+        for ppt in (1, 2):
+            self.fwd_ppt = ppt
             ms = timed(lambda: self.forward(s))
-            result[f"forward_ppt{ppt}_g{gs}_ms"] = ms
-            best = (ms, ppt, gs) if best is None or ms < best[0] else best
-        self.fwd_ppt, self.fwd_group = best[1], best[2]
-        # record staging by bulk copies, on the chosen forward variant
-        if self.records is not None:
-            self.stage_bulk = True
-            ms = timed(lambda: self.forward(s))
-            result["forward_bulk_staging_ms"] = ms
-            self.stage_bulk = ms < best[0]
+            result[f"forward_ppt{ppt}_ms"] = ms
+            best = (ms, ppt) if best is None or ms < best[0] else best
+        self.fwd_ppt = best[1]
         self.forward(s)
         self.image_loss(tgt_img, tgt_tex)
         best = None
@@ -503,8 +492,7 @@ class BatchRenderer:
             result[f"backward_ppt{ppt}_g{gs}_ms"] = ms
             best = (ms, ppt, gs) if best is None or ms < best[0] else best
         self.bwd_ppt, self.bwd_group = best[1], best[2]
-        result.update(fwd_ppt=self.fwd_ppt, fwd_group=self.fwd_group, stage_bulk=self.stage_bulk,
-                      bwd_ppt=self.bwd_ppt, bwd_group=self.bwd_group)
+        result.update(fwd_ppt=self.fwd_ppt, bwd_ppt=self.bwd_ppt, bwd_group=self.bwd_group)
         self.graph = None
         return result
 

@@ -541,7 +541,6 @@ static int batch_scene(const gstex_batch_inputs* in, SceneArgs& a, BatchArgs& ba
     ba.vcolors = nullptr;
     ba.queue = in->queue;
     ba.recs = (const RecAll*)in->records;
-    ba.stage_bulk = in->stage_bulk;
     return GSTEX_OK;
 }
 
@@ -589,8 +588,8 @@ extern "C" int gstex_batch_forward(const gstex_batch_inputs* in, const gstex_for
     if (e != cudaSuccess) { set_cuda_error(e, "batch_forward"); return GSTEX_ERR_CUDA; }
     FwdOut o{ (float3*)out->img, out->depth, out->reg, out->texture, (float3*)out->normal, out->final_T,
               out->final_idx, out->depth_idx, (float3*)out->reg_s };
-    return launch_fwd_batch(a, ba, o, in->block_width, in->texture_dtype, in->pixels_per_thread, in->group_lanes,
-                            grid_of(in, false), stream);
+    return launch_fwd_batch(a, ba, o, in->block_width, in->texture_dtype, in->pixels_per_thread, grid_of(in, false),
+                            stream);
 }
 
 extern "C" size_t gstex_batch_backward_workspace_bytes(int num_points) {

@@ -63,66 +63,6 @@ __device__ __forceinline__ void stage_job(const Recs& R, int slot, const SceneAr
     }
 }
 
-// ---------------------------------------------------------------------------
-// Bulk staging: the hot, warm and cold parts of a prebuilt record copied into
-// their shared-memory slots by the copy engine (cp.async.bulk, no registers or
-// load/store instructions per 16 bytes), completing on a CTA mbarrier that the
-// batch waits on.  The barrier expects one arrival per thread; each thread
-// announces the bytes of its own copies (arrive.expect_tx) before issuing
-// them, so the barrier's transaction count never runs ahead of its
-// expectation.  Every wait is bounded: non-blocking polls with a short sleep,
-// at most kStageSpins of them (about 0.2 s); then the kernel counts the
-// time-out in g_wait_timeouts and stops (no tile is rendered from a batch that
-// did not arrive).
-// ---------------------------------------------------------------------------
-__device__ unsigned int g_wait_timeouts;
-constexpr int kStageSpins = 1 << 21;
-constexpr unsigned kStageBytes = sizeof(RecHot) + sizeof(RecWarm) + sizeof(RecCold);
-
-__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, unsigned parity) {
-    unsigned ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
-    for (int i = 0; i < kStageSpins; ++i) {
-        if (mbar_test_wait(bar, parity)) return true;
-        if (i >= 32) __nanosleep(100);
-    }
-    return false;
-}
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-            smem_u32(dst)),
-        "l"(src), "r"(bytes), "r"(smem_u32(bar))
-        : "memory");
-}
-
-// Issues the copies of the prebuilt record of Gaussian gid into slot.
-__device__ __forceinline__ void stage_bulk(const Recs& R, int slot, const TileJob& J, int gid, uint64_t* bar) {
-    const unsigned char* src = reinterpret_cast<const unsigned char*>(J.recs + gid);
-    bulk_g2s(R.hot + slot, src, sizeof(RecHot), bar);
-    bulk_g2s(R.warm + slot, src + sizeof(RecHot), sizeof(RecWarm), bar);
-    bulk_g2s(R.cold + slot, src + sizeof(RecHot) + sizeof(RecWarm), sizeof(RecCold), bar);
-}
-
 // Completes a Hit in the direct form, rebuilding the Gaussian's camera-space
 // frame from its parameters (rare: splats at the camera plane and pixels within
 // the reference's denominator clamp).
@@ -300,22 +240,8 @@ __device__ __forceinline__ int build_group_list(uint8_t* gl, const uint8_t* wl, 
 // bw x bw tile; each thread owns PPT vertically adjacent pixels, so every
 // staged record read from shared memory is used for PPT pixels.
 // ---------------------------------------------------------------------------
-//
-// GS < 32 (full warps only): each group of GS lanes (a compact pixel block,
-// see thread_pixel) walks its own list of the staged slots whose screen box
-// meets the group's pixels, so a warp composites 32 / GS splats at once.  A
-// skipped splat can still end a pixel whose T is within 1/(1 - 1/255) of the
-// 1e-4 limit (texture.cu:213-221): a group with such a pixel walks every slot
-// of the batch from then on, in order, as the reference does.
-//
-// With bar (a CTA mbarrier expecting one arrival per thread; phase its
-// current parity) and prebuilt records, each batch is staged by bulk copies;
-// returns false when a batch did not arrive within the bounded wait (the tile
-// is then not written).
-template <int TEXMODE, int CT, int PPT, int GS = 32>
-__device__ __forceinline__ bool fwd_tile(const SceneArgs& a, const TileJob& J, const FwdOut& o, const Recs& R,
-                                         uint8_t* lists, uint64_t* bar = nullptr, unsigned* phase = nullptr) {
-    static_assert(GS == 32 || GS == 16 || GS == 8 || GS == 4, "group of 32, 16, 8 or 4 lanes");
+template <int TEXMODE, int CT, int PPT>
+__device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, const FwdOut& o, const Recs& R) {
     const int nthr = blockDim.x * blockDim.y;
     const int tr = threadIdx.y * blockDim.x + threadIdx.x;
     const int bw = blockDim.x;
@@ -337,9 +263,8 @@ __device__ __forceinline__ bool fwd_tile(const SceneArgs& a, const TileJob& J, c
     const bool white_outline = a.settings & (1 << 24);
     const int C = CT >= 0 ? CT : a.C;
     constexpr int CA = CT > 0 ? CT : (CT == 0 ? 1 : kMaxChannels);
-    const int2 lp = thread_pixel<PPT, GS>(bw);
+    const int2 lp = thread_pixel<PPT>(bw);
     const int pj = J.tx * bw + lp.y;
-    const unsigned lane = tr & 31;
     PixelRay P[PPT];
     bool inside[PPT], done[PPT];
     float T[PPT], depth[PPT], reg[PPT];
@@ -363,52 +288,27 @@ __device__ __forceinline__ bool fwd_tile(const SceneArgs& a, const TileJob& J, c
 #pragma unroll
         for (int k = 0; k < CA; k++) otex[p][k] = 0.f;
     }
-    // GS < 32: the warp's and the group's rectangles of pixel centres, lists
-    float rx0 = 0.f, rx1 = 0.f, ry0 = 0.f, ry1 = 0.f, qx0 = 0.f, qx1 = 0.f, qy0 = 0.f, qy1 = 0.f;
-    unsigned gmask = 0u;
-    uint8_t* wl = lists + (tr >> 5) * nthr;
-    uint8_t* gl = lists + ((size_t)ceil_div(nthr, 32) + tr / GS) * nthr;
-    if (GS < 32) {
-        const int pi0 = J.ty * bw + lp.x;
-        rx0 = (float)__reduce_min_sync(0xffffffffu, pj) + 0.5f;
-        rx1 = (float)__reduce_max_sync(0xffffffffu, pj) + 0.5f;
-        ry0 = (float)__reduce_min_sync(0xffffffffu, pi0) + 0.5f;
-        ry1 = (float)__reduce_max_sync(0xffffffffu, pi0 + PPT - 1) + 0.5f;
-        qx0 = (float)group_min<GS>(pj) + 0.5f;
-        qx1 = (float)group_max<GS>(pj) + 0.5f;
-        qy0 = (float)group_min<GS>(pi0) + 0.5f;
-        qy1 = (float)group_max<GS>(pi0 + PPT - 1) + 0.5f;
-        gmask = ((1u << GS) - 1u) << (lane & ~(unsigned)(GS - 1));
-    }
     const int2 range = J.range;
     const int nb = ceil_div(range.y - range.x, nthr);
 
-    const bool bulk = bar != nullptr && J.recs != nullptr;
     for (int b = 0; b < nb; ++b) {
         if (__syncthreads_count(all_done) >= nthr) break;
         const int bstart = range.x + nthr * b;
         const int idx = bstart + tr;
+        if (idx < range.y) stage_job(R, tr, a, J, a.gids[idx], use_blur);
+        __syncthreads();
         const int bsize = min(nthr, range.y - bstart);
-        if (bulk) {
-            // the slots were last read before the barrier above
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            mbar_arrive_expect_tx(bar, idx < range.y ? kStageBytes : 0u);
-            if (idx < range.y) stage_bulk(R, tr, J, a.gids[idx], bar);
-            const bool ok = mbar_wait_bounded(bar, *phase);
-            if (__syncthreads_or(!ok)) {
-                if (tr == 0) atomicAdd(&g_wait_timeouts, 1u);
-                mbar_wait_bounded(bar, *phase);  // copies still in flight: one more bounded wait
-                return false;
-            }
-            *phase ^= 1u;
-        } else {
-            if (idx < range.y) stage_job(R, tr, a, J, a.gids[idx], use_blur);
-            __syncthreads();
-        }
         if (__all_sync(wmask, all_done)) continue;
-        // Composites staged slot k into this thread's pixels (those not done
-        // and, while T > 1.01e-4, inside the splat's alpha >= 1/255 box).
-        auto visit = [&](const int k) {
+        // Every staged slot in order; each pixel tests the splat's box first.
+        for (int k = 0; k < bsize; ++k) {
+            const float4 bx = R.hot[k].box;
+            bool need = false;
+#pragma unroll
+            for (int p = 0; p < PPT; p++) {
+                const bool out_box = P[p].px < bx.x || P[p].px > bx.y || P[p].py < bx.z || P[p].py > bx.w;
+                need = need || (!done[p] && !(out_box && T[p] > 1.01e-4f));
+            }
+            if (need) {
             const RecHot Hr = R.hot[k];
 #pragma unroll
             for (int p = 0; p < PPT; p++) {
@@ -477,63 +377,12 @@ __device__ __forceinline__ bool fwd_tile(const SceneArgs& a, const TileJob& J, c
                 T[p] = next_T;
                 cur[p] = bstart + k;
             }
-        };
-        auto update_done = [&]() {
+            }
             bool ad = true;
 #pragma unroll
             for (int p = 0; p < PPT; p++) ad = ad && done[p];
             all_done = ad;
-        };
-        if (GS == 32) {
-            // Every staged slot in order; each pixel tests the splat's box first.
-            for (int k = 0; k < bsize; ++k) {
-                const float4 bx = R.hot[k].box;
-                bool need = false;
-#pragma unroll
-                for (int p = 0; p < PPT; p++) {
-                    const bool out_box = P[p].px < bx.x || P[p].px > bx.y || P[p].py < bx.z || P[p].py > bx.w;
-                    need = need || (!done[p] && !(out_box && T[p] > 1.01e-4f));
-                }
-                if (need) visit(k);
-                update_done();
-                if (__all_sync(wmask, all_done)) break;
-            }
-        } else {
-            // the group's slots whose box meets its pixels (warp list, then the
-            // group's filter of it), or every slot once a pixel is near 1e-4
-            auto near_done = [&]() {
-                bool nd = false;
-#pragma unroll
-                for (int p = 0; p < PPT; p++) nd = nd || (!done[p] && T[p] <= 1.01e-4f);
-                return nd;
-            };
-            const int cntw = build_list(wl, R, 0, bsize, rx0, rx1, ry0, ry1, 0xffffffffu, lane);
-            const int cnt = build_group_list<GS>(gl, wl, cntw, R, 0, qx0, qx1, qy0, qy1, lane);
-            bool dense = (__ballot_sync(0xffffffffu, near_done()) & gmask) != 0;
-            int j = 0, kd = -1;
-            while (true) {
-                int k;
-                bool act;
-                if (dense) {
-                    k = kd + 1;
-                    act = k < bsize;
-                } else {
-                    act = j < cnt;
-                    k = act ? gl[j] : 0;
-                }
-                if (!__any_sync(0xffffffffu, act)) break;
-                if (act) visit(k);
-                if (dense) kd = k;
-                else ++j;
-                update_done();
-                if (__all_sync(0xffffffffu, all_done)) break;
-                // every lane takes part in the ballot (dense differs between groups)
-                const unsigned nd = __ballot_sync(0xffffffffu, act && near_done());
-                if (!dense && (nd & gmask)) {
-                    dense = true;
-                    kd = k;
-                }
-            }
+            if (__all_sync(wmask, all_done)) break;
         }
     }
 #pragma unroll
@@ -551,7 +400,6 @@ __device__ __forceinline__ bool fwd_tile(const SceneArgs& a, const TileJob& J, c
         o.reg_s[pix] = ts[p];
         for (int ch = 0; ch < C; ch++) o.tex[pix * C + ch] = otex[p][ch];
     }
-    return true;
 }
 
 // ---------------------------------------------------------------------------
@@ -1148,7 +996,7 @@ __global__ void __launch_bounds__(256, 4) edit_view_kernel(SceneArgs a, ViewArgs
 #define FWD_BOUNDS(PPT) __launch_bounds__((PPT) == 2 ? 128 : 256, (PPT) == 2 ? GSTEX_FWD_MINB : GSTEX_FWD_MINB1)
 #define BWD_BOUNDS(PPT) __launch_bounds__((PPT) == 2 ? 128 : 256, (PPT) == 2 ? GSTEX_BWD_MINB : GSTEX_BWD_MINB1)
 
-template <int TEXMODE, int CT, int PPT, int GS>
+template <int TEXMODE, int CT, int PPT>
 __global__ void FWD_BOUNDS(PPT) fwd_view_kernel(SceneArgs a, ViewArgs va, FwdOut o) {
     extern __shared__ __align__(16) unsigned char smem[];
     TileJob J;
@@ -1162,14 +1010,7 @@ __global__ void FWD_BOUNDS(PPT) fwd_view_kernel(SceneArgs a, ViewArgs va, FwdOut
     J.vc_stride = 3;
     J.recs = va.recs;
     const int nthr = blockDim.x * blockDim.y;
-    __shared__ uint64_t s_bar;
-    unsigned phase = 0;
-    if (va.stage_bulk && J.recs) {
-        if (threadIdx.x == 0 && threadIdx.y == 0) mbar_init(&s_bar, nthr);
-        __syncthreads();
-    }
-    fwd_tile<TEXMODE, CT, PPT, GS>(a, J, o, Recs::carve(smem, nthr, false), smem + (size_t)kRecBytes * nthr,
-                                   va.stage_bulk ? &s_bar : nullptr, &phase);
+    fwd_tile<TEXMODE, CT, PPT>(a, J, o, Recs::carve(smem, nthr, false));
 }
 
 template <int TEXMODE, int CT, int PPT, int GS>
@@ -1215,23 +1056,14 @@ __device__ __forceinline__ bool next_job(const BatchArgs& ba, int* s_tile, TileJ
     return true;
 }
 
-template <int TEXMODE, int CT, int PPT, int GS>
+template <int TEXMODE, int CT, int PPT>
 __global__ void FWD_BOUNDS(PPT) fwd_batch_kernel(SceneArgs a, BatchArgs ba, FwdOut o) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_tile;
     TileJob J;
     const int nthr = blockDim.x * blockDim.y;
     const Recs R = Recs::carve(smem, nthr, false);
-    uint8_t* lists = smem + (size_t)kRecBytes * nthr;
-    __shared__ uint64_t s_bar;
-    unsigned phase = 0;
-    const bool bulk = ba.stage_bulk && ba.recs;
-    if (bulk) {
-        if (threadIdx.x == 0 && threadIdx.y == 0) mbar_init(&s_bar, nthr);
-        __syncthreads();
-    }
-    while (next_job(ba, &s_tile, J))
-        if (!fwd_tile<TEXMODE, CT, PPT, GS>(a, J, o, R, lists, bulk ? &s_bar : nullptr, &phase)) break;
+    while (next_job(ba, &s_tile, J)) fwd_tile<TEXMODE, CT, PPT>(a, J, o, R);
 }
 
 template <int TEXMODE, int CT, int PPT, int GS>
@@ -1477,9 +1309,9 @@ int gs_of(int bw, int ppt, int C, int requested) {
     if ((bw & 7) != 0 || ppt != 1 || (C != 0 && C != 3)) return 32;
     return (requested == 16 || requested == 8 || requested == 4) ? requested : 32;
 }
-// Kernel variant of (channels, texel type, pixels per thread, lanes per splat
-// walk gs from gs_of): 1 or 2 pixels per thread with gs = 32; gs < 32 with
-// one pixel per thread and 0 or 3 channels.
+// Backward kernel variant of (channels, texel type, pixels per thread, lanes
+// per splat walk gs from gs_of): 1 or 2 pixels per thread with gs = 32;
+// gs < 32 with one pixel per thread and 0 or 3 channels.
 template <template <int, int, int, int> class Sel>
 static typename Sel<0, 0, 1, 32>::type pick(int C, int texmode, int ppt, int gs) {
     if (gs == 16) {
@@ -1503,20 +1335,27 @@ static typename Sel<0, 0, 1, 32>::type pick(int C, int texmode, int ppt, int gs)
     if (C == 3) return texmode == 1 ? Sel<1, 3, 1, 32>::get() : Sel<0, 3, 1, 32>::get();
     return Sel<0, -1, 1, 32>::get();
 }
-// Forward kernel: the alpha-visualisation variants (settings bit 16) come
-// with 1 pixel per thread, gs = 32 and the generic fp32 or the bf16 texel path.
-template <template <int, int, int, int> class Sel>
-static typename Sel<0, 0, 1, 32>::type pick_fwd(int C, int texmode, int& ppt, int& gs, int settings) {
+// Forward kernel (pixels per thread only): the alpha-visualisation variants
+// (settings bit 16) come with 1 pixel per thread and the generic fp32 or the
+// bf16 texel path.
+template <template <int, int, int> class Sel>
+static typename Sel<0, 0, 1>::type pick_fwd(int C, int texmode, int& ppt, int settings) {
     if (settings & (1 << 16)) {
         ppt = 1;
-        gs = 32;
-        return texmode == 1 ? Sel<3, 3, 1, 32>::get() : Sel<2, -1, 1, 32>::get();
+        return texmode == 1 ? Sel<3, 3, 1>::get() : Sel<2, -1, 1>::get();
     }
-    return pick<Sel>(C, texmode, ppt, gs);
+    if (ppt == 2) {
+        if (C == 0) return Sel<0, 0, 2>::get();
+        if (C == 3) return texmode == 1 ? Sel<1, 3, 2>::get() : Sel<0, 3, 2>::get();
+        return Sel<0, -1, 2>::get();
+    }
+    if (C == 0) return Sel<0, 0, 1>::get();
+    if (C == 3) return texmode == 1 ? Sel<1, 3, 1>::get() : Sel<0, 3, 1>::get();
+    return Sel<0, -1, 1>::get();
 }
-template <int M, int C, int P, int G> struct FwdView { typedef void (*type)(SceneArgs, ViewArgs, FwdOut); static type get() { return fwd_view_kernel<M, C, P, G>; } };
+template <int M, int C, int P> struct FwdView { typedef void (*type)(SceneArgs, ViewArgs, FwdOut); static type get() { return fwd_view_kernel<M, C, P>; } };
 template <int M, int C, int P, int G> struct BwdView { typedef void (*type)(SceneArgs, ViewArgs, BwdArgs); static type get() { return bwd_view_kernel<M, C, P, G>; } };
-template <int M, int C, int P, int G> struct FwdBatch { typedef void (*type)(SceneArgs, BatchArgs, FwdOut); static type get() { return fwd_batch_kernel<M, C, P, G>; } };
+template <int M, int C, int P> struct FwdBatch { typedef void (*type)(SceneArgs, BatchArgs, FwdOut); static type get() { return fwd_batch_kernel<M, C, P>; } };
 template <int M, int C, int P, int G> struct BwdBatch { typedef void (*type)(SceneArgs, BatchArgs, BwdArgs); static type get() { return bwd_batch_kernel<M, C, P, G>; } };
 
 static dim3 block_of(int bw, int ppt) { return dim3(bw, bw / ppt); }
@@ -1526,9 +1365,7 @@ static size_t list_bytes(int bw, int ppt, int gs) {
     const int n = threads_of(bw, ppt);
     return ((size_t)ceil_div(n, 32) + (gs < 32 ? (size_t)ceil_div(n, gs) : 0)) * n;
 }
-size_t fwd_smem(int bw, int ppt, int gs) {
-    return (size_t)kRecBytes * threads_of(bw, ppt) + (gs < 32 ? list_bytes(bw, ppt, gs) : 0);
-}
+size_t fwd_smem(int bw, int ppt) { return (size_t)kRecBytes * threads_of(bw, ppt); }
 size_t bwd_smem(int bw, int ppt, int gs) {
     // ... then one "touched" flag per slot
     return ((size_t)kRecBytes + kEdgeBytes + kMomSlot * sizeof(float) + 1) * threads_of(bw, ppt) +
@@ -1545,12 +1382,11 @@ int launch_finalize(const SceneArgs& a, const float* moments, float* v_opac, flo
     return check_launch("finalize");
 }
 
-int launch_fwd_batch(const SceneArgs& a, const BatchArgs& ba, const FwdOut& o, int bw, int texmode, int ppt, int gs,
-                     int grid, cudaStream_t stream) {
+int launch_fwd_batch(const SceneArgs& a, const BatchArgs& ba, const FwdOut& o, int bw, int texmode, int ppt, int grid,
+                     cudaStream_t stream) {
     ppt = ppt_of(bw, ppt);
-    gs = gs_of(bw, ppt, a.C, gs);
-    auto k = pick_fwd<FwdBatch>(a.C, texmode, ppt, gs, a.settings);
-    const size_t smem = fwd_smem(bw, ppt, gs);
+    auto k = pick_fwd<FwdBatch>(a.C, texmode, ppt, a.settings);
+    const size_t smem = fwd_smem(bw, ppt);
     int rc = set_smem(k, smem, "batch forward");
     if (rc) return rc;
     k<<<grid, block_of(bw, ppt), smem, stream>>>(a, ba, o);
@@ -1583,8 +1419,8 @@ int resident_ctas(int bw, bool backward, int texmode, int C, int ppt, int gs) {
         if (set_smem(k, smem, "occupancy")) return 0;
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, threads_of(bw, ppt), smem);
     } else {
-        auto k = pick<FwdBatch>(C, texmode, ppt, gs);
-        const size_t smem = fwd_smem(bw, ppt, gs);
+        auto k = pick_fwd<FwdBatch>(C, texmode, ppt, 0);
+        const size_t smem = fwd_smem(bw, ppt);
         if (set_smem(k, smem, "occupancy")) return 0;
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, threads_of(bw, ppt), smem);
     }
@@ -1609,22 +1445,11 @@ static ViewArgs view_args(const gstex_raster_inputs* in) {
     va.colors = (const float3*)in->colors;
     va.vcolors = nullptr;
     va.recs = (const RecAll*)in->records;
-    va.stage_bulk = in->stage_bulk;
     return va;
 }
 
 // records [N], then the count and list of deferred near-edge-on records
 static size_t view_records_fix_offset(int n) { return (size_t)n * sizeof(RecAll); }
-
-extern "C" unsigned int gstex_wait_timeouts(void) {
-    unsigned int n = 0;
-    cudaError_t e = cudaMemcpyFromSymbol(&n, g_wait_timeouts, sizeof(n));
-    if (e != cudaSuccess) {
-        set_cuda_error(e, "wait_timeouts");
-        return 0xffffffffu;
-    }
-    return n;
-}
 
 extern "C" size_t gstex_view_records_bytes(int num_points) {
     const int n = num_points > 0 ? num_points : 0;
@@ -1666,9 +1491,8 @@ extern "C" int gstex_texture_forward(const gstex_raster_inputs* in, const gstex_
     cudaStream_t stream = (cudaStream_t)s;
     const dim3 grid(va.tiles_x, ceil_div(va.H, bw));
     int ppt = ppt_of(bw, in->pixels_per_thread);
-    int gs = gs_of(bw, ppt, a.C, in->group_lanes);
-    auto k = pick_fwd<FwdView>(a.C, in->texture_dtype, ppt, gs, a.settings);
-    const size_t smem = fwd_smem(bw, ppt, gs);
+    auto k = pick_fwd<FwdView>(a.C, in->texture_dtype, ppt, a.settings);
+    const size_t smem = fwd_smem(bw, ppt);
     if ((rc = set_smem(k, smem, "texture_forward"))) return rc;
     k<<<grid, block_of(bw, ppt), smem, stream>>>(a, va, o);
     return check_launch("texture_forward");

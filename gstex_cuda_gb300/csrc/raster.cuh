@@ -36,7 +36,6 @@ struct ViewArgs {
     const float3* colors;
     float* vcolors;       // [N,3] colour gradients (backward)
     const RecAll* recs;   // optional [N] prebuilt records of the view; null: built per tile
-    int stage_bulk;       // forward: stage prebuilt records with bulk copies
 };
 
 // Per-view constants of a batched launch (device array).
@@ -59,7 +58,6 @@ struct BatchArgs {
     float* vcolors;            // [V, N, 4] (rgb + pad: one vector atomic per flush)
     int* queue;                // tile counter, zero before each launch
     const RecAll* recs;        // optional [V, N] prebuilt records; null: built per tile
-    int stage_bulk;            // forward: stage prebuilt records with bulk copies
 };
 
 // What one CTA needs to render one tile.
@@ -105,10 +103,10 @@ struct BwdArgs {
 int fill_scene(const gstex_raster_inputs* in, SceneArgs& a, bool need_bins);
 int ppt_of(int bw, int requested);
 int gs_of(int bw, int ppt, int C, int requested);
-size_t fwd_smem(int bw, int ppt, int gs);
+size_t fwd_smem(int bw, int ppt);
 size_t bwd_smem(int bw, int ppt, int gs);
-int launch_fwd_batch(const SceneArgs& a, const BatchArgs& ba, const FwdOut& o, int bw, int texmode, int ppt, int gs,
-                     int grid, cudaStream_t stream);
+int launch_fwd_batch(const SceneArgs& a, const BatchArgs& ba, const FwdOut& o, int bw, int texmode, int ppt, int grid,
+                     cudaStream_t stream);
 int launch_bwd_batch(const SceneArgs& a, const BatchArgs& ba, const BwdArgs& g, int bw, int texmode, int ppt, int gs,
                      int grid, cudaStream_t stream);
 // Gradients w.r.t. the trainer's raw parameters (raw_quats == nullptr: the

@@ -180,16 +180,11 @@ def _texture_mode(texture, channels):
 
 
 PIXELS_PER_THREAD = 1  # 1 or 2 (2 halves the threads per tile; even block widths only)
-# Lanes that walk one list of staged splats in texture_forward /
-# texture_backward: 32 (a warp's 8x4 pixel block), 16 (4x4), 8 (4x2) or 4
-# (2x2); below 32 only for block widths that are multiples of 8, one pixel per
-# thread and 0 or 3 channels (else 32).
-FORWARD_GROUP_LANES = 32
+# Lanes that walk one list of staged splats in texture_backward: 32 (a
+# warp's 8x4 pixel block), 16 (4x4), 8 (4x2) or 4 (2x2); below 32 only for
+# block widths that are multiples of 8, one pixel per thread and 0 or 3
+# channels (else 32).
 BACKWARD_GROUP_LANES = 32
-# texture_forward with prebuilt records: stage each batch of records into
-# shared memory with bulk copies (cp.async.bulk on an mbarrier) instead of
-# per-thread 16-byte loads.
-STAGE_BULK = False
 # texture_forward / texture_backward build one splat record per Gaussian of the
 # view first (gstex_view_records) and the tiles copy them; False: every tile
 # derives the records of its Gaussians itself.
@@ -257,8 +252,6 @@ def texture_forward(tile_bounds, block, img_size, texture_info, texture_dims, ga
     ri, C = _raster_inputs(W, H, bw, texture_info, texture_dims, gaussian_ids_sorted, tile_bins, colors, opacities,
                            means, scales, glob_scale, quats, uv0, umap, vmap, texture, viewmat, fx, fy, cx, cy,
                            settings, background)
-    ri.group_lanes = int(FORWARD_GROUP_LANES)
-    ri.stage_bulk = int(bool(STAGE_BULK))
     dev = means.device
     f32 = dict(dtype=torch.float32, device=dev)
     out_img = torch.empty((H, W, 3), **f32)

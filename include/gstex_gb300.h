@@ -41,12 +41,6 @@ const char* gstex_last_cuda_error(void);
 const char* gstex_version(void);
 /* Number of kernels this library has launched since it was loaded. */
 unsigned long long gstex_launch_count(void);
-/* Number of bounded device-side waits (bulk-copy staging) that gave up on
- * the current device since the library was loaded; a kernel whose wait gives
- * up stops without writing the tiles it had not finished.  Synchronous
- * (reads device memory); 0xffffffff if the read fails.  No counterpart in the
- * reference, whose kernels have no waits. */
-unsigned int gstex_wait_timeouts(void);
 
 /* ---------------------------------------------------------------------
  * Projection
@@ -186,17 +180,12 @@ typedef struct gstex_raster_inputs {
      * of its Gaussians itself.  Read by texture_forward / texture_backward,
      * not by texture_edit. */
     const void* records;
-    /* Lanes of the launched compositor kernel (texture_forward or
-     * texture_backward) that walk one list of staged splats: 32 (a warp's
-     * 8x4 pixel block), 16 (4x4), 8 (4x2) or 4 (2x2); 0 = 32.  Values below
-     * 32 apply to block widths that are multiples of 8, one pixel per thread
-     * and 0 or 3 channels; elsewhere 32 is used.  Results do not depend on
-     * it beyond float summation order. */
+    /* texture_backward: lanes that walk one list of staged splats, 32 (a
+     * warp's 8x4 pixel block), 16 (4x4), 8 (4x2) or 4 (2x2); 0 = 32.  Values
+     * below 32 apply to block widths that are multiples of 8, one pixel per
+     * thread and 0 or 3 channels; elsewhere 32 is used.  Gradients do not
+     * depend on it beyond float summation order.  texture_forward ignores it. */
     int group_lanes;
-    /* texture_forward with records: 1 stages each batch of records into
-     * shared memory with bulk copies (cp.async.bulk completing on a CTA
-     * mbarrier, bounded wait), 0 with per-thread 16-byte loads. */
-    int stage_bulk;
 } gstex_raster_inputs;
 
 /* Bytes of the records buffer of one view: 224 per Gaussian plus the list
@@ -398,9 +387,7 @@ typedef struct gstex_batch_inputs {
     int pixels_per_thread;              /* 0 = default (1); 2 needs an even block width */
     const void* records;                /* optional: gstex_batch_records output (16-byte aligned);
                                            null = each tile derives the records it stages */
-    int group_lanes;                    /* lanes per splat walk of the launched kernel
-                                           (see gstex_raster_inputs) */
-    int stage_bulk;                     /* forward: bulk-copy record staging (see gstex_raster_inputs) */
+    int group_lanes;                    /* backward: lanes per splat walk (see gstex_raster_inputs) */
 } gstex_batch_inputs;
 
 /* Bytes of the per-(view, Gaussian) splat records of gstex_batch_records

@@ -26,7 +26,7 @@ def setup(request):
                     texture_dims=spec.texture_dims.to(DEV), texture=spec.texture.to(DEV))
     bcams = [B.Camera(c.viewmat, c.fx, c.fy, c.cx, c.cy, c.width, c.height) for c in cams]
     r = B.BatchRenderer(bcams, spec.num_points, capacity=1 << 20, fwd_ppt=request.param[0],
-                        bwd_ppt=request.param[1], fwd_group=request.param[2], bwd_group=request.param[2])
+                        bwd_ppt=request.param[1], bwd_group=request.param[2])
     P = r.total_pixels
     gen = torch.Generator().manual_seed(1)
     tgt_img = torch.rand(P, 3, generator=gen).to(DEV)
@@ -238,7 +238,7 @@ def test_forward_tile_order_does_not_change_outputs(setup):
     spec, cams, r, scene, _ = setup
     bcams = [B.Camera(c.viewmat, c.fx, c.fy, c.cx, c.cy, c.width, c.height) for c in cams]
     r2 = B.BatchRenderer(bcams, spec.num_points, capacity=1 << 20, fwd_ppt=r.fwd_ppt, bwd_ppt=r.bwd_ppt,
-                         fwd_group=r.fwd_group, bwd_group=r.bwd_group, heavy_first=False)
+                         bwd_group=r.bwd_group, heavy_first=False)
     assert r.tile_order is not None and r2.tile_order is None
     for x in (r, r2):
         x.bin(scene)
@@ -249,62 +249,6 @@ def test_forward_tile_order_does_not_change_outputs(setup):
     assert np.array_equal(np.sort(order), np.arange(r.total_tiles)) and np.all(np.diff(cost[order]) <= 0)
     for k in ("img", "depth", "reg", "texture", "normal", "final_T", "final_idx", "depth_idx", "reg_s"):
         assert np.array_equal(r.out[k].cpu().numpy(), r2.out[k].cpu().numpy()), k
-
-
-def test_forward_group_walk_does_not_change_outputs(setup):
-    """Lanes per splat walk of the forward (32: every slot in order, each
-    pixel testing the splat's box; 16 / 8 / 4: each lane group walks the
-    slots whose box meets its pixels, or every slot once a pixel's T nears
-    1e-4) change which lanes run together, not what a pixel composites: the
-    outputs are bit-identical."""
-    from gstex_cuda_gb300 import batch as B
-    spec, cams, r, scene, _ = setup
-    bcams = [B.Camera(c.viewmat, c.fx, c.fy, c.cx, c.cy, c.width, c.height) for c in cams]
-    outs = {}
-    for gs in (32, 16, 8, 4):
-        x = B.BatchRenderer(bcams, spec.num_points, capacity=1 << 20, fwd_group=gs)
-        x.bin(scene)
-        x.forward(scene)
-        torch.cuda.synchronize()
-        outs[gs] = {k: v.cpu().numpy() for k, v in x.out.items()}
-    for gs in (16, 8, 4):
-        for k in outs[32]:
-            assert np.array_equal(outs[gs][k], outs[32][k]), (gs, k)
-
-
-def test_forward_group_walk_dense_tiles():
-    """The forward's lane groups on tiles with several batches of splats and
-    pixels that saturate, where a group falls back to walking every slot
-    while other groups of the same warp still walk their lists: outputs
-    bit-identical to the 32-lane walk for every group size, with per-thread
-    loads and with bulk-copy staging, and no bounded wait gave up."""
-    from gstex_cuda_gb300 import _lib, batch as B, synthetic
-    g = torch.Generator().manual_seed(29)
-    cams = synthetic.sphere_cameras(g, 2, radius=8.0, resolutions=[(128, 96), (96, 128)])
-    means = (0.3 * torch.randn(20_000, 3, generator=g))
-    spec = synthetic._finish_with_area(g, means, 0.05, 0.3, 3, "normal", cams, 60_000, "dense", {})
-    scene = B.Scene(means=spec.means.to(DEV), scales=spec.scales.to(DEV), quats=spec.quats.to(DEV),
-                    opacity=spec.opacity.to(DEV), sh_coeffs=spec.sh_coeffs.to(DEV), sh_degree=3,
-                    uv0=spec.uv0.to(DEV), umap=spec.umap.to(DEV), vmap=spec.vmap.to(DEV),
-                    texture_dims=spec.texture_dims.to(DEV), texture=spec.texture.to(DEV))
-    bcams = [B.Camera(c.viewmat, c.fx, c.fy, c.cx, c.cy, c.width, c.height) for c in cams]
-    outs = {}
-    for gs, bulk in ((32, False), (16, False), (8, False), (4, False), (32, True), (8, True)):
-        x = B.BatchRenderer(bcams, spec.num_points, capacity=4_000_000, fwd_group=gs, stage_bulk=bulk)
-        x.bin(scene)
-        x.forward(scene)
-        torch.cuda.synchronize()
-        assert x.check_capacity()
-        outs[gs, bulk] = {k: v.cpu().numpy() for k, v in x.out.items()}
-        if gs == 32 and not bulk:
-            cost = (x.bins[:, 1] - x.bins[:, 0]).cpu().numpy()
-            assert cost.max() > 3 * 256  # several batches per tile
-            # pixels whose T came within 1.01e-4 (the in-order fallback of their group)
-            assert (outs[gs, bulk]["final_T"] <= 1.01e-4).sum() >= 5
-    for key in outs:
-        for k in outs[32, False]:
-            assert np.array_equal(outs[key][k], outs[32, False][k]), (key, k)
-    assert _lib.lib().gstex_wait_timeouts() == 0
 
 
 def test_batch_graph_replay_matches_eager(setup):
@@ -332,7 +276,7 @@ def test_prebuilt_records_match_per_tile_records(setup):
     spec, cams, r, scene, loss = setup
     bcams = [B.Camera(c.viewmat, c.fx, c.fy, c.cx, c.cy, c.width, c.height) for c in cams]
     r2 = B.BatchRenderer(bcams, spec.num_points, capacity=1 << 20, fwd_ppt=r.fwd_ppt, bwd_ppt=r.bwd_ppt,
-                         fwd_group=r.fwd_group, bwd_group=r.bwd_group, prebuilt_records=False)
+                         bwd_group=r.bwd_group, prebuilt_records=False)
     gen = torch.Generator().manual_seed(1)
     tgt_img = torch.rand(r.total_pixels, 3, generator=gen).to(DEV)
     tgt_tex = torch.rand(r.total_pixels, 3, generator=gen).to(DEV)
@@ -473,7 +417,7 @@ def test_raw_parameter_step_matches_preprocess_then_step(setup):
     path: the standalone preprocess kernel, the step on the activated scene,
     and the preprocess adjoint on the activated gradients.  Same loss and raw
     gradients up to float rounding; the activated parameters it wrote equal
-    the preprocess kernel's to a few ulp."""
+    the preprocess kernel's to a few ulp of the largest entry."""
     from gstex_cuda_gb300 import batch as B
     from gstex_cuda_gb300.preprocess import preprocess
     spec, cams, r, scene, _ = setup
@@ -492,7 +436,8 @@ def test_raw_parameter_step_matches_preprocess_then_step(setup):
     sc, qu, u0, um, vm, op = preprocess(*leaves)
     for k, v in zip(("scales", "quats", "uv0", "umap", "vmap", "opacity"), (sc, qu, u0, um, vm, op)):
         ref = v.detach().reshape(act[k].shape)
-        assert torch.allclose(act[k], ref, rtol=2e-6, atol=1e-6), k
+        # fused and standalone kernels differ in multiply-add contraction only
+        assert float((act[k] - ref).abs().max()) <= 2e-6 * float(ref.abs().max()), k
     s2 = B.Scene(means=scene.means, scales=sc.detach().contiguous(), quats=qu.detach().contiguous(),
                  opacity=op.detach().contiguous(), sh_coeffs=scene.sh_coeffs, sh_degree=3,
                  uv0=u0.detach().contiguous(), umap=um.detach().contiguous(), vmap=vm.detach().contiguous(),

@@ -213,14 +213,13 @@ def test_raster_tiny_matches_reference_golden():
 
 @pytest.fixture(params=[(1, 32), (2, 32), (1, 16), (1, 8), (1, 4)], ids=["1px", "2px", "1px_g16", "1px_g8", "1px_g4"])
 def pixels_per_thread(request):
-    """Pixels per thread, and lanes per splat walk of both compositor kernels
-    (group sizes below 32 apply to block widths that are multiples of 8)."""
+    """Pixels per thread, and lanes per splat walk of the backward (group
+    sizes below 32 apply to block widths that are multiples of 8)."""
     import gstex_cuda_gb300.cuda as C
-    old = C.PIXELS_PER_THREAD, C.FORWARD_GROUP_LANES, C.BACKWARD_GROUP_LANES
-    ppt, gs = request.param
-    C.PIXELS_PER_THREAD, C.FORWARD_GROUP_LANES, C.BACKWARD_GROUP_LANES = ppt, gs, gs
-    yield ppt
-    C.PIXELS_PER_THREAD, C.FORWARD_GROUP_LANES, C.BACKWARD_GROUP_LANES = old
+    old = C.PIXELS_PER_THREAD, C.BACKWARD_GROUP_LANES
+    C.PIXELS_PER_THREAD, C.BACKWARD_GROUP_LANES = request.param
+    yield request.param[0]
+    C.PIXELS_PER_THREAD, C.BACKWARD_GROUP_LANES = old
 
 
 @pytest.mark.parametrize("w,h,bw", [(64, 64, 16), (48, 32, 16), (70, 45, 8), (33, 29, 5), (40, 30, 10)])
@@ -322,25 +321,3 @@ def test_alpha_visualisation_forward_vs_oracle(extra):
         ups = upstream(case.cam.height, case.cam.width, case.spec.texture.shape[1])
         case.backward_cuda(out, b["gaussian_ids_sorted"], b["tile_bins"], ups, bw, settings, bgt)
 
-
-def test_forward_bulk_staging_bit_identical():
-    """texture_forward with the view's records staged by bulk copies (one
-    cp.async.bulk per record part, completing on a CTA mbarrier) gives the
-    same bits as per-thread loads, at block widths 16 and 8."""
-    import gstex_cuda_gb300.cuda as CU
-    from gstex_cuda_gb300 import _lib
-    case = Case(small_scene(n=500, width=96, height=80, seed=43))
-    old = CU.STAGE_BULK
-    try:
-        for bw in (16, 8):
-            b = case.binning_cuda(bw)
-            res = {}
-            for bulk in (False, True):
-                CU.STAGE_BULK = bulk
-                res[bulk], _ = case.forward_cuda(b["gaussian_ids_sorted"], b["tile_bins"], bw, 1 << 8)
-            torch.cuda.synchronize()
-            for k in res[False]:
-                assert torch.equal(res[True][k], res[False][k]), (bw, k)
-    finally:
-        CU.STAGE_BULK = old
-    assert _lib.lib().gstex_wait_timeouts() == 0
