@@ -152,7 +152,7 @@ class BatchRenderer:
     def __init__(self, cameras: Sequence[Camera], num_points: int, *, channels: int = 3, texture_dtype=torch.float32,
                  block_width: int = 16, settings: int = 1 << 8, background=(0.0, 0.0, 0.0), capacity: int = 0,
                  device="cuda:0", grid: int = 0, loss_weights: Optional[dict] = None, fwd_ppt: int = 1,
-                 bwd_ppt: int = 1, bwd_group: int = 32, prebuilt_records: bool = True, heavy_first: bool = True):
+                 bwd_ppt: int = 1, bwd_group: int = 8, prebuilt_records: bool = True, heavy_first: bool = True):
         self.dev = torch.device(device)
         self.N = int(num_points)
         self.V = len(cameras)

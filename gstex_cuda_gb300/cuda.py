@@ -183,8 +183,8 @@ PIXELS_PER_THREAD = 1  # 1 or 2 (2 halves the threads per tile; even block width
 # Lanes that walk one list of staged splats in texture_backward: 32 (a
 # warp's 8x4 pixel block), 16 (4x4), 8 (4x2) or 4 (2x2); below 32 only for
 # block widths that are multiples of 8, one pixel per thread and 0 or 3
-# channels (else 32).
-BACKWARD_GROUP_LANES = 32
+# channels (else 32).  8 measured fastest on the benchmark scenes.
+BACKWARD_GROUP_LANES = 8
 # texture_forward / texture_backward build one splat record per Gaussian of the
 # view first (gstex_view_records) and the tiles copy them; False: every tile
 # derives the records of its Gaussians itself.
