@@ -18,8 +18,6 @@
 // Two launch forms share the per-tile bodies: one CTA per tile of a single
 // view (the reference's texture_forward/backward), and a persistent kernel
 // that pulls tiles of many views from one global queue (batched rendering).
-#include <cstdlib>
-
 #include "common.cuh"
 #include "raster.cuh"
 
@@ -461,58 +459,13 @@ struct BwdPix {
     float vtex[CA];
 };
 
-// Texel-gradient contributions of one pair (bf16 [T, 4] texels): the four
-// bilinear corner rows and the weighted channel gradients; row[0] < 0 when
-// the lane has none.
-struct TexAcc {
-    int row[4];
-    float v[4][3];
-};
-
-// Adds every lane's TexAcc to the texel gradients with one 16-byte atomic per
-// corner per distinct texel cell: lanes whose pairs fall in the same cell of
-// the same chart (same four rows) are matched, their contributions summed by
-// the lowest such lane through shuffles, and only that lane adds.  All 32
-// lanes call it.
-__device__ __forceinline__ void tex_atomics_aggregated(float* v_texgrad, const TexAcc& ta, unsigned lane) {
-    const int key = ta.row[0] >= 0 ? ta.row[0] : -1 - (int)lane;
-    const unsigned peers = __match_any_sync(0xffffffffu, key);
-    const bool lead = (int)lane == __ffs(peers) - 1;
-    unsigned rem = lead ? (peers & ~(1u << lane)) : 0u;
-    const int iters = __reduce_max_sync(0xffffffffu, __popc(rem));
-    float s[4][3];
-#pragma unroll
-    for (int q = 0; q < 4; q++)
-#pragma unroll
-        for (int c = 0; c < 3; c++) s[q][c] = ta.v[q][c];
-    for (int t = 0; t < iters; t++) {
-        const int src = rem ? __ffs(rem) - 1 : (int)lane;
-        rem &= rem - 1u;
-#pragma unroll
-        for (int q = 0; q < 4; q++)
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                const float x = __shfl_sync(0xffffffffu, ta.v[q][c], src);
-                if (src != (int)lane) s[q][c] += x;
-            }
-    }
-    if (lead && ta.row[0] >= 0) {
-#pragma unroll
-        for (int q = 0; q < 4; q++)
-            if (s[q][0] != 0.f || s[q][1] != 0.f || s[q][2] != 0.f)
-                atomicAdd(reinterpret_cast<float4*>(v_texgrad) + ta.row[q], make_float4(s[q][0], s[q][1], s[q][2], 0.f));
-    }
-}
-
 // Adjoint of one (pixel, Gaussian) pair; adds its moments to m and returns
-// false when the pair is skipped.  Follows csrc/texture.cu:577-708.  With ta
-// (bf16 texels, 3 channels) the texel-gradient contributions are returned in
-// it instead of added.
+// false when the pair is skipped.  Follows csrc/texture.cu:577-708.
 template <int TEXMODE, int CT, int CA>
 __device__ __forceinline__ void bwd_pair(const SceneArgs& a, const BwdArgs& g, const Recs& R, int k, int gidx,
                                          const RecHot& Hr, const Hit& H, float alpha, float e, float eb, float nbf,
                                          float bf, BwdPix<CA>& S, int C, bool use_ndc, bool prop_uv, bool bilinear,
-                                         float (&m)[kMoments], TexAcc* ta = nullptr) {
+                                         float (&m)[kMoments]) {
     const RecWarm& Wm = R.warm[k];
     const float4 col = Wm.col, nw = Wm.nrm;
     const float is1 = col.w, is2 = nw.w;
@@ -543,16 +496,7 @@ __device__ __forceinline__ void bwd_pair(const SceneArgs& a, const BwdArgs& g, c
                 }
                 v_vis += val * S.vtex[ch];
             }
-            if (TEXMODE == 1 && ta) {
-                const int rows[4] = { B.i00, B.i01, B.i10, B.i11 };
-                const float wts[4] = { B.w00, B.w01, B.w10, B.w11 };
-#pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    ta->row[q] = rows[q];
-#pragma unroll
-                    for (int c = 0; c < 3; c++) ta->v[q][c] = wts[q] * gv[c];
-                }
-            } else if (gv[0] != 0.f || gv[1] != 0.f || gv[2] != 0.f) {
+            if (gv[0] != 0.f || gv[1] != 0.f || gv[2] != 0.f) {
                 const int rows[4] = { B.i00, B.i01, B.i10, B.i11 };
                 const float wts[4] = { B.w00, B.w01, B.w10, B.w11 };
 #pragma unroll
@@ -794,18 +738,11 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
             float m[kMoments];
 #pragma unroll
             for (int q = 0; q < kMoments; q++) m[q] = 0.f;
-            // bf16 texels with lane groups: texel-gradient atomics aggregated
-            // over the lanes that share a texel cell
-            constexpr bool kAgg = TEXMODE == 1 && CT == 3 && PPT == 1 && GS < 32;
-            const bool agg = kAgg && g.tex_aggregate;
-            TexAcc ta;
-            ta.row[0] = -1;
 #pragma unroll
             for (int p = 0; p < PPT; p++)
                 if (valid[p])
                     bwd_pair<TEXMODE, CT, CA>(a, g, R, k, gidx, Hr, H[p], alpha[p], e[p], eb[p], nbf[p], bf[p], S[p],
-                                              C, use_ndc, prop_uv, bilinear, m, agg ? &ta : nullptr);
-            if (kAgg && agg) tex_atomics_aggregated(g.v_texgrad, ta, lane);
+                                              C, use_ndc, prop_uv, bilinear, m);
             float* dst = smom + k * kMomSlot;
             if (GS == 32 && !full_warp) {
                 if (lane == 0) touched[k] = 1;
@@ -1393,11 +1330,8 @@ int launch_fwd_batch(const SceneArgs& a, const BatchArgs& ba, const FwdOut& o, i
     return check_launch("batch forward");
 }
 
-int launch_bwd_batch(const SceneArgs& a, const BatchArgs& ba, const BwdArgs& g0, int bw, int texmode, int ppt, int gs,
+int launch_bwd_batch(const SceneArgs& a, const BatchArgs& ba, const BwdArgs& g, int bw, int texmode, int ppt, int gs,
                      int grid, cudaStream_t stream) {
-    BwdArgs g = g0;
-    const char* env = getenv("GSTEX_TEX_AGGREGATE");
-    g.tex_aggregate = env && env[0] == '1';
     ppt = ppt_of(bw, ppt);
     gs = gs_of(bw, ppt, a.C, gs);
     auto k = pick<BwdBatch>(a.C, texmode, ppt, gs);

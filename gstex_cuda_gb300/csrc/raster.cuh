@@ -97,7 +97,6 @@ struct BwdArgs {
     const float3* v_normal;
     float* moments;         // [N, kMomStride]
     float* v_texgrad;       // [T, C] (fp32 texture) or [T, 4] (bf16 texture)
-    int tex_aggregate;      // bf16 texels, lane groups: aggregate texel-gradient atomics per texel cell
 };
 
 int fill_scene(const gstex_raster_inputs* in, SceneArgs& a, bool need_bins);
