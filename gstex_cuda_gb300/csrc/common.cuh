@@ -167,127 +167,20 @@ struct __align__(16) RecAll {
 };
 static_assert(sizeof(RecAll) == kRecBytes + kEdgeBytes, "record layout");
 
-// The staged records of one batch in shared memory, in one of two layouts
-// with the same accessors.
-//
-// RecsAoS: one array per record part (hot, warm, cold, edges), a record per
-// slot.  Used where all lanes read the same slot (the forward's walk): the
-// part's fields are one base pointer away.
-struct RecsAoS {
-    RecHot* hp;
-    RecWarm* wp;
-    RecCold* cp;
-    RecEdge* ep;  // null when the kernel does not stage edges
-    bool with_edges;
-    __device__ __forceinline__ static RecsAoS carve(unsigned char* smem, int n, bool edges) {
-        RecsAoS r;
-        r.hp = reinterpret_cast<RecHot*>(smem);
-        r.wp = reinterpret_cast<RecWarm*>(smem + sizeof(RecHot) * n);
-        r.cp = reinterpret_cast<RecCold*>(smem + (sizeof(RecHot) + sizeof(RecWarm)) * n);
-        r.ep = edges ? reinterpret_cast<RecEdge*>(smem + (size_t)kRecBytes * n) : nullptr;
-        r.with_edges = edges;
+struct Recs {
+    RecHot* hot;
+    RecWarm* warm;
+    RecCold* cold;
+    RecEdge* edge;  // null when the kernel does not stage edges
+    __device__ __forceinline__ static Recs carve(unsigned char* smem, int n, bool with_edges) {
+        Recs r;
+        r.hot = reinterpret_cast<RecHot*>(smem);
+        r.warm = reinterpret_cast<RecWarm*>(smem + sizeof(RecHot) * n);
+        r.cold = reinterpret_cast<RecCold*>(smem + (sizeof(RecHot) + sizeof(RecWarm)) * n);
+        r.edge = with_edges ? reinterpret_cast<RecEdge*>(smem + (size_t)kRecBytes * n) : nullptr;
         return r;
     }
-    __device__ __forceinline__ float4 box(int k) const { return hp[k].box; }
-    __device__ __forceinline__ const RecHot& hot(int k) const { return hp[k]; }
-    __device__ __forceinline__ const float4& uvm(int k) const { return wp[k].uvm; }
-    __device__ __forceinline__ const float4& uvs(int k) const { return wp[k].uvs; }
-    __device__ __forceinline__ const float4& col(int k) const { return wp[k].col; }
-    __device__ __forceinline__ const float4& nrm(int k) const { return wp[k].nrm; }
-    __device__ __forceinline__ const int4& tex(int k) const { return wp[k].tex; }
-    __device__ __forceinline__ const RecWarm& warm(int k) const { return wp[k]; }
-    __device__ __forceinline__ const RecCold& cold(int k) const { return cp[k]; }
-    __device__ __forceinline__ const RecEdge& edge(int k) const { return ep[k]; }
-    // Stores 16-byte word q (RecAll order) of slot k.
-    __device__ __forceinline__ void put(int k, int q, uint4 v) const {
-        constexpr int nh = sizeof(RecHot) / 16, nw = sizeof(RecWarm) / 16, nc = sizeof(RecCold) / 16;
-        if (q < nh) reinterpret_cast<uint4*>(hp + k)[q] = v;
-        else if (q < nh + nw) reinterpret_cast<uint4*>(wp + k)[q - nh] = v;
-        else if (q < nh + nw + nc) reinterpret_cast<uint4*>(cp + k)[q - nh - nw] = v;
-        else reinterpret_cast<uint4*>(ep + k)[q - nh - nw - nc] = v;
-    }
-    __device__ __forceinline__ void put(int k, const RecHot& h, const RecWarm& w, const RecCold& c,
-                                        const RecEdge* e) const {
-        hp[k] = h;
-        wp[k] = w;
-        cp[k] = c;
-        if (e && ep) ep[k] = *e;
-    }
 };
-
-// RecsSoA: one array per 16-byte field (structure of arrays): field q of
-// slot k at base[q * n + k], in the order of RecAll (hot: box, org, lc, nop;
-// warm: uvm, uvs, col, nrm, tex; cold: mu, dt; edges: A, B, C).  Used where
-// lanes read different slots (the backward's candidate lists and lane
-// groups): they read 16-byte words of one field, and a warp staging
-// consecutive slots stores them, without the bank conflicts of a 64-, 80- or
-// 48-byte record stride.
-struct RecsSoA {
-    float4* base;
-    int n;
-    bool with_edges;
-    static constexpr int kFields = kRecBytes / 16;
-    __device__ __forceinline__ static RecsSoA carve(unsigned char* smem, int n, bool with_edges) {
-        RecsSoA r;
-        r.base = reinterpret_cast<float4*>(smem);
-        r.n = n;
-        r.with_edges = with_edges;
-        return r;
-    }
-    __device__ __forceinline__ float4 f(int q, int k) const { return base[q * n + k]; }
-    __device__ __forceinline__ float4 box(int k) const { return f(0, k); }
-    __device__ __forceinline__ RecHot hot(int k) const {
-        RecHot h;
-        h.box = f(0, k); h.org = f(1, k); h.lc = f(2, k); h.nop = f(3, k);
-        return h;
-    }
-    __device__ __forceinline__ float4 uvm(int k) const { return f(4, k); }
-    __device__ __forceinline__ float4 uvs(int k) const { return f(5, k); }
-    __device__ __forceinline__ float4 col(int k) const { return f(6, k); }
-    __device__ __forceinline__ float4 nrm(int k) const { return f(7, k); }
-    __device__ __forceinline__ int4 tex(int k) const {
-        const float4 t = f(8, k);
-        return make_int4(__float_as_int(t.x), __float_as_int(t.y), __float_as_int(t.z), __float_as_int(t.w));
-    }
-    __device__ __forceinline__ RecWarm warm(int k) const {
-        RecWarm w;
-        w.uvm = uvm(k); w.uvs = uvs(k); w.col = col(k); w.nrm = nrm(k); w.tex = tex(k);
-        return w;
-    }
-    __device__ __forceinline__ RecCold cold(int k) const {
-        RecCold c;
-        c.mu = f(9, k); c.dt = f(10, k);
-        return c;
-    }
-    __device__ __forceinline__ RecEdge edge(int k) const {
-        RecEdge e;
-        e.A = f(kFields, k); e.B = f(kFields + 1, k); e.C = f(kFields + 2, k);
-        return e;
-    }
-    // Stores the 16-byte words of a record (RecAll order) into slot k.
-    __device__ __forceinline__ void put(int k, int q, uint4 v) const {
-        reinterpret_cast<uint4*>(base)[q * n + k] = v;
-    }
-    __device__ __forceinline__ void put(int k, const RecHot& h, const RecWarm& w, const RecCold& c,
-                                        const RecEdge* e) const {
-        const uint4* ph = reinterpret_cast<const uint4*>(&h);
-        const uint4* pw = reinterpret_cast<const uint4*>(&w);
-        const uint4* pc = reinterpret_cast<const uint4*>(&c);
-#pragma unroll
-        for (int q = 0; q < 4; q++) put(k, q, ph[q]);
-#pragma unroll
-        for (int q = 0; q < 5; q++) put(k, 4 + q, pw[q]);
-#pragma unroll
-        for (int q = 0; q < 2; q++) put(k, 9 + q, pc[q]);
-        if (e && with_edges) {
-            const uint4* pe = reinterpret_cast<const uint4*>(e);
-#pragma unroll
-            for (int q = 0; q < 3; q++) put(k, kFields + q, pe[q]);
-        }
-    }
-};
-static_assert(sizeof(RecHot) == 64 && sizeof(RecWarm) == 80 && sizeof(RecCold) == 32 && sizeof(RecEdge) == 48,
-              "record fields are whole 16-byte words");
 
 __device__ __forceinline__ float4 f4(float3 v, float w) { return make_float4(v.x, v.y, v.z, w); }
 __device__ __forceinline__ float3 f3(float4 v) { return make_float3(v.x, v.y, v.z); }

@@ -23,42 +23,38 @@
 
 namespace gstex {
 
-// Builds the record of Gaussian gid into slot: in place for the per-record
-// layout, through registers for the field-array layout.
-__device__ __forceinline__ void stage(const RecsAoS& R, int slot, const SceneArgs& a, const View& V,
-                                      const float3* colors, int gid, bool use_blur) {
-    make_record(R.hp[slot], R.wp[slot], R.cp[slot], gid, V, a.means[gid], a.quats[gid],
+__device__ __forceinline__ void stage(const Recs& R, int slot, const SceneArgs& a, const View& V, const float3* colors,
+                                      int gid, bool use_blur) {
+    make_record(R.hot[slot], R.warm[slot], R.cold[slot], gid, V, a.means[gid], a.quats[gid],
                 make_float2(a.scales[3 * gid], a.scales[3 * gid + 1]), a.glob, a.opac[gid],
-                colors ? colors[gid] : make_float3(0.f, 0.f, 0.f), a.uv0[gid], a.umap[gid], a.vmap[gid], a.dims[gid],
-                use_blur, true, R.ep ? R.ep + slot : nullptr, !(a.settings & (1 << 16)));
-}
-__device__ __forceinline__ void stage(const RecsSoA& R, int slot, const SceneArgs& a, const View& V,
-                                      const float3* colors, int gid, bool use_blur) {
-    RecHot h;
-    RecWarm w;
-    RecCold c;
-    RecEdge e;
-    make_record(h, w, c, gid, V, a.means[gid], a.quats[gid], make_float2(a.scales[3 * gid], a.scales[3 * gid + 1]),
-                a.glob, a.opac[gid], colors ? colors[gid] : make_float3(0.f, 0.f, 0.f), a.uv0[gid], a.umap[gid],
-                a.vmap[gid], a.dims[gid], use_blur, true, R.with_edges ? &e : nullptr, !(a.settings & (1 << 16)));
-    R.put(slot, h, w, c, R.with_edges ? &e : nullptr);
+                colors ? colors[gid] : make_float3(0.f, 0.f, 0.f), a.uv0[gid],
+                a.umap[gid], a.vmap[gid], a.dims[gid], use_blur, true, R.edge ? R.edge + slot : nullptr,
+                !(a.settings & (1 << 16)));
 }
 
 // Stages the record of Gaussian gid for one tile: a copy of the prebuilt
 // (view, Gaussian) record when the batched path built them, else built here.
-template <class RS>
-__device__ __forceinline__ void stage_job(const RS& R, int slot, const SceneArgs& a, const TileJob& J, int gid,
+__device__ __forceinline__ void stage_job(const Recs& R, int slot, const SceneArgs& a, const TileJob& J, int gid,
                                           bool use_blur) {
     if (J.recs) {
         const uint4* src = reinterpret_cast<const uint4*>(J.recs + gid);
         uint4 v[kRecBytes / 16];
 #pragma unroll
         for (int q = 0; q < kRecBytes / 16; q++) v[q] = __ldg(src + q);
+        uint4* hot = reinterpret_cast<uint4*>(R.hot + slot);
+        uint4* warm = reinterpret_cast<uint4*>(R.warm + slot);
+        uint4* cold = reinterpret_cast<uint4*>(R.cold + slot);
+        constexpr int nh = sizeof(RecHot) / 16, nw = sizeof(RecWarm) / 16, nc = sizeof(RecCold) / 16;
 #pragma unroll
-        for (int q = 0; q < kRecBytes / 16; q++) R.put(slot, q, v[q]);
-        if (R.with_edges) {
+        for (int q = 0; q < nh; q++) hot[q] = v[q];
 #pragma unroll
-            for (int q = 0; q < kEdgeBytes / 16; q++) R.put(slot, kRecBytes / 16 + q, __ldg(src + kRecBytes / 16 + q));
+        for (int q = 0; q < nw; q++) warm[q] = v[nh + q];
+#pragma unroll
+        for (int q = 0; q < nc; q++) cold[q] = v[nh + nw + q];
+        if (R.edge) {
+            uint4* edge = reinterpret_cast<uint4*>(R.edge + slot);
+#pragma unroll
+            for (int q = 0; q < kEdgeBytes / 16; q++) edge[q] = __ldg(src + kRecBytes / 16 + q);
         }
     } else {
         stage(R, slot, a, J.V, J.colors, gid, use_blur);
@@ -80,20 +76,18 @@ __device__ __forceinline__ void direct_hit(Hit& H, const float4* __restrict__ qu
                      is2, uv0.x, uv0.y);
 }
 
-template <class RS>
-__device__ __forceinline__ Hit hit_pixel(const RecHot& Hr, const RS& R, int k, const SceneArgs& a, const View& V,
+__device__ __forceinline__ Hit hit_pixel(const RecHot& Hr, const Recs& R, int k, const SceneArgs& a, const View& V,
                                          const PixelRay& P) {
     Hit H = intersect(Hr, P);
     if (H.direct)
-        direct_hit(H, a.quats, a.means, a.scales, a.glob, a.uv0, a.umap, a.vmap, V, R.tex(k).w, P, Hr.org.w);
+        direct_hit(H, a.quats, a.means, a.scales, a.glob, a.uv0, a.umap, a.vmap, V, R.warm[k].tex.w, P, Hr.org.w);
     return H;
 }
 
 // Distance (in pixels) from the pixel to the nearest pixel of its 7x7
 // neighbourhood whose ray meets the splat outside sigma <= sth
 // (texture_helpers.cuh:390-417); 1000 when there is none.
-template <class RS>
-__device__ __noinline__ float local_outline(const RecHot& Hr, const RS& R, int k, const SceneArgs& a, const View& V,
+__device__ __noinline__ float local_outline(const RecHot& Hr, const Recs& R, int k, const SceneArgs& a, const View& V,
                                             const TileJob& J, const PixelRay& P, float sth) {
     float best = 1000.f;
     const int pi = (int)(P.py - 0.5f), pj = (int)(P.px - 0.5f);
@@ -186,14 +180,13 @@ __device__ __forceinline__ int group_min(int v) {
 // splat left out is outside its alpha >= 1/255 box for every pixel of the
 // warp.  Returns the count; the entries are in wl[0, count).  The lanes of a
 // partial warp (tile widths that are not a multiple of 8) are its low lanes.
-template <class RS>
-__device__ __forceinline__ bool splat_meets_rect(const RS& R, int kk, float rx0, float rx1, float ry0, float ry1) {
-    const float4 bx = R.box(kk);
+__device__ __forceinline__ bool splat_meets_rect(const Recs& R, int kk, float rx0, float rx1, float ry0, float ry1) {
+    const float4 bx = R.hot[kk].box;
     bool hit = !(bx.y < rx0 || bx.x > rx1 || bx.w < ry0 || bx.z > ry1);
-    if (hit && R.with_edges) {
+    if (hit && R.edge) {
         // separating axes of the splat's quad: the rectangle's corner
         // furthest inside each edge must be inside it
-        const RecEdge& e = R.edge(kk);
+        const RecEdge e = R.edge[kk];
         const float ea[4] = { e.A.x, e.A.y, e.A.z, e.A.w }, eb[4] = { e.B.x, e.B.y, e.B.z, e.B.w };
         const float ec[4] = { e.C.x, e.C.y, e.C.z, e.C.w };
 #pragma unroll
@@ -203,8 +196,7 @@ __device__ __forceinline__ bool splat_meets_rect(const RS& R, int kk, float rx0,
     return hit;
 }
 
-template <class RS>
-__device__ __forceinline__ int build_list(uint8_t* wl, const RS& R, int k0, int bsize, float rx0, float rx1,
+__device__ __forceinline__ int build_list(uint8_t* wl, const Recs& R, int k0, int bsize, float rx0, float rx1,
                                           float ry0, float ry1, unsigned wmask, unsigned lane) {
     const int nl = __popc(wmask);
     int cnt = 0;
@@ -223,8 +215,8 @@ __device__ __forceinline__ int build_list(uint8_t* wl, const RS& R, int k0, int 
 // entries of the warp's list wl[0, cntw) (built with the warp's rectangle)
 // that are at or after slot k0 (k0 per group) and whose box and quad meet the
 // group's rectangle, in order.
-template <int GS, class RS>
-__device__ __forceinline__ int build_group_list(uint8_t* gl, const uint8_t* wl, int cntw, const RS& R, int k0,
+template <int GS>
+__device__ __forceinline__ int build_group_list(uint8_t* gl, const uint8_t* wl, int cntw, const Recs& R, int k0,
                                                 float rx0, float rx1, float ry0, float ry1, unsigned lane) {
     const unsigned lg = lane & (GS - 1);
     const unsigned gm = ((1u << GS) - 1u) << (lane & ~(unsigned)(GS - 1));
@@ -247,7 +239,7 @@ __device__ __forceinline__ int build_group_list(uint8_t* gl, const uint8_t* wl, 
 // staged record read from shared memory is used for PPT pixels.
 // ---------------------------------------------------------------------------
 template <int TEXMODE, int CT, int PPT>
-__device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, const FwdOut& o, const RecsAoS& R) {
+__device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, const FwdOut& o, const Recs& R) {
     const int nthr = blockDim.x * blockDim.y;
     const int tr = threadIdx.y * blockDim.x + threadIdx.x;
     const int bw = blockDim.x;
@@ -307,7 +299,7 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
         if (__all_sync(wmask, all_done)) continue;
         // Every staged slot in order; each pixel tests the splat's box first.
         for (int k = 0; k < bsize; ++k) {
-            const float4 bx = R.box(k);
+            const float4 bx = R.hot[k].box;
             bool need = false;
 #pragma unroll
             for (int p = 0; p < PPT; p++) {
@@ -315,7 +307,7 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
                 need = need || (!done[p] && !(out_box && T[p] > 1.01e-4f));
             }
             if (need) {
-            const RecHot Hr = R.hot(k);
+            const RecHot Hr = R.hot[k];
 #pragma unroll
             for (int p = 0; p < PPT; p++) {
                 if (done[p]) continue;
@@ -324,7 +316,7 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
                 const float sigma = 0.5f * (H.l1s * H.l1s + H.l2s * H.l2s);
                 float nbf = 1.f, bf = 0.f, sigma_blur = 0.f;
                 if (use_blur) {
-                    const float4 uvs = R.uvs(k);
+                    const float4 uvs = R.warm[k].uvs;
                     const float dx = uvs.z - P[p].px, dy = uvs.w - P[p].py;
                     sigma_blur = 0.5f * kBlurFsq * (dx * dx + dy * dy);
                     if (sigma_blur < sigma) { bf = 1.f; nbf = 0.f; }
@@ -340,7 +332,7 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
                 const float next_T = T[p] * (1.f - alpha);
                 if (next_T <= kTDone) { done[p] = true; continue; }
                 if (skip) continue;
-                const RecWarm& Wm = R.warm(k);
+                const RecWarm& Wm = R.warm[k];
                 const float vis = alpha * T[p];
                 const float4 col = Wm.col;
                 // outside the outline: the colour; on it: white (bit 24) or nothing
@@ -470,11 +462,11 @@ struct BwdPix {
 // Adjoint of one (pixel, Gaussian) pair; adds its moments to m and returns
 // false when the pair is skipped.  Follows csrc/texture.cu:577-708.
 template <int TEXMODE, int CT, int CA>
-__device__ __forceinline__ void bwd_pair(const SceneArgs& a, const BwdArgs& g, const RecsSoA& R, int k, int gidx,
+__device__ __forceinline__ void bwd_pair(const SceneArgs& a, const BwdArgs& g, const Recs& R, int k, int gidx,
                                          const RecHot& Hr, const Hit& H, float alpha, float e, float eb, float nbf,
                                          float bf, BwdPix<CA>& S, int C, bool use_ndc, bool prop_uv, bool bilinear,
                                          float (&m)[kMoments]) {
-    const RecWarm& Wm = R.warm(k);
+    const RecWarm& Wm = R.warm[k];
     const float4 col = Wm.col, nw = Wm.nrm;
     const float is1 = col.w, is2 = nw.w;
     const PixelRay& P = S.P;
@@ -565,7 +557,7 @@ __device__ __forceinline__ void bwd_pair(const SceneArgs& a, const BwdArgs& g, c
     const float p1 = H.l1s * v_sigma, p2 = H.l2s * v_sigma;
     const float l1 = __fdividef(H.l1s, is1), l2 = __fdividef(H.l2s, is2);
     // ray . axis from the hit: l = a . (t r - mu) gives a . r = (l + a . mu) / t
-    const RecCold& Cd = R.cold(k);
+    const RecCold& Cd = R.cold[k];
     const float it = __fdividef(1.f, H.t);
     const float ra1 = (l1 + Cd.mu.w) * it;
     const float ra2 = (l2 + Cd.dt.x) * it;
@@ -613,7 +605,7 @@ __device__ __forceinline__ void bwd_pair(const SceneArgs& a, const BwdArgs& g, c
 // and a small splat occupies the lanes of the pixels it can reach, not a whole
 // warp.
 template <int TEXMODE, int CT, int PPT, int GS = 32>
-__device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, const BwdArgs& g, const RecsSoA& R,
+__device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, const BwdArgs& g, const Recs& R,
                                          float* smom, uint8_t* lists, uint8_t* touched) {
     static_assert(GS == 32 || GS == 16 || GS == 8 || GS == 4, "group of 32, 16, 8 or 4 lanes");
     using Red = Ragged<kMoments, GS / 2>;
@@ -706,7 +698,7 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
             const int k = act ? list[j] : 0;
             const int gidx = bend - k;
             {
-                const float4 bx = R.box(k);
+                const float4 bx = R.hot[k].box;
                 bool need = false;
 #pragma unroll
                 for (int p = 0; p < PPT; p++)
@@ -714,7 +706,7 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
                                     !(S[p].P.px < bx.x || S[p].P.px > bx.y || S[p].P.py < bx.z || S[p].P.py > bx.w));
                 if (!__any_sync(wmask, act && need)) continue;
             }
-            const RecHot Hr = R.hot(k);
+            const RecHot Hr = R.hot[k];
             bool valid[PPT];
             Hit H[PPT];
             float e[PPT], eb[PPT], nbf[PPT], bf[PPT], alpha[PPT];
@@ -729,7 +721,7 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
                     const float sigma = 0.5f * (H[p].l1s * H[p].l1s + H[p].l2s * H[p].l2s);
                     float sigma_blur = 0.f;
                     if (use_blur) {
-                        const float4 uvs = R.uvs(k);
+                        const float4 uvs = R.warm[k].uvs;
                         const float dx = uvs.z - S[p].P.px, dy = uvs.w - S[p].P.py;
                         sigma_blur = 0.5f * kBlurFsq * (dx * dx + dy * dy);
                         if (sigma_blur < sigma) { bf[p] = 1.f; nbf[p] = 0.f; }
@@ -777,7 +769,7 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
                 sm[4 * q] = v4.x; sm[4 * q + 1] = v4.y; sm[4 * q + 2] = v4.z; sm[4 * q + 3] = v4.w;
             }
             {
-                const int gid = R.tex(tr).w;
+                const int gid = R.warm[tr].tex.w;
                 if (J.vc_stride == 4) {
                     atomicAdd(reinterpret_cast<float4*>(J.vcolors) + gid, make_float4(sm[0], sm[1], sm[2], 0.f));
                 } else {
@@ -788,12 +780,12 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
                 }
                 float4* dst = reinterpret_cast<float4*>(g.moments + (size_t)gid * kMomStride);
                 // blur moments -> world-space mean gradient (helpers.cuh:155-164, 114-121)
-                const float3 p = f3(R.cold(tr).mu);
+                const float3 p = f3(R.cold[tr].mu);
                 const float rw = 1.f / (p.z + 1e-6f);
                 const float vx = V.fx * sm[21], vy = V.fy * sm[22];
                 const float3 vmb = V.rot_t(make_float3(vx * rw, vy * rw, -(vx * p.x + vy * p.y) * rw * rw));
                 // the per-Gaussian factors left out of the pixel sums
-                const float is1 = R.col(tr).w, is2 = R.nrm(tr).w;
+                const float is1 = R.warm[tr].col.w, is2 = R.warm[tr].nrm.w;
                 const float r1 = 1.f / is1, r2 = 1.f / is2;
                 float v[kMomStride];
                 v[0] = sm[3];
@@ -837,7 +829,7 @@ struct EditIO {
     float* out;  // [T, 5]
 };
 
-__device__ __forceinline__ void edit_tile(const SceneArgs& a, const TileJob& J, const EditIO& E, const RecsAoS& R) {
+__device__ __forceinline__ void edit_tile(const SceneArgs& a, const TileJob& J, const EditIO& E, const Recs& R) {
     const int nthr = blockDim.x * blockDim.y;
     const int tr = threadIdx.y * blockDim.x + threadIdx.x;
     const int bw = blockDim.x;
@@ -869,7 +861,7 @@ __device__ __forceinline__ void edit_tile(const SceneArgs& a, const TileJob& J, 
         __syncthreads();
         const int bsize = min(nthr, range.y - bstart);
         for (int k = 0; k < bsize && !done; ++k) {
-            const RecHot Hr = R.hot(k);
+            const RecHot Hr = R.hot[k];
             // outside the alpha >= 1/255 box a splat is skipped; it can end the
             // pixel there only when T <= 1e-4 * 255/254
             if (outside_box(Hr, P) && T > 1.01e-4f) continue;
@@ -877,7 +869,7 @@ __device__ __forceinline__ void edit_tile(const SceneArgs& a, const TileJob& J, 
             const float sigma = 0.5f * (H.l1s * H.l1s + H.l2s * H.l2s);
             float nbf = 1.f, bf = 0.f, sigma_blur = 0.f;
             if (use_blur) {
-                const float4 uvs = R.uvs(k);
+                const float4 uvs = R.warm[k].uvs;
                 const float dx = uvs.z - P.px, dy = uvs.w - P.py;
                 sigma_blur = 0.5f * kBlurFsq * (dx * dx + dy * dy);
                 if (sigma_blur < sigma) { bf = 1.f; nbf = 0.f; }
@@ -888,7 +880,7 @@ __device__ __forceinline__ void edit_tile(const SceneArgs& a, const TileJob& J, 
             if (next_T <= kTDone) { done = true; continue; }
             if (skip) continue;
             if (H.tcam >= lo && H.tcam <= hi) {
-                const RecWarm& Wm = R.warm(k);
+                const RecWarm& Wm = R.warm[k];
                 const float2 uv = hit_uv(H, Wm);
                 const int4 tx = Wm.tex;
                 const Bilerp B = bilerp(tx.x, tx.y, tx.z, clamp01(uv.x), clamp01(uv.y), true);
@@ -919,7 +911,7 @@ __global__ void __launch_bounds__(256, 4) edit_view_kernel(SceneArgs a, ViewArgs
     J.vcolors = nullptr;
     J.vc_stride = 3;
     J.recs = nullptr;
-    edit_tile(a, J, E, RecsAoS::carve(smem, blockDim.x * blockDim.y, false));
+    edit_tile(a, J, E, Recs::carve(smem, blockDim.x * blockDim.y, false));
 }
 
 // ---------------------------------------------------------------------------
@@ -955,7 +947,7 @@ __global__ void FWD_BOUNDS(PPT) fwd_view_kernel(SceneArgs a, ViewArgs va, FwdOut
     J.vc_stride = 3;
     J.recs = va.recs;
     const int nthr = blockDim.x * blockDim.y;
-    fwd_tile<TEXMODE, CT, PPT>(a, J, o, RecsAoS::carve(smem, nthr, false));
+    fwd_tile<TEXMODE, CT, PPT>(a, J, o, Recs::carve(smem, nthr, false));
 }
 
 template <int TEXMODE, int CT, int PPT, int GS>
@@ -973,7 +965,7 @@ __global__ void BWD_BOUNDS(PPT) bwd_view_kernel(SceneArgs a, ViewArgs va, BwdArg
     J.vc_stride = 3;
     J.recs = va.recs;
     uint8_t* lists = smem + (size_t)(kRecBytes + kEdgeBytes + kMomSlot * sizeof(float)) * nthr;
-    bwd_tile<TEXMODE, CT, PPT, GS>(a, J, g, RecsSoA::carve(smem, nthr, true),
+    bwd_tile<TEXMODE, CT, PPT, GS>(a, J, g, Recs::carve(smem, nthr, true),
                                    reinterpret_cast<float*>(smem + (size_t)(kRecBytes + kEdgeBytes) * nthr), lists,
                                    lists + ((size_t)ceil_div(nthr, 32) + (GS < 32 ? ceil_div(nthr, GS) : 0)) * nthr);
 }
@@ -1007,7 +999,7 @@ __global__ void FWD_BOUNDS(PPT) fwd_batch_kernel(SceneArgs a, BatchArgs ba, FwdO
     __shared__ int s_tile;
     TileJob J;
     const int nthr = blockDim.x * blockDim.y;
-    const RecsAoS R = RecsAoS::carve(smem, nthr, false);
+    const Recs R = Recs::carve(smem, nthr, false);
     while (next_job(ba, &s_tile, J)) fwd_tile<TEXMODE, CT, PPT>(a, J, o, R);
 }
 
@@ -1017,7 +1009,7 @@ __global__ void BWD_BOUNDS(PPT) bwd_batch_kernel(SceneArgs a, BatchArgs ba, BwdA
     __shared__ int s_tile;
     const int nthr = blockDim.x * blockDim.y;
     TileJob J;
-    const RecsSoA R = RecsSoA::carve(smem, nthr, true);
+    const Recs R = Recs::carve(smem, nthr, true);
     float* smom = reinterpret_cast<float*>(smem + (size_t)(kRecBytes + kEdgeBytes) * nthr);
     uint8_t* lists = smem + (size_t)(kRecBytes + kEdgeBytes + kMomSlot * sizeof(float)) * nthr;
     uint8_t* touched = lists + ((size_t)ceil_div(nthr, 32) + (GS < 32 ? ceil_div(nthr, GS) : 0)) * nthr;
