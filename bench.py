@@ -62,6 +62,9 @@ def parse():
     p.add_argument("--no-autotune", action="store_true",
                    help="use the backward variant given by --bwd-group (profiling runs)")
     p.add_argument("--bwd-group", type=int, default=8)
+    p.add_argument("--tile-widths", default="16,8",
+                   help="tile widths the autotuner tries (each bins the scene anew); the first is used "
+                        "with --no-autotune")
     p.add_argument("--no-graph", action="store_true")
     return p.parse_args()
 
@@ -337,25 +340,55 @@ def main():
     nviews = len(spec.cameras)
     cams = cameras_of(spec)
     scene = device_scene(spec, dev, bf16=True)
-    r = B.BatchRenderer(cams, spec.num_points, channels=3, texture_dtype=torch.bfloat16, device=dev)
-    P = r.total_pixels
+    widths = [int(w) for w in args.tile_widths.split(",") if w]
+
+    def make_renderer(bw):
+        r = B.BatchRenderer(cams, spec.num_points, channels=3, texture_dtype=torch.bfloat16, device=dev,
+                            block_width=bw)
+        # first step: size the intersection buffers
+        r.step(scene, tgt_img, tgt_tex)
+        torch.cuda.synchronize(dev)
+        while not r.check_capacity():
+            r.grow(1.25)
+            r.step(scene, tgt_img, tgt_tex)
+            torch.cuda.synchronize(dev)
+        return r
+
+    P = sum(c.width * c.height for c in cams)
     gen = torch.Generator().manual_seed(11 + rank)
     tgt_img = torch.rand(P, 3, generator=gen).to(dev)
     tgt_tex = torch.rand(P, 3, generator=gen).to(dev)
-    # first step: size the intersection buffers
-    r.step(scene, tgt_img, tgt_tex)
-    torch.cuda.synchronize(dev)
-    while not r.check_capacity():
-        r.grow(1.25)
-        r.step(scene, tgt_img, tgt_tex)
-        torch.cuda.synchronize(dev)
+    if args.no_autotune:
+        r = make_renderer(widths[0])
+        r.bwd_group = args.bwd_group
+        tuned = {"fixed": True, "block_width": r.bw, "fwd_ppt": r.fwd_ppt, "bwd_ppt": r.bwd_ppt,
+                 "bwd_group": r.bwd_group}
+    else:
+        # tile width: each candidate bins the scene anew, is tuned on its own
+        # and timed over whole steps; the fastest renderer is kept
+        stream = torch.cuda.current_stream(dev)
+        r, tuned, grid = None, None, {}
+        for bw in widths:
+            cand = make_renderer(bw)
+            t = cand.autotune(scene, tgt_img, tgt_tex)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            cand.step(scene, tgt_img, tgt_tex)
+            e0.record(stream)
+            for _ in range(3):
+                cand.step(scene, tgt_img, tgt_tex)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            ms = e0.elapsed_time(e1) / 3
+            grid[f"step_bw{bw}_ms"] = ms
+            log(f"block width {bw}: {ms:.2f} ms/step, intersections {cand.intersections()}, tuned {t}")
+            if r is None or ms < grid[f"step_bw{r.bw}_ms"]:
+                r, tuned = cand, t
+            else:
+                del cand
+            torch.cuda.empty_cache()
+        tuned = dict(tuned, block_width=r.bw, tile_width_grid=grid)
     I = r.intersections()
     log(f"intersections {I}, pixels {P}, tiles {r.total_tiles}, capacity {r.capacity}")
-    if args.no_autotune:
-        r.bwd_group = args.bwd_group
-        tuned = {"fixed": True, "fwd_ppt": r.fwd_ppt, "bwd_ppt": r.bwd_ppt, "bwd_group": r.bwd_group}
-    else:
-        tuned = r.autotune(scene, tgt_img, tgt_tex)
     log(f"autotune: {tuned}")
 
     # timed region: eager steps (one launch per stage), CUDA events around the

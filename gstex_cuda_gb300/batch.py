@@ -42,7 +42,8 @@ class BatchInputs(ctypes.Structure):
                 ("views", _P), ("tile_view", _P), ("tile_order", _P), ("gaussian_ids_sorted", _P), ("tile_bins", _P),
                 ("colors", _P), ("opacities", _P), ("means", _P), ("scales", _P), ("glob_scale", _F), ("quats", _P),
                 ("uv0", _P), ("umap", _P), ("vmap", _P), ("texture_dims", _P), ("texture", _P), ("background", _P),
-                ("queue", _P), ("grid", _I), ("pixels_per_thread", _I), ("records", _P), ("group_lanes", _I)]
+                ("queue", _P), ("grid", _I), ("pixels_per_thread", _I), ("records", _P), ("group_lanes", _I),
+                ("batch_size", _I)]
 
 
 class RawGrads(ctypes.Structure):
@@ -152,7 +153,8 @@ class BatchRenderer:
     def __init__(self, cameras: Sequence[Camera], num_points: int, *, channels: int = 3, texture_dtype=torch.float32,
                  block_width: int = 16, settings: int = 1 << 8, background=(0.0, 0.0, 0.0), capacity: int = 0,
                  device="cuda:0", grid: int = 0, loss_weights: Optional[dict] = None, fwd_ppt: int = 1,
-                 bwd_ppt: int = 1, bwd_group: int = 8, prebuilt_records: bool = True, heavy_first: bool = True):
+                 bwd_ppt: int = 1, bwd_group: int = 8, fwd_batch: int = 0, bwd_batch: int = 0,
+                 prebuilt_records: bool = True, heavy_first: bool = True):
         self.dev = torch.device(device)
         self.N = int(num_points)
         self.V = len(cameras)
@@ -163,6 +165,7 @@ class BatchRenderer:
         self.grid = int(grid)
         self.fwd_ppt, self.bwd_ppt = int(fwd_ppt), int(bwd_ppt)
         self.bwd_group = int(bwd_group)
+        self.fwd_batch, self.bwd_batch = int(fwd_batch), int(bwd_batch)
         self.lw = dict(LOSS_WEIGHTS if loss_weights is None else loss_weights)
         L = _L()
         descs = (ViewDesc * self.V)()
@@ -271,6 +274,7 @@ class BatchRenderer:
         bi.queue, bi.grid = ptr(self.queue), self.grid
         bi.pixels_per_thread = self.bwd_ppt if backward else self.fwd_ppt
         bi.group_lanes = self.bwd_group if backward else 32
+        bi.batch_size = self.bwd_batch if backward else self.fwd_batch
         bi.records = ptr(self.records) if self.records is not None else None
         return bi
 
@@ -459,9 +463,12 @@ class BatchRenderer:
 
     # ------------------------------------------------------------------
     def autotune(self, s: Scene, tgt_img, tgt_tex, reps: int = 2) -> dict:
-        """Choose pixels-per-thread of the forward kernel, and pixels-per-thread
-        and lanes per splat walk (32, 16, 8, 4) of the backward kernel, by
-        timing each candidate on this scene and these cameras (CUDA events)."""
+        """Choose pixels-per-thread and Gaussians per batch (64, 128 or one per
+        thread) of the forward kernel, and pixels-per-thread, lanes per splat
+        walk (32, 16, 8, 4) and Gaussians per batch of the backward kernel, by
+        timing each candidate on this scene and these cameras (CUDA events).
+        The tile width is fixed per renderer (it sets the binning): to tune
+        it, build a renderer per block_width and time whole steps."""
         stream = torch.cuda.current_stream(self.dev)
         self.bin(s)
 
@@ -478,21 +485,32 @@ class BatchRenderer:
         result = {}
         best = None
         for ppt in (1, 2):
-            self.fwd_ppt = ppt
+            self.fwd_ppt, self.fwd_batch = ppt, 0
             ms = timed(lambda: self.forward(s))
             result[f"forward_ppt{ppt}_ms"] = ms
-            best = (ms, ppt) if best is None or ms < best[0] else best
-        self.fwd_ppt = best[1]
+            best = (ms, ppt, 0) if best is None or ms < best[0] else best
+        for nb in (64, 128):
+            self.fwd_ppt, self.fwd_batch = 1, nb
+            ms = timed(lambda: self.forward(s))
+            result[f"forward_ppt1_batch{nb}_ms"] = ms
+            best = (ms, 1, nb) if ms < best[0] else best
+        self.fwd_ppt, self.fwd_batch = best[1], best[2]
         self.forward(s)
         self.image_loss(tgt_img, tgt_tex)
         best = None
         for ppt, gs in ((1, 32), (2, 32), (1, 16), (1, 8), (1, 4)):
-            self.bwd_ppt, self.bwd_group = ppt, gs
+            self.bwd_ppt, self.bwd_group, self.bwd_batch = ppt, gs, 0
             ms = timed(lambda: self.backward(s))
             result[f"backward_ppt{ppt}_g{gs}_ms"] = ms
-            best = (ms, ppt, gs) if best is None or ms < best[0] else best
-        self.bwd_ppt, self.bwd_group = best[1], best[2]
-        result.update(fwd_ppt=self.fwd_ppt, bwd_ppt=self.bwd_ppt, bwd_group=self.bwd_group)
+            best = (ms, ppt, gs, 0) if best is None or ms < best[0] else best
+        for nb in (64, 128):
+            self.bwd_ppt, self.bwd_group, self.bwd_batch = best[1], best[2], nb
+            ms = timed(lambda: self.backward(s))
+            result[f"backward_ppt{best[1]}_g{best[2]}_batch{nb}_ms"] = ms
+            best = (ms, best[1], best[2], nb) if ms < best[0] else best
+        self.bwd_ppt, self.bwd_group, self.bwd_batch = best[1], best[2], best[3]
+        result.update(fwd_ppt=self.fwd_ppt, fwd_batch=self.fwd_batch or "threads", bwd_ppt=self.bwd_ppt,
+                      bwd_group=self.bwd_group, bwd_batch=self.bwd_batch or "threads")
         self.graph = None
         return result
 

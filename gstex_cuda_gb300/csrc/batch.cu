@@ -509,6 +509,7 @@ static int batch_scene(const gstex_batch_inputs* in, SceneArgs& a, BatchArgs& ba
     GSTEX_REQUIRE(in && in->num_points >= 0 && in->num_views > 0 && in->total_tiles > 0);
     GSTEX_REQUIRE(in->block_width >= 2 && in->block_width <= kMaxBlockWidth);
     GSTEX_REQUIRE(in->channels >= 0);
+    GSTEX_REQUIRE(in->batch_size >= 0);
     if (in->channels > kMaxChannels) return GSTEX_ERR_UNSUPPORTED;
     if (in->texture_dtype == 1 && in->channels != 3) return GSTEX_ERR_UNSUPPORTED;
     GSTEX_REQUIRE(in->views && in->tile_view && in->tile_bins && in->background && in->queue);
@@ -530,6 +531,7 @@ static int batch_scene(const gstex_batch_inputs* in, SceneArgs& a, BatchArgs& ba
     a.vmap = (const float3*)in->vmap;
     a.tex = in->texture;
     a.settings = in->settings;
+    a.batch = in->batch_size;
     a.bg = in->background;
     ba.num_points = in->num_points;
     ba.total_tiles = in->total_tiles;

@@ -61,6 +61,12 @@ __device__ __forceinline__ void stage_job(const Recs& R, int slot, const SceneAr
     }
 }
 
+// Gaussians staged per round of a tile: a.batch when set (at most the
+// threads of the CTA, which stage one each), else one per thread.
+__device__ __forceinline__ int batch_of(const SceneArgs& a, int nthr) {
+    return (a.batch > 0 && a.batch < nthr) ? a.batch : nthr;
+}
+
 // Completes a Hit in the direct form, rebuilding the Gaussian's camera-space
 // frame from its parameters (rare: splats at the camera plane and pixels within
 // the reference's denominator clamp).
@@ -287,15 +293,16 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
         for (int k = 0; k < CA; k++) otex[p][k] = 0.f;
     }
     const int2 range = J.range;
-    const int nb = ceil_div(range.y - range.x, nthr);
+    const int bsz = batch_of(a, nthr);  // Gaussians staged per round
+    const int nb = ceil_div(range.y - range.x, bsz);
 
     for (int b = 0; b < nb; ++b) {
         if (__syncthreads_count(all_done) >= nthr) break;
-        const int bstart = range.x + nthr * b;
+        const int bstart = range.x + bsz * b;
         const int idx = bstart + tr;
-        if (idx < range.y) stage_job(R, tr, a, J, a.gids[idx], use_blur);
+        if (tr < bsz && idx < range.y) stage_job(R, tr, a, J, a.gids[idx], use_blur);
         __syncthreads();
-        const int bsize = min(nthr, range.y - bstart);
+        const int bsize = min(bsz, range.y - bstart);
         if (__all_sync(wmask, all_done)) continue;
         // Every staged slot in order; each pixel tests the splat's box first.
         for (int k = 0; k < bsize; ++k) {
@@ -672,14 +679,16 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
     const unsigned gmask = (GS == 32) ? wmask : (((1u << GS) - 1u) << (lane & ~(unsigned)(GS - 1)));
 
     const int2 range = J.range;
-    const int nb = ceil_div(range.y - range.x, nthr);
+    const int bsz = batch_of(a, nthr);  // Gaussians staged per round
+    const int nb = ceil_div(range.y - range.x, bsz);
     for (int b = 0; b < nb; ++b) {
         __syncthreads();
-        const int bend = range.y - 1 - nthr * b;
-        const int bsize = min(nthr, bend + 1 - range.x);
+        const int bend = range.y - 1 - bsz * b;
+        const int bsize = min(bsz, bend + 1 - range.x);
         const int idx = bend - tr;
-        if (idx >= range.x) stage_job(R, tr, a, J, a.gids[idx], use_blur);
-        for (int q = tr; q < nthr * (kMomSlot / 4); q += nthr)
+        const bool mine = tr < bsz && idx >= range.x;  // this thread stages and flushes slot tr
+        if (mine) stage_job(R, tr, a, J, a.gids[idx], use_blur);
+        for (int q = tr; q < bsz * (kMomSlot / 4); q += nthr)
             reinterpret_cast<float4*>(smom)[q] = make_float4(0.f, 0.f, 0.f, 0.f);
         touched[tr] = 0;
         __syncthreads();
@@ -761,7 +770,7 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
             }
         }
         __syncthreads();
-        if (idx >= range.x && touched[tr]) {
+        if (mine && touched[tr]) {
             float sm[kMomSlot];
 #pragma unroll
             for (int q = 0; q < kMomSlot / 4; q++) {
@@ -1233,6 +1242,7 @@ int fill_scene(const gstex_raster_inputs* in, SceneArgs& a, bool need_bins) {
     a.tex = in->texture;
     a.settings = in->settings;
     a.bg = in->background;
+    a.batch = 0;
     return GSTEX_OK;
 }
 

@@ -25,6 +25,7 @@ struct SceneArgs {
     const void* tex;
     int settings;
     const float* bg;      // [3] device
+    int batch;            // Gaussians staged per round (0: one per thread)
 };
 
 // One view rendered by a tile grid (the reference's launch form).

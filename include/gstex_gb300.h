@@ -388,6 +388,8 @@ typedef struct gstex_batch_inputs {
     const void* records;                /* optional: gstex_batch_records output (16-byte aligned);
                                            null = each tile derives the records it stages */
     int group_lanes;                    /* backward: lanes per splat walk (see gstex_raster_inputs) */
+    int batch_size;                     /* Gaussians a tile stages per round, 1..threads per CTA;
+                                           0 = one per thread (the reference's bw^2) */
 } gstex_batch_inputs;
 
 /* Bytes of the per-(view, Gaussian) splat records of gstex_batch_records

@@ -10,8 +10,9 @@ pytestmark = pytest.mark.gpu
 DEV = "cuda:0"
 
 
-@pytest.fixture(scope="module", params=[(1, 1, 32), (2, 2, 32), (1, 1, 16), (1, 1, 8), (1, 1, 4)],
-                ids=["1px", "2px", "1px_g16", "1px_g8", "1px_g4"])
+@pytest.fixture(scope="module", params=[(1, 1, 32, 16), (2, 2, 32, 16), (1, 1, 16, 16), (1, 1, 8, 16),
+                                        (1, 1, 4, 16), (1, 1, 8, 8), (2, 2, 32, 8)],
+                ids=["1px", "2px", "1px_g16", "1px_g8", "1px_g4", "bw8_1px_g8", "bw8_2px"])
 def setup(request):
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
@@ -26,7 +27,7 @@ def setup(request):
                     texture_dims=spec.texture_dims.to(DEV), texture=spec.texture.to(DEV))
     bcams = [B.Camera(c.viewmat, c.fx, c.fy, c.cx, c.cy, c.width, c.height) for c in cams]
     r = B.BatchRenderer(bcams, spec.num_points, capacity=1 << 20, fwd_ppt=request.param[0],
-                        bwd_ppt=request.param[1], bwd_group=request.param[2])
+                        bwd_ppt=request.param[1], bwd_group=request.param[2], block_width=request.param[3])
     P = r.total_pixels
     gen = torch.Generator().manual_seed(1)
     tgt_img = torch.rand(P, 3, generator=gen).to(DEV)
@@ -44,6 +45,7 @@ def _scene_np(spec, colors):
 
 def test_batch_binning_bit_exact_per_view(setup):
     spec, cams, r, scene, _ = setup
+    bw = r.bw
     assert r.check_capacity()
     ks = r.keys_sorted.cpu().numpy()
     gs = r.gids_sorted.cpu().numpy()
@@ -53,12 +55,12 @@ def test_batch_binning_bit_exact_per_view(setup):
     for v, cam in enumerate(cams):
         c, e = oracle.get_aabb_2d(spec.means.numpy(), spec.scales.numpy(), 1.0, spec.quats.numpy(),
                                   cam.viewmat.numpy(), cam.fx, cam.fy, cam.cx, cam.cy)
-        nt = oracle.num_tiles_hit(c, e, cam.height, cam.width, 16)
+        nt = oracle.num_tiles_hit(c, e, cam.height, cam.width, bw)
         np.testing.assert_array_equal(counts[v], nt)
         d = oracle.camera_depths(spec.means.numpy(), cam.viewmat.numpy())
-        b = oracle.bin_and_sort(c, e, d, nt, cam.height, cam.width, 16)
+        b = oracle.bin_and_sort(c, e, d, nt, cam.height, cam.width, bw)
         m = b["n_isect"]
-        toff = int(sum(((cc.width + 15) // 16) * ((cc.height + 15) // 16) for cc in cams[:v]))
+        toff = int(sum(((cc.width + bw - 1) // bw) * ((cc.height + bw - 1) // bw) for cc in cams[:v]))
         # keys are (global tile << 1 | real): the tile of every slot and the
         # Gaussian order within each tile equal the reference's 64-bit sort
         np.testing.assert_array_equal((ks[off:off + m].astype(np.int64) >> 1) - toff,
@@ -151,6 +153,7 @@ def test_depth_first_binning_equals_64bit_binning(setup):
 
 def test_batch_forward_backward_vs_oracle(setup):
     spec, cams, r, scene, loss = setup
+    bw = r.bw
     gs = r.gids_sorted.cpu().numpy()
     bins = r.bins.cpu().numpy()
     vcol = r.grads["vcolors"][..., :3].cpu().numpy()
@@ -165,10 +168,10 @@ def test_batch_forward_backward_vs_oracle(setup):
         sc = _scene_np(spec, r.colors[v].cpu().numpy())
         oc = oracle.Camera(cam.viewmat.numpy(), cam.c2w.numpy(), cam.fx, cam.fy, cam.cx, cam.cy, cam.height,
                            cam.width)
-        nt = ((cam.width + 15) // 16) * ((cam.height + 15) // 16)
+        nt = ((cam.width + bw - 1) // bw) * ((cam.height + bw - 1) // bw)
         vb = bins[toff:toff + nt]
         toff += nt
-        ref = oracle.texture_forward(sc, oc, gs, vb, 16, 1 << 8, np.zeros(3), prec="f64")
+        ref = oracle.texture_forward(sc, oc, gs, vb, bw, 1 << 8, np.zeros(3), prec="f64")
         for k in ("img", "texture", "normal", "final_T"):
             got = r.view_output(k, v).cpu().numpy()
             err = np.abs(got - ref[k].reshape(got.shape))
@@ -178,7 +181,7 @@ def test_batch_forward_backward_vs_oracle(setup):
         H, W = cam.height, cam.width
         up = dict(img=ups["img"][a:b].reshape(H, W, 3), texture=ups["texture"][a:b].reshape(H, W, 3),
                   normal=ups["normal"][a:b].reshape(H, W, 3), reg=ups["reg"][a:b].reshape(H, W))
-        g = oracle.texture_backward(sc, oc, gs, vb, 16, 1 << 8, np.zeros(3), ref, up["img"], np.zeros((H, W)),
+        g = oracle.texture_backward(sc, oc, gs, vb, bw, 1 << 8, np.zeros(3), ref, up["img"], np.zeros((H, W)),
                                     up["reg"], np.zeros((H, W)), up["texture"], up["normal"], prec="f64")
         err = np.abs(vcol[v] - g["colors"]).max() / (np.abs(g["colors"]).max() + 1e-12)
         assert err < 5e-4, ("vcolors", v, err)
@@ -221,7 +224,7 @@ def test_plain_per_view_step_matches_batched_step(setup):
     tgt_tex = torch.rand(r.total_pixels, 3, generator=gen).to(DEV)
     l_batch = float(r.step(scene, tgt_img, tgt_tex).item())
     g_batch = {k: v.clone() for k, v in r.grads.items()}
-    l_plain, g_plain = B.plain_step(scene, bcams, tgt_img, tgt_tex, r.pix_offsets_host)
+    l_plain, g_plain = B.plain_step(scene, bcams, tgt_img, tgt_tex, r.pix_offsets_host, block_width=r.bw)
     assert abs(float(l_plain.item()) - l_batch) <= 1e-5 * abs(l_batch)
     for k in ("opacity", "means", "scales", "quats", "uv0", "umap", "vmap", "texture", "sh_coeffs"):
         a = g_plain[k].reshape(-1).cpu().numpy()
@@ -237,7 +240,8 @@ def test_forward_tile_order_does_not_change_outputs(setup):
     from gstex_cuda_gb300 import batch as B
     spec, cams, r, scene, _ = setup
     bcams = [B.Camera(c.viewmat, c.fx, c.fy, c.cx, c.cy, c.width, c.height) for c in cams]
-    r2 = B.BatchRenderer(bcams, spec.num_points, capacity=1 << 20, fwd_ppt=r.fwd_ppt, bwd_ppt=r.bwd_ppt,
+    r2 = B.BatchRenderer(bcams, spec.num_points, capacity=1 << 20, block_width=r.bw, fwd_ppt=r.fwd_ppt,
+                         bwd_ppt=r.bwd_ppt,
                          bwd_group=r.bwd_group, heavy_first=False)
     assert r.tile_order is not None and r2.tile_order is None
     for x in (r, r2):
@@ -249,6 +253,33 @@ def test_forward_tile_order_does_not_change_outputs(setup):
     assert np.array_equal(np.sort(order), np.arange(r.total_tiles)) and np.all(np.diff(cost[order]) <= 0)
     for k in ("img", "depth", "reg", "texture", "normal", "final_T", "final_idx", "depth_idx", "reg_s"):
         assert np.array_equal(r.out[k].cpu().numpy(), r2.out[k].cpu().numpy()), k
+
+
+@pytest.mark.parametrize("fwd_batch,bwd_batch", [(64, 128), (128, 64), (32, 32)])
+def test_gaussians_per_batch_does_not_change_results(setup, fwd_batch, bwd_batch):
+    """Staging fewer Gaussians per round than threads per CTA changes when a
+    tile checks for early exit and flushes its moments, not what it
+    composites: forward outputs are bit-identical, gradients equal up to the
+    order of the global atomics."""
+    from gstex_cuda_gb300 import batch as B
+    spec, cams, r, scene, _ = setup
+    bcams = [B.Camera(c.viewmat, c.fx, c.fy, c.cx, c.cy, c.width, c.height) for c in cams]
+    r2 = B.BatchRenderer(bcams, spec.num_points, capacity=1 << 20, block_width=r.bw, fwd_ppt=r.fwd_ppt,
+                         bwd_ppt=r.bwd_ppt,
+                         bwd_group=r.bwd_group, fwd_batch=fwd_batch, bwd_batch=bwd_batch)
+    gen = torch.Generator().manual_seed(1)
+    tgt_img = torch.rand(r.total_pixels, 3, generator=gen).to(DEV)
+    tgt_tex = torch.rand(r.total_pixels, 3, generator=gen).to(DEV)
+    r.step(scene, tgt_img, tgt_tex)
+    g1 = {k: v.clone() for k, v in r.grads.items()}
+    o1 = {k: v.clone() for k, v in r.out.items()}
+    r2.step(scene, tgt_img, tgt_tex)
+    torch.cuda.synchronize()
+    for k in ("img", "depth", "reg", "texture", "normal", "final_T", "final_idx", "depth_idx", "reg_s"):
+        assert np.array_equal(r2.out[k].cpu().numpy(), o1[k].cpu().numpy()), k
+    for k in ("opacity", "means", "scales", "quats", "uv0", "umap", "vmap", "texture", "sh_coeffs"):
+        a, b = r2.grads[k].cpu().numpy(), g1[k].cpu().numpy()
+        assert np.abs(a - b).max() <= 1e-4 * (np.abs(b).max() + 1e-12), k
 
 
 def test_batch_graph_replay_matches_eager(setup):
@@ -275,7 +306,8 @@ def test_prebuilt_records_match_per_tile_records(setup):
     from gstex_cuda_gb300 import batch as B
     spec, cams, r, scene, loss = setup
     bcams = [B.Camera(c.viewmat, c.fx, c.fy, c.cx, c.cy, c.width, c.height) for c in cams]
-    r2 = B.BatchRenderer(bcams, spec.num_points, capacity=1 << 20, fwd_ppt=r.fwd_ppt, bwd_ppt=r.bwd_ppt,
+    r2 = B.BatchRenderer(bcams, spec.num_points, capacity=1 << 20, block_width=r.bw, fwd_ppt=r.fwd_ppt,
+                         bwd_ppt=r.bwd_ppt,
                          bwd_group=r.bwd_group, prebuilt_records=False)
     gen = torch.Generator().manual_seed(1)
     tgt_img = torch.rand(r.total_pixels, 3, generator=gen).to(DEV)

@@ -64,8 +64,11 @@ def _workload(which):
     return synthetic.stress(seed=4, n=1_000_000, texels=32_000_000, views=8)
 
 
-@pytest.mark.parametrize("which", ["multiview_32x_500k_16M", "stress_8x1080p_1M_32M"])
-def test_batched_step_at_full_size_vs_reference_kernels(which):
+@pytest.mark.parametrize("which,bw", [("multiview_32x_500k_16M", 16), ("multiview_32x_500k_16M", 8),
+                                      ("stress_8x1080p_1M_32M", 16)])
+def test_batched_step_at_full_size_vs_reference_kernels(which, bw):
+    """Tile widths 16 (the reference's) and 8 (the autotuner's choice on the
+    32-view scene): the reference's kernels run with the same width."""
     from gstex_cuda_gb300 import batch as B
     from oracle import refkern as R
     spec = _workload(which)
@@ -80,7 +83,7 @@ def test_batched_step_at_full_size_vs_reference_kernels(which):
                     sh_coeffs=d(sh16), sh_degree=spec.sh_degree, uv0=d(spec.uv0), umap=d(spec.umap),
                     vmap=d(spec.vmap), texture_dims=d(spec.texture_dims), texture=d(t16))
     bcams = [B.Camera(c.viewmat, c.fx, c.fy, c.cx, c.cy, c.width, c.height) for c in cams]
-    r = B.BatchRenderer(bcams, spec.num_points, texture_dtype=torch.bfloat16, device=DEV)
+    r = B.BatchRenderer(bcams, spec.num_points, texture_dtype=torch.bfloat16, device=DEV, block_width=bw)
     gen = torch.Generator().manual_seed(11)
     tgt_img = torch.rand(r.total_pixels, 3, generator=gen).to(DEV)
     tgt_tex = torch.rand(r.total_pixels, 3, generator=gen).to(DEV)
@@ -108,10 +111,10 @@ def test_batched_step_at_full_size_vs_reference_kernels(which):
         # binning bit for bit against the oracle's restatement
         c, e = oracle.get_aabb_2d(spec.means.numpy(), spec.scales.numpy(), 1.0, spec.quats.numpy(),
                                   cam.viewmat.numpy(), cam.fx, cam.fy, cam.cx, cam.cy)
-        cnt = oracle.num_tiles_hit(c, e, cam.height, cam.width, 16)
+        cnt = oracle.num_tiles_hit(c, e, cam.height, cam.width, bw)
         np.testing.assert_array_equal(counts_b[v], cnt, err_msg=f"tile counts of view {v}")
         ob = oracle.bin_and_sort(c, e, oracle.camera_depths(spec.means.numpy(), cam.viewmat.numpy()), cnt,
-                                 cam.height, cam.width, 16)
+                                 cam.height, cam.width, bw)
         n = ob["n_isect"]
         obins = ob["tile_bins"].reshape(-1, 2)
         nt = obins.shape[0]
@@ -124,7 +127,7 @@ def test_batched_step_at_full_size_vs_reference_kernels(which):
         # boxes within rounding of a tile boundary
         rc = np_(R.num_tiles_hit(*R.get_aabb_2d(t["means"], t["scales"], 1.0, t["quats"],
                                                 cam.viewmat.contiguous().to(DEV), cam.fx, cam.fy, cam.cx, cam.cy),
-                                 cam.height, cam.width, 16))
+                                 cam.height, cam.width, bw))
         flips = int((rc != cnt).sum())
         count_flips += flips
         assert flips <= max(2, 1e-4 * spec.num_points), (v, flips)
@@ -132,7 +135,7 @@ def test_batched_step_at_full_size_vs_reference_kernels(which):
         local = np.ascontiguousarray(np.where(nonempty, obins, 0).astype(np.int32))
         vg = torch.from_numpy(np.ascontiguousarray(gids_b[off:off + n])).to(DEV)
         vb = torch.from_numpy(local).to(DEV)
-        f = R.view_forward(t, cam, spec.sh_degree, binning=(vg, vb))
+        f = R.view_forward(t, cam, spec.sh_degree, block_width=bw, binning=(vg, vb))
         # SH colours of the view from the same (bf16-rounded) coefficients
         np.testing.assert_allclose(np_(r.colors[v]), np_(f["colors"]), atol=2e-6, rtol=2e-5)
         got = {k: r.view_output(k, v) for k in ("img", "depth", "reg", "texture", "normal", "final_T", "final_idx",
@@ -142,8 +145,8 @@ def test_batched_step_at_full_size_vs_reference_kernels(which):
         # pixel's tile range
         refo = dict(f["out"])
         for k in ("final_idx", "depth_idx"):
-            got[k] = _tile_local(np_(got[k]), bins_b[toff:toff + nt], cam.width, cam.height)
-            refo[k] = _tile_local(np_(refo[k]), local, cam.width, cam.height)
+            got[k] = _tile_local(np_(got[k]), bins_b[toff:toff + nt], cam.width, cam.height, bw)
+            refo[k] = _tile_local(np_(refo[k]), local, cam.width, cam.height, bw)
         # the outlier cap is 5e-2 here (1e-2 in the single-view tests): over
         # 32 random viewpoints some splats are seen almost edge-on, which
         # this path solves in double and the reference in fast-math fp32, so
@@ -156,7 +159,7 @@ def test_batched_step_at_full_size_vs_reference_kernels(which):
         a, b = r.pix_offsets_host[v], r.pix_offsets_host[v + 1]
         H, W = cam.height, cam.width
         ups = {k: r.ups[k][a:b].reshape(H, W, *r.ups[k].shape[1:]) for k in ("img", "texture", "normal", "reg")}
-        g = R.view_backward(t, cam, spec.sh_degree, f, ups)
+        g = R.view_backward(t, cam, spec.sh_degree, f, ups, block_width=bw)
         cref = np_(g["colors"])
         crow = np.abs(np_(vcol_b[v]) - cref).max(-1) / (np.abs(cref).max() + 1e-12)
         assert (crow > 2e-3).mean() <= 1e-3 and crow.max() < cap, ("colors", v, float(crow.max()))
