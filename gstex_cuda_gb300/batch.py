@@ -43,7 +43,7 @@ class BatchInputs(ctypes.Structure):
                 ("colors", _P), ("opacities", _P), ("means", _P), ("scales", _P), ("glob_scale", _F), ("quats", _P),
                 ("uv0", _P), ("umap", _P), ("vmap", _P), ("texture_dims", _P), ("texture", _P), ("background", _P),
                 ("queue", _P), ("grid", _I), ("pixels_per_thread", _I), ("records", _P), ("group_lanes", _I),
-                ("batch_size", _I)]
+                ("batch_size", _I), ("resident_ctas", _I)]
 
 
 class RawGrads(ctypes.Structure):
@@ -154,6 +154,7 @@ class BatchRenderer:
                  block_width: int = 16, settings: int = 1 << 8, background=(0.0, 0.0, 0.0), capacity: int = 0,
                  device="cuda:0", grid: int = 0, loss_weights: Optional[dict] = None, fwd_ppt: int = 1,
                  bwd_ppt: int = 1, bwd_group: int = 8, fwd_batch: int = 0, bwd_batch: int = 0,
+                 bwd_ctas: int = 0,
                  prebuilt_records: bool = True, heavy_first: bool = True):
         self.dev = torch.device(device)
         self.N = int(num_points)
@@ -166,6 +167,7 @@ class BatchRenderer:
         self.fwd_ppt, self.bwd_ppt = int(fwd_ppt), int(bwd_ppt)
         self.bwd_group = int(bwd_group)
         self.fwd_batch, self.bwd_batch = int(fwd_batch), int(bwd_batch)
+        self.bwd_ctas = int(bwd_ctas)
         self.lw = dict(LOSS_WEIGHTS if loss_weights is None else loss_weights)
         L = _L()
         descs = (ViewDesc * self.V)()
@@ -275,6 +277,7 @@ class BatchRenderer:
         bi.pixels_per_thread = self.bwd_ppt if backward else self.fwd_ppt
         bi.group_lanes = self.bwd_group if backward else 32
         bi.batch_size = self.bwd_batch if backward else self.fwd_batch
+        bi.resident_ctas = self.bwd_ctas if backward else 0
         bi.records = ptr(self.records) if self.records is not None else None
         return bi
 
@@ -490,6 +493,8 @@ class BatchRenderer:
             result[f"forward_ppt{ppt}_ms"] = ms
             best = (ms, ppt, 0) if best is None or ms < best[0] else best
         for nb in (64, 128):
+            if nb >= self.bw * self.bw:
+                continue  # not below one Gaussian per thread
             self.fwd_ppt, self.fwd_batch = 1, nb
             ms = timed(lambda: self.forward(s))
             result[f"forward_ppt1_batch{nb}_ms"] = ms
@@ -504,13 +509,27 @@ class BatchRenderer:
             result[f"backward_ppt{ppt}_g{gs}_ms"] = ms
             best = (ms, ppt, gs, 0) if best is None or ms < best[0] else best
         for nb in (64, 128):
+            if nb >= self.bw * self.bw // best[1]:
+                continue  # not below one Gaussian per thread
             self.bwd_ppt, self.bwd_group, self.bwd_batch = best[1], best[2], nb
             ms = timed(lambda: self.backward(s))
             result[f"backward_ppt{best[1]}_g{best[2]}_batch{nb}_ms"] = ms
             best = (ms, best[1], best[2], nb) if ms < best[0] else best
         self.bwd_ppt, self.bwd_group, self.bwd_batch = best[1], best[2], best[3]
+        # 8x8 tiles with 8-lane groups and bf16 RGB texels: kernels compiled
+        # for 9 or 10 resident CTAs per SM (fewer registers, more warps)
+        self.bwd_ctas = 0
+        if self.bw == 8 and self.bwd_ppt == 1 and self.bwd_group == 8 and self.C == 3 and self.texmode == 1:
+            best_c = (best[0], 0)
+            for ctas in (9, 10):
+                self.bwd_ctas = ctas
+                ms = timed(lambda: self.backward(s))
+                result[f"backward_ppt1_g8_ctas{ctas}_ms"] = ms
+                best_c = (ms, ctas) if ms < best_c[0] else best_c
+            self.bwd_ctas = best_c[1]
         result.update(fwd_ppt=self.fwd_ppt, fwd_batch=self.fwd_batch or "threads", bwd_ppt=self.bwd_ppt,
-                      bwd_group=self.bwd_group, bwd_batch=self.bwd_batch or "threads")
+                      bwd_group=self.bwd_group, bwd_batch=self.bwd_batch or "threads",
+                      bwd_ctas=self.bwd_ctas or "default")
         self.graph = None
         return result
 

@@ -509,7 +509,7 @@ static int batch_scene(const gstex_batch_inputs* in, SceneArgs& a, BatchArgs& ba
     GSTEX_REQUIRE(in && in->num_points >= 0 && in->num_views > 0 && in->total_tiles > 0);
     GSTEX_REQUIRE(in->block_width >= 2 && in->block_width <= kMaxBlockWidth);
     GSTEX_REQUIRE(in->channels >= 0);
-    GSTEX_REQUIRE(in->batch_size >= 0);
+    GSTEX_REQUIRE(in->batch_size >= 0 && in->resident_ctas >= 0);
     if (in->channels > kMaxChannels) return GSTEX_ERR_UNSUPPORTED;
     if (in->texture_dtype == 1 && in->channels != 3) return GSTEX_ERR_UNSUPPORTED;
     GSTEX_REQUIRE(in->views && in->tile_view && in->tile_bins && in->background && in->queue);
@@ -573,7 +573,7 @@ extern "C" int gstex_batch_records(const gstex_batch_inputs* in, const int32_t* 
 static int grid_of(const gstex_batch_inputs* in, bool backward) {
     if (in->grid > 0) return in->grid;
     int g = resident_ctas(in->block_width, backward, in->texture_dtype, in->channels, in->pixels_per_thread,
-                          in->group_lanes);
+                          in->group_lanes, backward ? in->resident_ctas : 0);
     return g > 0 ? g : 152;
 }
 
@@ -633,7 +633,7 @@ static int batch_backward_impl(const gstex_batch_inputs* in, const gstex_backwar
                io->v_depth, io->v_reg, io->v_alpha, io->v_texture, (const float3*)io->v_normal,
                (float*)io->workspace, io->v_tex_grad };
     if ((rc = launch_bwd_batch(a, ba, g, in->block_width, in->texture_dtype, in->pixels_per_thread,
-                               in->group_lanes, grid_of(in, true), stream)))
+                               in->group_lanes, in->resident_ctas, grid_of(in, true), stream)))
         return rc;
     return launch_finalize(a, (const float*)io->workspace, io->v_opacity, io->v_means, io->v_scales, io->v_quats,
                            io->v_uv0, io->v_umap, io->v_vmap, stream, rg);

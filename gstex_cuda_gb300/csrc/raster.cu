@@ -1013,7 +1013,7 @@ __global__ void FWD_BOUNDS(PPT) fwd_batch_kernel(SceneArgs a, BatchArgs ba, FwdO
 }
 
 template <int TEXMODE, int CT, int PPT, int GS>
-__global__ void BWD_BOUNDS(PPT) bwd_batch_kernel(SceneArgs a, BatchArgs ba, BwdArgs g) {
+__device__ __forceinline__ void bwd_batch_body(const SceneArgs& a, const BatchArgs& ba, const BwdArgs& g) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_tile;
     const int nthr = blockDim.x * blockDim.y;
@@ -1023,6 +1023,21 @@ __global__ void BWD_BOUNDS(PPT) bwd_batch_kernel(SceneArgs a, BatchArgs ba, BwdA
     uint8_t* lists = smem + (size_t)(kRecBytes + kEdgeBytes + kMomSlot * sizeof(float)) * nthr;
     uint8_t* touched = lists + ((size_t)ceil_div(nthr, 32) + (GS < 32 ? ceil_div(nthr, GS) : 0)) * nthr;
     while (next_job(ba, &s_tile, J)) bwd_tile<TEXMODE, CT, PPT, GS>(a, J, g, R, smom, lists, touched);
+}
+
+template <int TEXMODE, int CT, int PPT, int GS>
+__global__ void BWD_BOUNDS(PPT) bwd_batch_kernel(SceneArgs a, BatchArgs ba, BwdArgs g) {
+    bwd_batch_body<TEXMODE, CT, PPT, GS>(a, ba, g);
+}
+
+// 8x8 tiles (64 threads, one pixel each) with 8-lane groups, compiled for
+// NB resident CTAs per SM: at most 112 registers per thread for 9 CTAs, 96
+// for 10 (the general kernel uses 124, which allows 8), in exchange for more
+// warps per SM.
+template <int TEXMODE, int CT, int NB>
+__global__ void __launch_bounds__(64) __maxnreg__(NB == 9 ? 112 : 96)
+    bwd_batch64_kernel(SceneArgs a, BatchArgs ba, BwdArgs g) {
+    bwd_batch_body<TEXMODE, CT, 1, 8>(a, ba, g);
 }
 
 // Writes the 32 records of a warp, assembled in shared memory (src), to
@@ -1340,27 +1355,53 @@ int launch_fwd_batch(const SceneArgs& a, const BatchArgs& ba, const FwdOut& o, i
     return check_launch("batch forward");
 }
 
+// The backward kernel of a launch: the 64-thread variant compiled for
+// `ctas` resident CTAs per SM where one exists (8x8 tiles, one pixel per
+// thread, 8-lane groups, bf16 texels with 3 channels; ctas 9 or 10), else the
+// general kernel.
+static BwdBatch<0, 0, 1, 32>::type pick_bwd_batch(int bw, int C, int texmode, int ppt, int gs, int ctas) {
+    if (threads_of(bw, ppt) == 64 && ppt == 1 && gs == 8 && C == 3 && texmode == 1) {
+        if (ctas == 9) return bwd_batch64_kernel<1, 3, 9>;
+        if (ctas == 10) return bwd_batch64_kernel<1, 3, 10>;
+    }
+    return pick<BwdBatch>(C, texmode, ppt, gs);
+}
+
+// Dynamic shared memory of a backward kernel; the 64-thread variants also ask
+// for the largest shared-memory carveout, which 10 CTAs of 22 KB need.
+template <typename K>
+static int set_bwd_smem(K k, size_t smem, const char* what) {
+    int rc = set_smem(k, smem, what);
+    if (rc) return rc;
+    if (k == (K)bwd_batch64_kernel<1, 3, 9> || k == (K)bwd_batch64_kernel<1, 3, 10>) {
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                             (int)cudaSharedmemCarveoutMaxShared);
+        if (e != cudaSuccess) { set_cuda_error(e, what); return GSTEX_ERR_CUDA; }
+    }
+    return GSTEX_OK;
+}
+
 int launch_bwd_batch(const SceneArgs& a, const BatchArgs& ba, const BwdArgs& g, int bw, int texmode, int ppt, int gs,
-                     int grid, cudaStream_t stream) {
+                     int ctas, int grid, cudaStream_t stream) {
     ppt = ppt_of(bw, ppt);
     gs = gs_of(bw, ppt, a.C, gs);
-    auto k = pick<BwdBatch>(a.C, texmode, ppt, gs);
+    auto k = pick_bwd_batch(bw, a.C, texmode, ppt, gs, ctas);
     const size_t smem = bwd_smem(bw, ppt, gs);
-    int rc = set_smem(k, smem, "batch backward");
+    int rc = set_bwd_smem(k, smem, "batch backward");
     if (rc) return rc;
     k<<<grid, block_of(bw, ppt), smem, stream>>>(a, ba, g);
     return check_launch("batch backward");
 }
 
-int resident_ctas(int bw, bool backward, int texmode, int C, int ppt, int gs) {
+int resident_ctas(int bw, bool backward, int texmode, int C, int ppt, int gs, int ctas) {
     int n = 0;
     cudaError_t e;
     ppt = ppt_of(bw, ppt);
     gs = gs_of(bw, ppt, C, gs);
     if (backward) {
-        auto k = pick<BwdBatch>(C, texmode, ppt, gs);
+        auto k = pick_bwd_batch(bw, C, texmode, ppt, gs, ctas);
         const size_t smem = bwd_smem(bw, ppt, gs);
-        if (set_smem(k, smem, "occupancy")) return 0;
+        if (set_bwd_smem(k, smem, "occupancy")) return 0;
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, threads_of(bw, ppt), smem);
     } else {
         auto k = pick_fwd<FwdBatch>(C, texmode, ppt, 0);

@@ -108,7 +108,7 @@ size_t bwd_smem(int bw, int ppt, int gs);
 int launch_fwd_batch(const SceneArgs& a, const BatchArgs& ba, const FwdOut& o, int bw, int texmode, int ppt, int grid,
                      cudaStream_t stream);
 int launch_bwd_batch(const SceneArgs& a, const BatchArgs& ba, const BwdArgs& g, int bw, int texmode, int ppt, int gs,
-                     int grid, cudaStream_t stream);
+                     int ctas, int grid, cudaStream_t stream);
 // Gradients w.r.t. the trainer's raw parameters (raw_quats == nullptr: the
 // activated parameters' gradients are written instead).
 struct RawGradArgs {
@@ -124,7 +124,7 @@ struct RawGradArgs {
 int launch_finalize(const SceneArgs& a, const float* moments, float* v_opac, float* v_means, float* v_scales,
                     float* v_quats, float* v_uv0, float* v_umap, float* v_vmap, cudaStream_t stream,
                     const RawGradArgs& rg = RawGradArgs{});
-int resident_ctas(int bw, bool backward, int texmode, int C, int ppt, int gs);
+int resident_ctas(int bw, bool backward, int texmode, int C, int ppt, int gs, int ctas = 0);
 int launch_records(const SceneArgs& a, const BatchArgs& ba, int num_views, const int32_t* counts, RecAll* recs,
                    int* fix_count, uint32_t* fix, cudaStream_t stream);
 

@@ -390,6 +390,9 @@ typedef struct gstex_batch_inputs {
     int group_lanes;                    /* backward: lanes per splat walk (see gstex_raster_inputs) */
     int batch_size;                     /* Gaussians a tile stages per round, 1..threads per CTA;
                                            0 = one per thread (the reference's bw^2) */
+    int resident_ctas;                  /* backward, 8x8 tiles with 8-lane groups and bf16 RGB texels:
+                                           9 or 10 selects a kernel compiled for that many CTAs per SM
+                                           (fewer registers per thread); other values: the general kernel */
 } gstex_batch_inputs;
 
 /* Bytes of the per-(view, Gaussian) splat records of gstex_batch_records

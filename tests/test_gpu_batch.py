@@ -349,6 +349,40 @@ def _bf16_case():
     return spec, cams, r, t16[:, :3].double().numpy(), sh16.double().numpy()
 
 
+def test_backward_occupancy_variants_match_general_kernel():
+    """8x8 tiles, 8-lane groups, bf16 texels: the backward kernels compiled
+    for 9 and 10 resident CTAs per SM (fewer registers) give the general
+    kernel's gradients up to the order of the global atomics."""
+    from gstex_cuda_gb300 import batch as B, synthetic
+    g = torch.Generator().manual_seed(23)
+    cams = synthetic.sphere_cameras(g, 3, radius=8.0, resolutions=[(96, 64), (80, 80), (128, 72)])
+    spec = synthetic._finish_with_area(g, torch.empty(2500, 3).uniform_(-3, 3, generator=g), 0.01, 0.1, 3, "normal",
+                                       cams, 30_000, "multi", {})
+    t16 = torch.zeros(spec.texture.shape[0], 4, dtype=torch.bfloat16)
+    t16[:, :3] = spec.texture.to(torch.bfloat16)
+    scene = B.Scene(means=spec.means.to(DEV), scales=spec.scales.to(DEV), quats=spec.quats.to(DEV),
+                    opacity=spec.opacity.to(DEV), sh_coeffs=spec.sh_coeffs.to(torch.bfloat16).to(DEV), sh_degree=3,
+                    uv0=spec.uv0.to(DEV), umap=spec.umap.to(DEV), vmap=spec.vmap.to(DEV),
+                    texture_dims=spec.texture_dims.to(DEV), texture=t16.to(DEV))
+    bcams = [B.Camera(c.viewmat, c.fx, c.fy, c.cx, c.cy, c.width, c.height) for c in cams]
+    gen = torch.Generator().manual_seed(2)
+    P = sum(c.width * c.height for c in cams)
+    tgt_img = torch.rand(P, 3, generator=gen).to(DEV)
+    tgt_tex = torch.rand(P, 3, generator=gen).to(DEV)
+    res = {}
+    for ctas in (0, 9, 10):
+        r = B.BatchRenderer(bcams, spec.num_points, texture_dtype=torch.bfloat16, capacity=1 << 20, block_width=8,
+                            bwd_group=8, bwd_ctas=ctas)
+        loss = float(r.step(scene, tgt_img, tgt_tex).item())
+        torch.cuda.synchronize()
+        res[ctas] = (loss, {k: v.cpu().numpy().copy() for k, v in r.grads.items()})
+    for ctas in (9, 10):
+        assert abs(res[ctas][0] - res[0][0]) <= 1e-5 * abs(res[0][0])  # the loss sums by atomics
+        for k in ("opacity", "means", "scales", "quats", "uv0", "umap", "vmap", "texture", "sh_coeffs"):
+            a, b = res[ctas][1][k], res[0][1][k]
+            assert np.abs(a - b).max() <= 1e-4 * (np.abs(b).max() + 1e-12), (ctas, k)
+
+
 def _oracle_views(spec, cams, r, texture, sh):
     """Per-view fp64 oracle outputs and view-summed gradients for the given
     texel values and SH coefficients, on the renderer's binning."""
