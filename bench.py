@@ -62,8 +62,10 @@ def parse():
     p.add_argument("--no-autotune", action="store_true",
                    help="use the backward variant given by --bwd-group (profiling runs)")
     p.add_argument("--bwd-group", type=int, default=8)
+    p.add_argument("--bwd-ctas", type=int, default=10,
+                   help="with --no-autotune: backward kernel compiled for this many CTAs per SM (8x8 tiles)")
     p.add_argument("--tile-widths", default="16,8",
-                   help="tile widths the autotuner tries (each bins the scene anew); the first is used "
+                   help="tile widths the autotuner tries (each bins the scene anew); the last is used "
                         "with --no-autotune")
     p.add_argument("--no-graph", action="store_true")
     return p.parse_args()
@@ -359,10 +361,10 @@ def main():
     tgt_img = torch.rand(P, 3, generator=gen).to(dev)
     tgt_tex = torch.rand(P, 3, generator=gen).to(dev)
     if args.no_autotune:
-        r = make_renderer(widths[0])
-        r.bwd_group = args.bwd_group
+        r = make_renderer(widths[-1])
+        r.bwd_group, r.bwd_ctas = args.bwd_group, args.bwd_ctas
         tuned = {"fixed": True, "block_width": r.bw, "fwd_ppt": r.fwd_ppt, "bwd_ppt": r.bwd_ppt,
-                 "bwd_group": r.bwd_group}
+                 "bwd_group": r.bwd_group, "bwd_ctas": r.bwd_ctas}
     else:
         # tile width: each candidate bins the scene anew, is tuned on its own
         # and timed over whole steps; the fastest renderer is kept

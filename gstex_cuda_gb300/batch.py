@@ -520,13 +520,13 @@ class BatchRenderer:
         # for 9 or 10 resident CTAs per SM (fewer registers, more warps)
         self.bwd_ctas = 0
         if self.bw == 8 and self.bwd_ppt == 1 and self.bwd_group == 8 and self.C == 3 and self.texmode == 1:
-            best_c = (best[0], 0)
-            for ctas in (9, 10):
-                self.bwd_ctas = ctas
+            best_c = (best[0], 0, self.bwd_batch)
+            for ctas, nb in ((9, 0), (10, 0), (10, 48)):
+                self.bwd_ctas, self.bwd_batch = ctas, nb
                 ms = timed(lambda: self.backward(s))
-                result[f"backward_ppt1_g8_ctas{ctas}_ms"] = ms
-                best_c = (ms, ctas) if ms < best_c[0] else best_c
-            self.bwd_ctas = best_c[1]
+                result[f"backward_ppt1_g8_ctas{ctas}_batch{nb or 'threads'}_ms"] = ms
+                best_c = (ms, ctas, nb) if ms < best_c[0] else best_c
+            self.bwd_ctas, self.bwd_batch = best_c[1], best_c[2]
         result.update(fwd_ppt=self.fwd_ppt, fwd_batch=self.fwd_batch or "threads", bwd_ppt=self.bwd_ppt,
                       bwd_group=self.bwd_group, bwd_batch=self.bwd_batch or "threads",
                       bwd_ctas=self.bwd_ctas or "default")

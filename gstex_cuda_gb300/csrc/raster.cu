@@ -621,9 +621,11 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
     const int bw = blockDim.x;
     const unsigned lane = tr & 31;
     const unsigned wmask = __activemask();
-    // candidate lists: one per warp, then (GS < 32) one per group
-    uint8_t* wl = lists + (tr >> 5) * nthr;
-    uint8_t* gl = lists + ((size_t)ceil_div(nthr, 32) + tr / GS) * nthr;
+    // Gaussians staged per round (the shared-memory slots); candidate lists
+    // of that length: one per warp, then (GS < 32) one per group
+    const int bsz = batch_of(a, nthr);
+    uint8_t* wl = lists + (tr >> 5) * bsz;
+    uint8_t* gl = lists + ((size_t)ceil_div(nthr, 32) + tr / GS) * bsz;
     const bool full_warp = wmask == 0xffffffffu;
     int my_slot[Red::OUT];
 #pragma unroll
@@ -679,7 +681,6 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
     const unsigned gmask = (GS == 32) ? wmask : (((1u << GS) - 1u) << (lane & ~(unsigned)(GS - 1)));
 
     const int2 range = J.range;
-    const int bsz = batch_of(a, nthr);  // Gaussians staged per round
     const int nb = ceil_div(range.y - range.x, bsz);
     for (int b = 0; b < nb; ++b) {
         __syncthreads();
@@ -690,7 +691,7 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
         if (mine) stage_job(R, tr, a, J, a.gids[idx], use_blur);
         for (int q = tr; q < bsz * (kMomSlot / 4); q += nthr)
             reinterpret_cast<float4*>(smom)[q] = make_float4(0.f, 0.f, 0.f, 0.f);
-        touched[tr] = 0;
+        if (tr < bsz) touched[tr] = 0;
         __syncthreads();
         // splats outside their alpha >= 1/255 box contribute nothing here:
         // walk the candidates of the warp or group, back to front
@@ -1007,8 +1008,8 @@ __global__ void FWD_BOUNDS(PPT) fwd_batch_kernel(SceneArgs a, BatchArgs ba, FwdO
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_tile;
     TileJob J;
-    const int nthr = blockDim.x * blockDim.y;
-    const Recs R = Recs::carve(smem, nthr, false);
+    const int slots = batch_of(a, blockDim.x * blockDim.y);
+    const Recs R = Recs::carve(smem, slots, false);
     while (next_job(ba, &s_tile, J)) fwd_tile<TEXMODE, CT, PPT>(a, J, o, R);
 }
 
@@ -1017,11 +1018,12 @@ __device__ __forceinline__ void bwd_batch_body(const SceneArgs& a, const BatchAr
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_tile;
     const int nthr = blockDim.x * blockDim.y;
+    const int slots = batch_of(a, nthr);
     TileJob J;
-    const Recs R = Recs::carve(smem, nthr, true);
-    float* smom = reinterpret_cast<float*>(smem + (size_t)(kRecBytes + kEdgeBytes) * nthr);
-    uint8_t* lists = smem + (size_t)(kRecBytes + kEdgeBytes + kMomSlot * sizeof(float)) * nthr;
-    uint8_t* touched = lists + ((size_t)ceil_div(nthr, 32) + (GS < 32 ? ceil_div(nthr, GS) : 0)) * nthr;
+    const Recs R = Recs::carve(smem, slots, true);
+    float* smom = reinterpret_cast<float*>(smem + (size_t)(kRecBytes + kEdgeBytes) * slots);
+    uint8_t* lists = smem + (size_t)(kRecBytes + kEdgeBytes + kMomSlot * sizeof(float)) * slots;
+    uint8_t* touched = lists + ((size_t)ceil_div(nthr, 32) + (GS < 32 ? ceil_div(nthr, GS) : 0)) * slots;
     while (next_job(ba, &s_tile, J)) bwd_tile<TEXMODE, CT, PPT, GS>(a, J, g, R, smom, lists, touched);
 }
 
@@ -1031,11 +1033,14 @@ __global__ void BWD_BOUNDS(PPT) bwd_batch_kernel(SceneArgs a, BatchArgs ba, BwdA
 }
 
 // 8x8 tiles (64 threads, one pixel each) with 8-lane groups, compiled for
-// NB resident CTAs per SM: at most 112 registers per thread for 9 CTAs, 96
-// for 10 (the general kernel uses 124, which allows 8), in exchange for more
-// warps per SM.
+// NB resident CTAs per SM: at most 65536 / (64 NB) registers per thread
+// rounded down to a multiple of 8 (112 for 9 CTAs, 96 for 10; the general
+// kernel uses 124, which allows 8), in exchange for more warps per SM.  (11
+// and 12 CTAs, at 88 and 80 registers and with fewer Gaussians per batch so
+// that the shared memory fits, spill 144-188 bytes and lose.)
+constexpr int regs_for_ctas(int nb) { return (65536 / (64 * nb)) / 8 * 8; }
 template <int TEXMODE, int CT, int NB>
-__global__ void __launch_bounds__(64) __maxnreg__(NB == 9 ? 112 : 96)
+__global__ void __launch_bounds__(64) __maxnreg__(regs_for_ctas(NB))
     bwd_batch64_kernel(SceneArgs a, BatchArgs ba, BwdArgs g) {
     bwd_batch_body<TEXMODE, CT, 1, 8>(a, ba, g);
 }
@@ -1323,15 +1328,21 @@ template <int M, int C, int P, int G> struct BwdBatch { typedef void (*type)(Sce
 static dim3 block_of(int bw, int ppt) { return dim3(bw, bw / ppt); }
 static int threads_of(int bw, int ppt) { return bw * (bw / ppt); }
 // records, then (backward) the moment slots, then one candidate list per warp
-static size_t list_bytes(int bw, int ppt, int gs) {
+// Shared-memory slots of a launch: `batch` Gaussians per round when set
+// below the threads of the CTA, else one per thread.
+static int slots_of(int bw, int ppt, int batch) {
     const int n = threads_of(bw, ppt);
-    return ((size_t)ceil_div(n, 32) + (gs < 32 ? (size_t)ceil_div(n, gs) : 0)) * n;
+    return (batch > 0 && batch < n) ? batch : n;
 }
-size_t fwd_smem(int bw, int ppt) { return (size_t)kRecBytes * threads_of(bw, ppt); }
-size_t bwd_smem(int bw, int ppt, int gs) {
+static size_t list_bytes(int bw, int ppt, int gs, int batch) {
+    const int n = threads_of(bw, ppt);
+    return ((size_t)ceil_div(n, 32) + (gs < 32 ? (size_t)ceil_div(n, gs) : 0)) * slots_of(bw, ppt, batch);
+}
+size_t fwd_smem(int bw, int ppt, int batch) { return (size_t)kRecBytes * slots_of(bw, ppt, batch); }
+size_t bwd_smem(int bw, int ppt, int gs, int batch) {
     // ... then one "touched" flag per slot
-    return ((size_t)kRecBytes + kEdgeBytes + kMomSlot * sizeof(float) + 1) * threads_of(bw, ppt) +
-           list_bytes(bw, ppt, gs);
+    return ((size_t)kRecBytes + kEdgeBytes + kMomSlot * sizeof(float) + 1) * slots_of(bw, ppt, batch) +
+           list_bytes(bw, ppt, gs, batch);
 }
 
 int launch_finalize(const SceneArgs& a, const float* moments, float* v_opac, float* v_means, float* v_scales,
@@ -1348,7 +1359,7 @@ int launch_fwd_batch(const SceneArgs& a, const BatchArgs& ba, const FwdOut& o, i
                      cudaStream_t stream) {
     ppt = ppt_of(bw, ppt);
     auto k = pick_fwd<FwdBatch>(a.C, texmode, ppt, a.settings);
-    const size_t smem = fwd_smem(bw, ppt);
+    const size_t smem = fwd_smem(bw, ppt, a.batch);
     int rc = set_smem(k, smem, "batch forward");
     if (rc) return rc;
     k<<<grid, block_of(bw, ppt), smem, stream>>>(a, ba, o);
@@ -1386,26 +1397,26 @@ int launch_bwd_batch(const SceneArgs& a, const BatchArgs& ba, const BwdArgs& g, 
     ppt = ppt_of(bw, ppt);
     gs = gs_of(bw, ppt, a.C, gs);
     auto k = pick_bwd_batch(bw, a.C, texmode, ppt, gs, ctas);
-    const size_t smem = bwd_smem(bw, ppt, gs);
+    const size_t smem = bwd_smem(bw, ppt, gs, a.batch);
     int rc = set_bwd_smem(k, smem, "batch backward");
     if (rc) return rc;
     k<<<grid, block_of(bw, ppt), smem, stream>>>(a, ba, g);
     return check_launch("batch backward");
 }
 
-int resident_ctas(int bw, bool backward, int texmode, int C, int ppt, int gs, int ctas) {
+int resident_ctas(int bw, bool backward, int texmode, int C, int ppt, int gs, int ctas, int batch) {
     int n = 0;
     cudaError_t e;
     ppt = ppt_of(bw, ppt);
     gs = gs_of(bw, ppt, C, gs);
     if (backward) {
         auto k = pick_bwd_batch(bw, C, texmode, ppt, gs, ctas);
-        const size_t smem = bwd_smem(bw, ppt, gs);
+        const size_t smem = bwd_smem(bw, ppt, gs, batch);
         if (set_bwd_smem(k, smem, "occupancy")) return 0;
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, threads_of(bw, ppt), smem);
     } else {
         auto k = pick_fwd<FwdBatch>(C, texmode, ppt, 0);
-        const size_t smem = fwd_smem(bw, ppt);
+        const size_t smem = fwd_smem(bw, ppt, batch);
         if (set_smem(k, smem, "occupancy")) return 0;
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, threads_of(bw, ppt), smem);
     }
@@ -1477,7 +1488,7 @@ extern "C" int gstex_texture_forward(const gstex_raster_inputs* in, const gstex_
     const dim3 grid(va.tiles_x, ceil_div(va.H, bw));
     int ppt = ppt_of(bw, in->pixels_per_thread);
     auto k = pick_fwd<FwdView>(a.C, in->texture_dtype, ppt, a.settings);
-    const size_t smem = fwd_smem(bw, ppt);
+    const size_t smem = fwd_smem(bw, ppt, 0);
     if ((rc = set_smem(k, smem, "texture_forward"))) return rc;
     k<<<grid, block_of(bw, ppt), smem, stream>>>(a, va, o);
     return check_launch("texture_forward");
@@ -1563,7 +1574,7 @@ extern "C" int gstex_texture_backward(const gstex_raster_inputs* in, const gstex
     const int ppt = ppt_of(bw, in->pixels_per_thread);
     const int gs = gs_of(bw, ppt, a.C, in->group_lanes);
     auto k = pick<BwdView>(a.C, in->texture_dtype, ppt, gs);
-    const size_t smem = bwd_smem(bw, ppt, gs);
+    const size_t smem = bwd_smem(bw, ppt, gs, 0);
     if ((rc = set_smem(k, smem, "texture_backward"))) return rc;
     k<<<grid, block_of(bw, ppt), smem, stream>>>(a, va, g);
     if ((rc = check_launch("texture_backward"))) return rc;

@@ -103,8 +103,9 @@ struct BwdArgs {
 int fill_scene(const gstex_raster_inputs* in, SceneArgs& a, bool need_bins);
 int ppt_of(int bw, int requested);
 int gs_of(int bw, int ppt, int C, int requested);
-size_t fwd_smem(int bw, int ppt);
-size_t bwd_smem(int bw, int ppt, int gs);
+// shared memory of a compositor CTA staging `batch` Gaussians per round (0: one per thread)
+size_t fwd_smem(int bw, int ppt, int batch);
+size_t bwd_smem(int bw, int ppt, int gs, int batch);
 int launch_fwd_batch(const SceneArgs& a, const BatchArgs& ba, const FwdOut& o, int bw, int texmode, int ppt, int grid,
                      cudaStream_t stream);
 int launch_bwd_batch(const SceneArgs& a, const BatchArgs& ba, const BwdArgs& g, int bw, int texmode, int ppt, int gs,
@@ -124,7 +125,7 @@ struct RawGradArgs {
 int launch_finalize(const SceneArgs& a, const float* moments, float* v_opac, float* v_means, float* v_scales,
                     float* v_quats, float* v_uv0, float* v_umap, float* v_vmap, cudaStream_t stream,
                     const RawGradArgs& rg = RawGradArgs{});
-int resident_ctas(int bw, bool backward, int texmode, int C, int ppt, int gs, int ctas = 0);
+int resident_ctas(int bw, bool backward, int texmode, int C, int ppt, int gs, int ctas = 0, int batch = 0);
 int launch_records(const SceneArgs& a, const BatchArgs& ba, int num_views, const int32_t* counts, RecAll* recs,
                    int* fix_count, uint32_t* fix, cudaStream_t stream);
 

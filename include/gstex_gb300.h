@@ -392,7 +392,8 @@ typedef struct gstex_batch_inputs {
                                            0 = one per thread (the reference's bw^2) */
     int resident_ctas;                  /* backward, 8x8 tiles with 8-lane groups and bf16 RGB texels:
                                            9 or 10 selects a kernel compiled for that many CTAs per SM
-                                           (fewer registers per thread); other values: the general kernel */
+                                           (112 / 96 registers per thread instead of 124); other values:
+                                           the general kernel */
 } gstex_batch_inputs;
 
 /* Bytes of the per-(view, Gaussian) splat records of gstex_batch_records

@@ -351,8 +351,9 @@ def _bf16_case():
 
 def test_backward_occupancy_variants_match_general_kernel():
     """8x8 tiles, 8-lane groups, bf16 texels: the backward kernels compiled
-    for 9 and 10 resident CTAs per SM (fewer registers) give the general
-    kernel's gradients up to the order of the global atomics."""
+    for 9 and 10 resident CTAs per SM (fewer registers; 10 also with 48
+    Gaussians per batch) give the general kernel's gradients up to the order
+    of the global atomics."""
     from gstex_cuda_gb300 import batch as B, synthetic
     g = torch.Generator().manual_seed(23)
     cams = synthetic.sphere_cameras(g, 3, radius=8.0, resolutions=[(96, 64), (80, 80), (128, 72)])
@@ -370,17 +371,19 @@ def test_backward_occupancy_variants_match_general_kernel():
     tgt_img = torch.rand(P, 3, generator=gen).to(DEV)
     tgt_tex = torch.rand(P, 3, generator=gen).to(DEV)
     res = {}
-    for ctas in (0, 9, 10):
+    cases = ((0, 0), (9, 0), (10, 0), (10, 48))
+    for ctas, nb in cases:
         r = B.BatchRenderer(bcams, spec.num_points, texture_dtype=torch.bfloat16, capacity=1 << 20, block_width=8,
-                            bwd_group=8, bwd_ctas=ctas)
+                            bwd_group=8, bwd_ctas=ctas, bwd_batch=nb)
         loss = float(r.step(scene, tgt_img, tgt_tex).item())
         torch.cuda.synchronize()
-        res[ctas] = (loss, {k: v.cpu().numpy().copy() for k, v in r.grads.items()})
-    for ctas in (9, 10):
-        assert abs(res[ctas][0] - res[0][0]) <= 1e-5 * abs(res[0][0])  # the loss sums by atomics
+        res[(ctas, nb)] = (loss, {k: v.cpu().numpy().copy() for k, v in r.grads.items()})
+    base = res[cases[0]]
+    for case in cases[1:]:
+        assert abs(res[case][0] - base[0]) <= 1e-5 * abs(base[0])  # the loss sums by atomics
         for k in ("opacity", "means", "scales", "quats", "uv0", "umap", "vmap", "texture", "sh_coeffs"):
-            a, b = res[ctas][1][k], res[0][1][k]
-            assert np.abs(a - b).max() <= 1e-4 * (np.abs(b).max() + 1e-12), (ctas, k)
+            a, b = res[case][1][k], base[1][k]
+            assert np.abs(a - b).max() <= 1e-4 * (np.abs(b).max() + 1e-12), (case, k)
 
 
 def _oracle_views(spec, cams, r, texture, sh):
