@@ -216,19 +216,27 @@ def reference_kernels_leg(spec, dev, steps, warmup=1):
 
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one compositor
-# launch on the full 32-view workload, from a single-pass ncu capture of that
-# launch (profiles/compositor_dram_traffic_32views.md gives the command and
-# the raw figures).  Keyed by kernel; used only for the default workload.
-DRAM_BYTES_PER_LAUNCH = {}
+# launch on the full 32-view workload, from single-pass ncu captures of the
+# launches of one step (profiles/compositor_dram_traffic_32views.txt gives the
+# commands and the raw figures).  Keyed by (kernel, tile width); tile width 8
+# is the backward variant compiled for 10 CTAs per SM with 8-lane groups, 16
+# the general backward kernel with 8-lane groups (figures printed in GB with
+# two decimals).  Used only for the default workload.
+DRAM_BYTES_PER_LAUNCH = {
+    ("forward", 8): 20_606_735_360 + 1_797_965_568,
+    ("backward", 8): 21_534_149_120 + 7_764_672_256,
+    ("forward", 16): 13.14e9 + 1.77e9,
+    ("backward", 16): 20.45e9 + 7.37e9,
+}
 TRAFFIC_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch, 32-view workload"
 
 
-def dram_traffic_model(kernel, workload="batched", views=32):
-    """Measured DRAM bytes of one launch of `kernel` on the default workload,
-    or None (other workloads, or no capture of this build)."""
+def dram_traffic_model(kernel, block_width, workload="batched", views=32):
+    """Measured DRAM bytes of one launch of `kernel` at this tile width on the
+    default workload, or None (other workloads or widths)."""
     if workload != "batched" or views != 32:
         return None
-    return DRAM_BYTES_PER_LAUNCH.get(kernel)
+    return DRAM_BYTES_PER_LAUNCH.get((kernel, block_width))
 
 
 def algorithmic_bytes(I, tiles, T, P, C, N, tex_bytes_per_texel, grad_texel_bytes, backward):
@@ -344,16 +352,19 @@ def main():
     scene = device_scene(spec, dev, bf16=True)
     widths = [int(w) for w in args.tile_widths.split(",") if w]
 
-    def make_renderer(bw):
+    def make_renderer(bw, **knobs):
         r = B.BatchRenderer(cams, spec.num_points, channels=3, texture_dtype=torch.bfloat16, device=dev,
-                            block_width=bw)
-        # first step: size the intersection buffers
+                            block_width=bw, **knobs)
+        # first steps: size the intersection buffers
         r.step(scene, tgt_img, tgt_tex)
         torch.cuda.synchronize(dev)
+        sizing = 1
         while not r.check_capacity():
             r.grow(1.25)
             r.step(scene, tgt_img, tgt_tex)
             torch.cuda.synchronize(dev)
+            sizing += 1
+        log(f"block width {bw}: sizing steps: {sizing}")
         return r
 
     P = sum(c.width * c.height for c in cams)
@@ -361,8 +372,7 @@ def main():
     tgt_img = torch.rand(P, 3, generator=gen).to(dev)
     tgt_tex = torch.rand(P, 3, generator=gen).to(dev)
     if args.no_autotune:
-        r = make_renderer(widths[-1])
-        r.bwd_group, r.bwd_ctas = args.bwd_group, args.bwd_ctas
+        r = make_renderer(widths[-1], bwd_group=args.bwd_group, bwd_ctas=args.bwd_ctas)
         tuned = {"fixed": True, "block_width": r.bw, "fwd_ppt": r.fwd_ppt, "bwd_ppt": r.bwd_ppt,
                  "bwd_group": r.bwd_group, "bwd_ctas": r.bwd_ctas}
     else:
@@ -507,7 +517,7 @@ def main():
     peak, peak_kind = measured_peak_hbm()
     dom = ("backward", bb, bwd_ms) if bwd_ms >= fwd_ms else ("forward", fb, fwd_ms)
     achieved = dom[1] / (dom[2] / 1000.0) / 1e9
-    traffic = dram_traffic_model(dom[0], args.workload, nviews)
+    traffic = dram_traffic_model(dom[0], r.bw, args.workload, nviews)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
