@@ -573,7 +573,7 @@ extern "C" int gstex_batch_records(const gstex_batch_inputs* in, const int32_t* 
 static int grid_of(const gstex_batch_inputs* in, bool backward) {
     if (in->grid > 0) return in->grid;
     int g = resident_ctas(in->block_width, backward, in->texture_dtype, in->channels, in->pixels_per_thread,
-                          in->group_lanes, backward ? in->resident_ctas : 0, in->batch_size);
+                          in->group_lanes, backward ? in->resident_ctas : 0, in->batch_size, in->settings);
     return g > 0 ? g : 152;
 }
 

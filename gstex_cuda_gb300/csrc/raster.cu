@@ -244,17 +244,18 @@ __device__ __forceinline__ int build_group_list(uint8_t* gl, const uint8_t* wl, 
 // bw x bw tile; each thread owns PPT vertically adjacent pixels, so every
 // staged record read from shared memory is used for PPT pixels.
 // ---------------------------------------------------------------------------
-template <int TEXMODE, int CT, int PPT>
+template <int TEXMODE, int CT, int PPT, int FIX = 0>
 __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, const FwdOut& o, const Recs& R) {
     const int nthr = blockDim.x * blockDim.y;
     const int tr = threadIdx.y * blockDim.x + threadIdx.x;
     const int bw = blockDim.x;
     const unsigned wmask = __activemask();
     const View& V = J.V;
-    const bool use_blur = a.settings & (1 << 9);
-    const bool use_ndc = a.settings & (1 << 10);
-    const bool flip = a.settings & (1 << 15);
-    const bool bilinear = !(a.settings & (1 << 2));
+    // FIX = 1: compiled for the default settings (kFixedFwdMask bits off)
+    const bool use_blur = FIX ? false : (a.settings & (1 << 9)) != 0;
+    const bool use_ndc = FIX ? false : (a.settings & (1 << 10)) != 0;
+    const bool flip = FIX ? false : (a.settings & (1 << 15)) != 0;
+    const bool bilinear = FIX ? true : !(a.settings & (1 << 2));
     // alpha-visualisation mode (texture.cu:58-63, 201-241; settings bit 16,
     // selected at launch as TEXMODE | 2): alpha 0.99 inside
     // sigma <= alpha_bound^2 / 2, outlines within outline_bound pixels of its edge
@@ -468,11 +469,12 @@ struct BwdPix {
 
 // Adjoint of one (pixel, Gaussian) pair; adds its moments to m and returns
 // false when the pair is skipped.  Follows csrc/texture.cu:577-708.
-template <int TEXMODE, int CT, int CA>
+template <int TEXMODE, int CT, int CA, int NM>
 __device__ __forceinline__ void bwd_pair(const SceneArgs& a, const BwdArgs& g, const Recs& R, int k, int gidx,
                                          const RecHot& Hr, const Hit& H, float alpha, float e, float eb, float nbf,
                                          float bf, BwdPix<CA>& S, int C, bool use_ndc, bool prop_uv, bool bilinear,
-                                         float (&m)[kMoments]) {
+                                         float (&m)[NM]) {
+    static_assert(NM == kMoments || NM == kMoments - 2, "all moments, or all but the two blur moments");
     const RecWarm& Wm = R.warm[k];
     const float4 col = Wm.col, nw = Wm.nrm;
     const float is1 = col.w, is2 = nw.w;
@@ -602,8 +604,10 @@ __device__ __forceinline__ void bwd_pair(const SceneArgs& a, const BwdArgs& g, c
     m[18] += H.l2s * v_u;
     m[19] += H.l1s * v_v;
     m[20] += H.l2s * v_v;
-    m[21] += kBlurFsq * v_sb * (Wm.uvs.z - P.px);
-    m[22] += kBlurFsq * v_sb * (Wm.uvs.w - P.py);
+    if constexpr (NM == kMoments) {
+        m[21] += kBlurFsq * v_sb * (Wm.uvs.z - P.px);
+        m[22] += kBlurFsq * v_sb * (Wm.uvs.w - P.py);
+    }
 }
 
 // GS: lanes per splat walk.  32 = the warp walks one candidate list; 16, 8 or
@@ -611,11 +615,15 @@ __device__ __forceinline__ void bwd_pair(const SceneArgs& a, const BwdArgs& g, c
 // thread_pixel) walks its own list, so a warp works on 32 / GS splats at once
 // and a small splat occupies the lanes of the pixels it can reach, not a whole
 // warp.
-template <int TEXMODE, int CT, int PPT, int GS = 32>
+template <int TEXMODE, int CT, int PPT, int GS = 32, int FIX = 0>
 __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, const BwdArgs& g, const Recs& R,
                                          float* smom, uint8_t* lists, uint8_t* touched) {
     static_assert(GS == 32 || GS == 16 || GS == 8 || GS == 4, "group of 32, 16, 8 or 4 lanes");
-    using Red = Ragged<kMoments, GS / 2>;
+    // FIX = 1: compiled for the default settings (kFixedBwdSettings): no
+    // blur (its two moments are dropped), no NDC depth, uv gradients
+    // propagated, bilinear texels
+    constexpr int NM = FIX ? kMoments - 2 : kMoments;
+    using Red = Ragged<NM, GS / 2>;
     const int nthr = blockDim.x * blockDim.y;
     const int tr = threadIdx.y * blockDim.x + threadIdx.x;
     const int bw = blockDim.x;
@@ -631,10 +639,10 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
 #pragma unroll
     for (int q = 0; q < Red::OUT; q++) my_slot[q] = Red::slot(lane, q);
     const View& V = J.V;
-    const bool use_blur = a.settings & (1 << 9);
-    const bool use_ndc = a.settings & (1 << 10);
-    const bool prop_uv = a.settings & (1 << 8);
-    const bool bilinear = !(a.settings & (1 << 2));
+    const bool use_blur = FIX ? false : (a.settings & (1 << 9)) != 0;
+    const bool use_ndc = FIX ? false : (a.settings & (1 << 10)) != 0;
+    const bool prop_uv = FIX ? true : (a.settings & (1 << 8)) != 0;
+    const bool bilinear = FIX ? true : !(a.settings & (1 << 2));
     const int C = CT >= 0 ? CT : a.C;
     constexpr int CA = CT > 0 ? CT : (CT == 0 ? 1 : kMaxChannels);
     const float3 z3 = make_float3(0.f, 0.f, 0.f);
@@ -745,20 +753,20 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
             }
             const unsigned vmask = __ballot_sync(wmask, any);
             if (!vmask) continue;
-            float m[kMoments];
+            float m[NM];
 #pragma unroll
-            for (int q = 0; q < kMoments; q++) m[q] = 0.f;
+            for (int q = 0; q < NM; q++) m[q] = 0.f;
 #pragma unroll
             for (int p = 0; p < PPT; p++)
                 if (valid[p])
-                    bwd_pair<TEXMODE, CT, CA>(a, g, R, k, gidx, Hr, H[p], alpha[p], e[p], eb[p], nbf[p], bf[p], S[p],
-                                              C, use_ndc, prop_uv, bilinear, m);
+                    bwd_pair<TEXMODE, CT, CA, NM>(a, g, R, k, gidx, Hr, H[p], alpha[p], e[p], eb[p], nbf[p], bf[p],
+                                                  S[p], C, use_ndc, prop_uv, bilinear, m);
             float* dst = smom + k * kMomSlot;
             if (GS == 32 && !full_warp) {
                 if (lane == 0) touched[k] = 1;
                 if (any) {
 #pragma unroll
-                    for (int q = 0; q < kMoments; q++) atomicAdd(dst + q, m[q]);
+                    for (int q = 0; q < NM; q++) atomicAdd(dst + q, m[q]);
                 }
             } else {
                 Red::reduce(m, lane);
@@ -766,7 +774,7 @@ __device__ __forceinline__ void bwd_tile(const SceneArgs& a, const TileJob& J, c
                     if ((lane & (GS - 1)) == 0) touched[k] = 1;
 #pragma unroll
                     for (int q = 0; q < Red::OUT; q++)
-                        if (my_slot[q] < kMoments) atomicAdd(dst + my_slot[q], m[q]);
+                        if (my_slot[q] < NM) atomicAdd(dst + my_slot[q], m[q]);
                 }
             }
         }
@@ -1003,17 +1011,17 @@ __device__ __forceinline__ bool next_job(const BatchArgs& ba, int* s_tile, TileJ
     return true;
 }
 
-template <int TEXMODE, int CT, int PPT>
+template <int TEXMODE, int CT, int PPT, int FIX = 0>
 __global__ void FWD_BOUNDS(PPT) fwd_batch_kernel(SceneArgs a, BatchArgs ba, FwdOut o) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_tile;
     TileJob J;
     const int slots = batch_of(a, blockDim.x * blockDim.y);
     const Recs R = Recs::carve(smem, slots, false);
-    while (next_job(ba, &s_tile, J)) fwd_tile<TEXMODE, CT, PPT>(a, J, o, R);
+    while (next_job(ba, &s_tile, J)) fwd_tile<TEXMODE, CT, PPT, FIX>(a, J, o, R);
 }
 
-template <int TEXMODE, int CT, int PPT, int GS>
+template <int TEXMODE, int CT, int PPT, int GS, int FIX = 0>
 __device__ __forceinline__ void bwd_batch_body(const SceneArgs& a, const BatchArgs& ba, const BwdArgs& g) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_tile;
@@ -1024,7 +1032,7 @@ __device__ __forceinline__ void bwd_batch_body(const SceneArgs& a, const BatchAr
     float* smom = reinterpret_cast<float*>(smem + (size_t)(kRecBytes + kEdgeBytes) * slots);
     uint8_t* lists = smem + (size_t)(kRecBytes + kEdgeBytes + kMomSlot * sizeof(float)) * slots;
     uint8_t* touched = lists + ((size_t)ceil_div(nthr, 32) + (GS < 32 ? ceil_div(nthr, GS) : 0)) * slots;
-    while (next_job(ba, &s_tile, J)) bwd_tile<TEXMODE, CT, PPT, GS>(a, J, g, R, smom, lists, touched);
+    while (next_job(ba, &s_tile, J)) bwd_tile<TEXMODE, CT, PPT, GS, FIX>(a, J, g, R, smom, lists, touched);
 }
 
 template <int TEXMODE, int CT, int PPT, int GS>
@@ -1039,10 +1047,11 @@ __global__ void BWD_BOUNDS(PPT) bwd_batch_kernel(SceneArgs a, BatchArgs ba, BwdA
 // and 12 CTAs, at 88 and 80 registers and with fewer Gaussians per batch so
 // that the shared memory fits, spill 144-188 bytes and lose.)
 constexpr int regs_for_ctas(int nb) { return (65536 / (64 * nb)) / 8 * 8; }
-template <int TEXMODE, int CT, int NB>
+// FIX = 1: compiled for the default settings (see bwd_tile).
+template <int TEXMODE, int CT, int NB, int FIX>
 __global__ void __launch_bounds__(64) __maxnreg__(regs_for_ctas(NB))
     bwd_batch64_kernel(SceneArgs a, BatchArgs ba, BwdArgs g) {
-    bwd_batch_body<TEXMODE, CT, 1, 8>(a, ba, g);
+    bwd_batch_body<TEXMODE, CT, 1, 8, FIX>(a, ba, g);
 }
 
 // Writes the 32 records of a warp, assembled in shared memory (src), to
@@ -1355,10 +1364,17 @@ int launch_finalize(const SceneArgs& a, const float* moments, float* v_opac, flo
     return check_launch("finalize");
 }
 
+// The batched forward kernel: compiled for the default settings where they
+// apply (one pixel per thread, bf16 RGB texels), else pick_fwd's.
+static FwdBatch<0, 0, 1>::type pick_fwd_batch(int C, int texmode, int& ppt, int settings) {
+    if (ppt == 1 && C == 3 && texmode == 1 && (settings & kFixedFwdMask) == 0) return fwd_batch_kernel<1, 3, 1, 1>;
+    return pick_fwd<FwdBatch>(C, texmode, ppt, settings);
+}
+
 int launch_fwd_batch(const SceneArgs& a, const BatchArgs& ba, const FwdOut& o, int bw, int texmode, int ppt, int grid,
                      cudaStream_t stream) {
     ppt = ppt_of(bw, ppt);
-    auto k = pick_fwd<FwdBatch>(a.C, texmode, ppt, a.settings);
+    auto k = pick_fwd_batch(a.C, texmode, ppt, a.settings);
     const size_t smem = fwd_smem(bw, ppt, a.batch);
     int rc = set_smem(k, smem, "batch forward");
     if (rc) return rc;
@@ -1370,10 +1386,12 @@ int launch_fwd_batch(const SceneArgs& a, const BatchArgs& ba, const FwdOut& o, i
 // `ctas` resident CTAs per SM where one exists (8x8 tiles, one pixel per
 // thread, 8-lane groups, bf16 texels with 3 channels; ctas 9 or 10), else the
 // general kernel.
-static BwdBatch<0, 0, 1, 32>::type pick_bwd_batch(int bw, int C, int texmode, int ppt, int gs, int ctas) {
+static BwdBatch<0, 0, 1, 32>::type pick_bwd_batch(int bw, int C, int texmode, int ppt, int gs, int ctas,
+                                                   int settings) {
     if (threads_of(bw, ppt) == 64 && ppt == 1 && gs == 8 && C == 3 && texmode == 1) {
-        if (ctas == 9) return bwd_batch64_kernel<1, 3, 9>;
-        if (ctas == 10) return bwd_batch64_kernel<1, 3, 10>;
+        const bool fixed = (settings & kFixedBwdMask) == kFixedBwdSettings;
+        if (ctas == 9) return bwd_batch64_kernel<1, 3, 9, 0>;
+        if (ctas == 10) return fixed ? bwd_batch64_kernel<1, 3, 10, 1> : bwd_batch64_kernel<1, 3, 10, 0>;
     }
     return pick<BwdBatch>(C, texmode, ppt, gs);
 }
@@ -1384,7 +1402,8 @@ template <typename K>
 static int set_bwd_smem(K k, size_t smem, const char* what) {
     int rc = set_smem(k, smem, what);
     if (rc) return rc;
-    if (k == (K)bwd_batch64_kernel<1, 3, 9> || k == (K)bwd_batch64_kernel<1, 3, 10>) {
+    if (k == (K)bwd_batch64_kernel<1, 3, 9, 0> || k == (K)bwd_batch64_kernel<1, 3, 10, 0> ||
+        k == (K)bwd_batch64_kernel<1, 3, 10, 1>) {
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
                                              (int)cudaSharedmemCarveoutMaxShared);
         if (e != cudaSuccess) { set_cuda_error(e, what); return GSTEX_ERR_CUDA; }
@@ -1396,7 +1415,7 @@ int launch_bwd_batch(const SceneArgs& a, const BatchArgs& ba, const BwdArgs& g, 
                      int ctas, int grid, cudaStream_t stream) {
     ppt = ppt_of(bw, ppt);
     gs = gs_of(bw, ppt, a.C, gs);
-    auto k = pick_bwd_batch(bw, a.C, texmode, ppt, gs, ctas);
+    auto k = pick_bwd_batch(bw, a.C, texmode, ppt, gs, ctas, a.settings);
     const size_t smem = bwd_smem(bw, ppt, gs, a.batch);
     int rc = set_bwd_smem(k, smem, "batch backward");
     if (rc) return rc;
@@ -1404,18 +1423,18 @@ int launch_bwd_batch(const SceneArgs& a, const BatchArgs& ba, const BwdArgs& g, 
     return check_launch("batch backward");
 }
 
-int resident_ctas(int bw, bool backward, int texmode, int C, int ppt, int gs, int ctas, int batch) {
+int resident_ctas(int bw, bool backward, int texmode, int C, int ppt, int gs, int ctas, int batch, int settings) {
     int n = 0;
     cudaError_t e;
     ppt = ppt_of(bw, ppt);
     gs = gs_of(bw, ppt, C, gs);
     if (backward) {
-        auto k = pick_bwd_batch(bw, C, texmode, ppt, gs, ctas);
+        auto k = pick_bwd_batch(bw, C, texmode, ppt, gs, ctas, settings);
         const size_t smem = bwd_smem(bw, ppt, gs, batch);
         if (set_bwd_smem(k, smem, "occupancy")) return 0;
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, threads_of(bw, ppt), smem);
     } else {
-        auto k = pick_fwd<FwdBatch>(C, texmode, ppt, 0);
+        auto k = pick_fwd_batch(C, texmode, ppt, settings);
         const size_t smem = fwd_smem(bw, ppt, batch);
         if (set_smem(k, smem, "occupancy")) return 0;
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, threads_of(bw, ppt), smem);

@@ -125,7 +125,17 @@ struct RawGradArgs {
 int launch_finalize(const SceneArgs& a, const float* moments, float* v_opac, float* v_means, float* v_scales,
                     float* v_quats, float* v_uv0, float* v_umap, float* v_vmap, cudaStream_t stream,
                     const RawGradArgs& rg = RawGradArgs{});
-int resident_ctas(int bw, bool backward, int texmode, int C, int ppt, int gs, int ctas = 0, int batch = 0);
+int resident_ctas(int bw, bool backward, int texmode, int C, int ppt, int gs, int ctas = 0, int batch = 0,
+                  int settings = 0);
+// Settings bits the backward reads (bilinear off, uv-gradient propagation,
+// blur, NDC depth) and the value for which kernels compiled for fixed
+// settings exist: uv gradients propagated, everything else off.
+constexpr int kFixedBwdMask = (1 << 2) | (1 << 8) | (1 << 9) | (1 << 10);
+constexpr int kFixedBwdSettings = 1 << 8;
+// Settings bits the forward reads besides the alpha-visualisation mode
+// (bilinear off, blur, NDC depth, flipped normals, alpha visualisation): the
+// kernel compiled for fixed settings applies when all are off.
+constexpr int kFixedFwdMask = (1 << 2) | (1 << 9) | (1 << 10) | (1 << 15) | (1 << 16);
 int launch_records(const SceneArgs& a, const BatchArgs& ba, int num_views, const int32_t* counts, RecAll* recs,
                    int* fix_count, uint32_t* fix, cudaStream_t stream);
 
