@@ -146,6 +146,12 @@ class RawScene:
 
 LOSS_WEIGHTS = dict(img=1.0, texture=1.0, reg=100.0, normal=0.05)
 
+# Settings bits the backward reads (bilinear off, uv-gradient propagation,
+# blur, NDC depth) and the value the kernels compiled for fixed settings
+# serve (the library's kFixedBwdMask / kFixedBwdSettings).
+FIXED_BWD_MASK = (1 << 2) | (1 << 8) | (1 << 9) | (1 << 10)
+FIXED_BWD_SETTINGS = 1 << 8
+
 
 class BatchRenderer:
     """Fixed cameras, fixed scene size; reusable buffers for repeated steps."""
@@ -468,8 +474,9 @@ class BatchRenderer:
     def autotune(self, s: Scene, tgt_img, tgt_tex, reps: int = 2) -> dict:
         """Choose pixels-per-thread and Gaussians per batch (64, 128 or one per
         thread) of the forward kernel, and pixels-per-thread, lanes per splat
-        walk (32, 16, 8, 4) and Gaussians per batch of the backward kernel, by
-        timing each candidate on this scene and these cameras (CUDA events).
+        walk (32, 16, 8, 4), the resident-CTA variant and Gaussians per batch
+        (48, 64, 128 or one per thread) of the backward kernel, by timing each
+        candidate on this scene and these cameras (CUDA events).
         The tile width is fixed per renderer (it sets the binning): to tune
         it, build a renderer per block_width and time whole steps."""
         stream = torch.cuda.current_stream(self.dev)
@@ -503,30 +510,26 @@ class BatchRenderer:
         self.forward(s)
         self.image_loss(tgt_img, tgt_tex)
         best = None
-        for ppt, gs in ((1, 32), (2, 32), (1, 16), (1, 8), (1, 4)):
-            self.bwd_ppt, self.bwd_group, self.bwd_batch = ppt, gs, 0
+        cands = [(1, 32, 0), (2, 32, 0), (1, 16, 0), (1, 8, 0), (1, 4, 0)]
+        # 8x8 tiles with bf16 RGB texels: kernels compiled for 10 resident
+        # CTAs per SM (96 registers instead of 124, more warps)
+        if self.bw == 8 and self.C == 3 and self.texmode == 1:
+            cands += [(1, 8, 10)]
+            if (self.settings & FIXED_BWD_MASK) == FIXED_BWD_SETTINGS:
+                cands += [(1, 32, 10)]
+        for ppt, gs, ctas in cands:
+            self.bwd_ppt, self.bwd_group, self.bwd_ctas, self.bwd_batch = ppt, gs, ctas, 0
             ms = timed(lambda: self.backward(s))
-            result[f"backward_ppt{ppt}_g{gs}_ms"] = ms
-            best = (ms, ppt, gs, 0) if best is None or ms < best[0] else best
-        for nb in (64, 128):
+            result[f"backward_ppt{ppt}_g{gs}" + (f"_ctas{ctas}" if ctas else "") + "_ms"] = ms
+            best = (ms, ppt, gs, ctas, 0) if best is None or ms < best[0] else best
+        for nb in (48, 64, 128):
             if nb >= self.bw * self.bw // best[1]:
                 continue  # not below one Gaussian per thread
-            self.bwd_ppt, self.bwd_group, self.bwd_batch = best[1], best[2], nb
+            self.bwd_ppt, self.bwd_group, self.bwd_ctas, self.bwd_batch = best[1], best[2], best[3], nb
             ms = timed(lambda: self.backward(s))
-            result[f"backward_ppt{best[1]}_g{best[2]}_batch{nb}_ms"] = ms
-            best = (ms, best[1], best[2], nb) if ms < best[0] else best
-        self.bwd_ppt, self.bwd_group, self.bwd_batch = best[1], best[2], best[3]
-        # 8x8 tiles with 8-lane groups and bf16 RGB texels: kernels compiled
-        # for 9 or 10 resident CTAs per SM (fewer registers, more warps)
-        self.bwd_ctas = 0
-        if self.bw == 8 and self.bwd_ppt == 1 and self.bwd_group == 8 and self.C == 3 and self.texmode == 1:
-            best_c = (best[0], 0, self.bwd_batch)
-            for ctas, nb in ((9, 0), (10, 0), (10, 48)):
-                self.bwd_ctas, self.bwd_batch = ctas, nb
-                ms = timed(lambda: self.backward(s))
-                result[f"backward_ppt1_g8_ctas{ctas}_batch{nb or 'threads'}_ms"] = ms
-                best_c = (ms, ctas, nb) if ms < best_c[0] else best_c
-            self.bwd_ctas, self.bwd_batch = best_c[1], best_c[2]
+            result[f"backward_ppt{best[1]}_g{best[2]}" + (f"_ctas{best[3]}" if best[3] else "") + f"_batch{nb}_ms"] = ms
+            best = (ms, best[1], best[2], best[3], nb) if ms < best[0] else best
+        self.bwd_ppt, self.bwd_group, self.bwd_ctas, self.bwd_batch = best[1], best[2], best[3], best[4]
         result.update(fwd_ppt=self.fwd_ppt, fwd_batch=self.fwd_batch or "threads", bwd_ppt=self.bwd_ppt,
                       bwd_group=self.bwd_group, bwd_batch=self.bwd_batch or "threads",
                       bwd_ctas=self.bwd_ctas or "default")

@@ -1040,18 +1040,19 @@ __global__ void BWD_BOUNDS(PPT) bwd_batch_kernel(SceneArgs a, BatchArgs ba, BwdA
     bwd_batch_body<TEXMODE, CT, PPT, GS>(a, ba, g);
 }
 
-// 8x8 tiles (64 threads, one pixel each) with 8-lane groups, compiled for
+// 8x8 tiles (64 threads, one pixel each) with GS-lane groups, compiled for
 // NB resident CTAs per SM: at most 65536 / (64 NB) registers per thread
-// rounded down to a multiple of 8 (112 for 9 CTAs, 96 for 10; the general
-// kernel uses 124, which allows 8), in exchange for more warps per SM.  (11
-// and 12 CTAs, at 88 and 80 registers and with fewer Gaussians per batch so
-// that the shared memory fits, spill 144-188 bytes and lose.)
+// rounded down to a multiple of 8 (96 for 10 CTAs; the general kernel uses
+// 124, which allows 8), in exchange for more warps per SM.  (9 CTAs at 112
+// registers measured between the two; 11 and 12 CTAs, at 88 and 80 registers
+// and with fewer Gaussians per batch so that the shared memory fits, spill
+// 130-190 bytes and lose.)
 constexpr int regs_for_ctas(int nb) { return (65536 / (64 * nb)) / 8 * 8; }
 // FIX = 1: compiled for the default settings (see bwd_tile).
-template <int TEXMODE, int CT, int NB, int FIX>
+template <int TEXMODE, int CT, int NB, int FIX, int GS>
 __global__ void __launch_bounds__(64) __maxnreg__(regs_for_ctas(NB))
     bwd_batch64_kernel(SceneArgs a, BatchArgs ba, BwdArgs g) {
-    bwd_batch_body<TEXMODE, CT, 1, 8, FIX>(a, ba, g);
+    bwd_batch_body<TEXMODE, CT, 1, GS, FIX>(a, ba, g);
 }
 
 // Writes the 32 records of a warp, assembled in shared memory (src), to
@@ -1384,14 +1385,14 @@ int launch_fwd_batch(const SceneArgs& a, const BatchArgs& ba, const FwdOut& o, i
 
 // The backward kernel of a launch: the 64-thread variant compiled for
 // `ctas` resident CTAs per SM where one exists (8x8 tiles, one pixel per
-// thread, 8-lane groups, bf16 texels with 3 channels; ctas 9 or 10), else the
-// general kernel.
+// thread, bf16 texels with 3 channels, ctas 10; 8-lane groups, or 32 with the
+// default settings), else the general kernel.
 static BwdBatch<0, 0, 1, 32>::type pick_bwd_batch(int bw, int C, int texmode, int ppt, int gs, int ctas,
                                                    int settings) {
-    if (threads_of(bw, ppt) == 64 && ppt == 1 && gs == 8 && C == 3 && texmode == 1) {
+    if (threads_of(bw, ppt) == 64 && ppt == 1 && C == 3 && texmode == 1 && ctas == 10) {
         const bool fixed = (settings & kFixedBwdMask) == kFixedBwdSettings;
-        if (ctas == 9) return bwd_batch64_kernel<1, 3, 9, 0>;
-        if (ctas == 10) return fixed ? bwd_batch64_kernel<1, 3, 10, 1> : bwd_batch64_kernel<1, 3, 10, 0>;
+        if (gs == 8) return fixed ? bwd_batch64_kernel<1, 3, 10, 1, 8> : bwd_batch64_kernel<1, 3, 10, 0, 8>;
+        if (gs == 32 && fixed) return bwd_batch64_kernel<1, 3, 10, 1, 32>;
     }
     return pick<BwdBatch>(C, texmode, ppt, gs);
 }
@@ -1402,8 +1403,8 @@ template <typename K>
 static int set_bwd_smem(K k, size_t smem, const char* what) {
     int rc = set_smem(k, smem, what);
     if (rc) return rc;
-    if (k == (K)bwd_batch64_kernel<1, 3, 9, 0> || k == (K)bwd_batch64_kernel<1, 3, 10, 0> ||
-        k == (K)bwd_batch64_kernel<1, 3, 10, 1>) {
+    if (k == (K)bwd_batch64_kernel<1, 3, 10, 0, 8> || k == (K)bwd_batch64_kernel<1, 3, 10, 1, 8> ||
+        k == (K)bwd_batch64_kernel<1, 3, 10, 1, 32>) {
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
                                              (int)cudaSharedmemCarveoutMaxShared);
         if (e != cudaSuccess) { set_cuda_error(e, what); return GSTEX_ERR_CUDA; }

@@ -390,10 +390,10 @@ typedef struct gstex_batch_inputs {
     int group_lanes;                    /* backward: lanes per splat walk (see gstex_raster_inputs) */
     int batch_size;                     /* Gaussians a tile stages per round, 1..threads per CTA;
                                            0 = one per thread (the reference's bw^2) */
-    int resident_ctas;                  /* backward, 8x8 tiles with 8-lane groups and bf16 RGB texels:
-                                           9 or 10 selects a kernel compiled for that many CTAs per SM
-                                           (112 / 96 registers per thread instead of 124); other values:
-                                           the general kernel */
+    int resident_ctas;                  /* backward, 8x8 tiles with bf16 RGB texels and 8-lane groups (or
+                                           32 at the default settings): 10 selects a kernel compiled for
+                                           10 CTAs per SM (96 registers per thread instead of 124); other
+                                           values: the general kernel */
 } gstex_batch_inputs;
 
 /* Bytes of the per-(view, Gaussian) splat records of gstex_batch_records

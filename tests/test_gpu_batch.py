@@ -350,10 +350,10 @@ def _bf16_case():
 
 
 def test_backward_occupancy_variants_match_general_kernel():
-    """8x8 tiles, 8-lane groups, bf16 texels: the backward kernels compiled
-    for 9 and 10 resident CTAs per SM (fewer registers; 10 also with 48
-    Gaussians per batch) give the general kernel's gradients up to the order
-    of the global atomics."""
+    """8x8 tiles, bf16 texels: the backward kernels compiled for 10 resident
+    CTAs per SM (fewer registers; 8-lane groups, also with 48 Gaussians per
+    batch, and the 32-lane walk) give the general kernel's gradients up to
+    the order of the global atomics."""
     from gstex_cuda_gb300 import batch as B, synthetic
     g = torch.Generator().manual_seed(23)
     cams = synthetic.sphere_cameras(g, 3, radius=8.0, resolutions=[(96, 64), (80, 80), (128, 72)])
@@ -371,13 +371,14 @@ def test_backward_occupancy_variants_match_general_kernel():
     tgt_img = torch.rand(P, 3, generator=gen).to(DEV)
     tgt_tex = torch.rand(P, 3, generator=gen).to(DEV)
     res = {}
-    cases = ((0, 0), (9, 0), (10, 0), (10, 48))
-    for ctas, nb in cases:
+    cases = ((0, 0, 8), (10, 0, 8), (10, 48, 8), (10, 0, 32))
+    for case in cases:
+        ctas, nb, gs = case
         r = B.BatchRenderer(bcams, spec.num_points, texture_dtype=torch.bfloat16, capacity=1 << 20, block_width=8,
-                            bwd_group=8, bwd_ctas=ctas, bwd_batch=nb)
+                            bwd_group=gs, bwd_ctas=ctas, bwd_batch=nb)
         loss = float(r.step(scene, tgt_img, tgt_tex).item())
         torch.cuda.synchronize()
-        res[(ctas, nb)] = (loss, {k: v.cpu().numpy().copy() for k, v in r.grads.items()})
+        res[case] = (loss, {k: v.cpu().numpy().copy() for k, v in r.grads.items()})
     base = res[cases[0]]
     for case in cases[1:]:
         assert abs(res[case][0] - base[0]) <= 1e-5 * abs(base[0])  # the loss sums by atomics
