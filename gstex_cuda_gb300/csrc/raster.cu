@@ -1040,15 +1040,17 @@ __global__ void BWD_BOUNDS(PPT) bwd_batch_kernel(SceneArgs a, BatchArgs ba, BwdA
     bwd_batch_body<TEXMODE, CT, PPT, GS>(a, ba, g);
 }
 
+// Registers per thread that let NB CTAs of 64 threads reside on one SM.
+constexpr int regs_for_ctas(int nb) { return (65536 / (64 * nb)) / 8 * 8; }
+
 // 8x8 tiles (64 threads, one pixel each) with GS-lane groups, compiled for
 // NB resident CTAs per SM: at most 65536 / (64 NB) registers per thread
 // rounded down to a multiple of 8 (96 for 10 CTAs; the general kernel uses
 // 124, which allows 8), in exchange for more warps per SM.  (9 CTAs at 112
 // registers measured between the two; 11 and 12 CTAs, at 88 and 80 registers
 // and with fewer Gaussians per batch so that the shared memory fits, spill
-// 130-190 bytes and lose.)
-constexpr int regs_for_ctas(int nb) { return (65536 / (64 * nb)) / 8 * 8; }
-// FIX = 1: compiled for the default settings (see bwd_tile).
+// 130-190 bytes and lose.)  FIX = 1: compiled for the default settings (see
+// bwd_tile).
 template <int TEXMODE, int CT, int NB, int FIX, int GS>
 __global__ void __launch_bounds__(64) __maxnreg__(regs_for_ctas(NB))
     bwd_batch64_kernel(SceneArgs a, BatchArgs ba, BwdArgs g) {
@@ -1367,6 +1369,8 @@ int launch_finalize(const SceneArgs& a, const float* moments, float* v_opac, flo
 
 // The batched forward kernel: compiled for the default settings where they
 // apply (one pixel per thread, bf16 RGB texels), else pick_fwd's.
+// (Kernels of 8x8 tiles compiled for 12, 14, 18 or 20 CTAs per SM, i.e. 80,
+// 72, 56 or 48 registers instead of 64 at 16, all measured slower.)
 static FwdBatch<0, 0, 1>::type pick_fwd_batch(int C, int texmode, int& ppt, int settings) {
     if (ppt == 1 && C == 3 && texmode == 1 && (settings & kFixedFwdMask) == 0) return fwd_batch_kernel<1, 3, 1, 1>;
     return pick_fwd<FwdBatch>(C, texmode, ppt, settings);
