@@ -66,7 +66,7 @@ _BATCH_SIGS = {
     "gstex_sort_pairs32": (_I, [_I, _P, _I, _P, _P, _P, _P, _P, ctypes.c_size_t, _P]),
     "gstex_get_tile_bin_edges32_dyn": (_I, [_I, _P, _P, _I, _I, _P, _P]),
     "gstex_batch_tile_order_workspace_bytes": (ctypes.c_size_t, [_I]),
-    "gstex_batch_tile_order": (_I, [_I, _P, _P, _P, ctypes.c_size_t, _P]),
+    "gstex_batch_tile_order": (_I, [_I, _P, _P, _P, _I, _P, _P, ctypes.c_size_t, _P]),
     "gstex_batch_emit": (_I, [_I, _I, _P, _P, _P, _F, _P, _I, _P, _P, _LL, _P, _P, _P, _P, _P]),
     "gstex_sort_pairs_dyn": (_I, [_I, _P, _I, _P, _P, _P, _P, _P, ctypes.c_size_t, _P]),
     "gstex_get_tile_bin_edges_dyn": (_I, [_I, _P, _P, _I, _P, _P]),
@@ -161,7 +161,7 @@ class BatchRenderer:
                  device="cuda:0", grid: int = 0, loss_weights: Optional[dict] = None, fwd_ppt: int = 1,
                  bwd_ppt: int = 1, bwd_group: int = 8, fwd_batch: int = 0, bwd_batch: int = 0,
                  bwd_ctas: int = 0,
-                 prebuilt_records: bool = True, heavy_first: bool = True):
+                 prebuilt_records: bool = True, heavy_first: bool = True, order_group: int = 4):
         self.dev = torch.device(device)
         self.N = int(num_points)
         self.V = len(cameras)
@@ -174,6 +174,7 @@ class BatchRenderer:
         self.bwd_group = int(bwd_group)
         self.fwd_batch, self.bwd_batch = int(fwd_batch), int(bwd_batch)
         self.bwd_ctas = int(bwd_ctas)
+        self.order_group = int(order_group)  # heaviest-first groups of order_group^2 tiles (forward)
         self.lw = dict(LOSS_WEIGHTS if loss_weights is None else loss_weights)
         L = _L()
         descs = (ViewDesc * self.V)()
@@ -360,7 +361,8 @@ class BatchRenderer:
         check(L.gstex_get_tile_bin_edges32_dyn(self.capacity, ptr(self.count), ptr(self.keys_sorted), 1,
                                                self.total_tiles, ptr(self.bins), st), "tile_bin_edges32_dyn")
         if self.tile_order is not None:
-            check(L.gstex_batch_tile_order(self.total_tiles, ptr(self.bins), ptr(self.tile_order), ptr(self.order_ws),
+            check(L.gstex_batch_tile_order(self.total_tiles, ptr(self.bins), ptr(self.tile_view), ptr(self.views_dev),
+                                           self.order_group, ptr(self.tile_order), ptr(self.order_ws),
                                            self.order_ws.numel(), st), "batch_tile_order")
         if self.records is not None:
             main.wait_event(self.ev_join)

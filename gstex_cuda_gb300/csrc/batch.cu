@@ -188,16 +188,43 @@ __global__ void batch_emit_sorted_kernel(int VN, int N, const BatchView* __restr
     }
 }
 
-// Queue order of the forward: tiles by decreasing intersection count (ties in
-// tile order), so the heaviest tiles do not start last and leave the end of
-// the persistent launch to a few CTAs.
-__global__ void tile_cost_keys_kernel(int T, const int2* __restrict__ bins, uint32_t* __restrict__ keys,
-                                      int32_t* __restrict__ ids) {
+// Queue order of the forward: groups of G x G neighbouring tiles of a view by
+// decreasing intersection count of the group (ties in tile order), the tiles
+// of a group back to back in tile order.  The heaviest work does not start
+// last and leave the end of the persistent launch to a few CTAs, and the
+// tiles of a group, which share most of their splats, run close together in
+// time (their records are still in L2).  First pass: the key of a tile is its
+// group (the global index of the group's first tile) and the group's cost is
+// kept; a stable sort by group, then one by decreasing cost, gives the order.
+__global__ void tile_group_keys_kernel(int T, const int2* __restrict__ bins, const int32_t* __restrict__ tile_view,
+                                       const BatchView* __restrict__ views, int G, uint32_t* __restrict__ group_key,
+                                       int32_t* __restrict__ ids, uint32_t* __restrict__ cost_key) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= T) return;
-    const int2 b = bins[t];
-    keys[t] = ~(uint32_t)max(b.y - b.x, 0);
     ids[t] = t;
+    if (G <= 1) {
+        const int2 b = bins[t];
+        group_key[t] = (uint32_t)t;
+        cost_key[t] = ~(uint32_t)max(b.y - b.x, 0);
+        return;
+    }
+    const BatchView& bv = views[tile_view[t]];
+    const int local = t - bv.tile_offset;
+    const int gx = local % bv.tiles_x / G * G, gy = local / bv.tiles_x / G * G;
+    group_key[t] = (uint32_t)(bv.tile_offset + gy * bv.tiles_x + gx);
+    uint32_t c = 0;
+    for (int dy = 0; dy < G && gy + dy < bv.tiles_y; dy++)
+        for (int dx = 0; dx < G && gx + dx < bv.tiles_x; dx++) {
+            const int2 b = bins[bv.tile_offset + (gy + dy) * bv.tiles_x + gx + dx];
+            c += (uint32_t)max(b.y - b.x, 0);
+        }
+    cost_key[t] = ~c;
+}
+
+__global__ void gather_keys_kernel(int T, const int32_t* __restrict__ ids, const uint32_t* __restrict__ key,
+                                   uint32_t* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < T) out[i] = key[ids[i]];
 }
 
 // ---------------------------------------------------------------------------
@@ -443,26 +470,43 @@ static size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 
 extern "C" size_t gstex_batch_tile_order_workspace_bytes(int total_tiles) {
     const int n = total_tiles > 0 ? total_tiles : 1;
-    return 3 * align256((size_t)n * 4) + gstex_sort32_workspace_bytes(n);
+    return 6 * align256((size_t)n * 4) + gstex_sort32_workspace_bytes(n);
 }
 
-extern "C" int gstex_batch_tile_order(int total_tiles, const int32_t* tile_bins, int32_t* order, void* workspace,
+extern "C" int gstex_batch_tile_order(int total_tiles, const int32_t* tile_bins, const int32_t* tile_view,
+                                      const void* views_dev, int group, int32_t* order, void* workspace,
                                       size_t workspace_bytes, gstex_stream_t s) {
-    GSTEX_REQUIRE(total_tiles >= 0);
+    GSTEX_REQUIRE(total_tiles >= 0 && group >= 1 && group <= 64);
     if (total_tiles == 0) return GSTEX_OK;
     GSTEX_REQUIRE(tile_bins && order && workspace && ((uintptr_t)workspace & 15) == 0);
+    if (group > 1) GSTEX_REQUIRE(tile_view && views_dev);
     if (workspace_bytes < gstex_batch_tile_order_workspace_bytes(total_tiles)) return GSTEX_ERR_CAPACITY;
     const size_t a = align256((size_t)total_tiles * 4);
     unsigned char* w = (unsigned char*)workspace;
-    uint32_t* keys = (uint32_t*)w;
+    uint32_t* group_key = (uint32_t*)w;
     int32_t* ids = (int32_t*)(w + a);
-    uint32_t* keys_sorted = (uint32_t*)(w + 2 * a);
-    tile_cost_keys_kernel<<<ceil_div(total_tiles, 256), 256, 0, (cudaStream_t)s>>>(total_tiles, (const int2*)tile_bins,
-                                                                                   keys, ids);
+    uint32_t* cost_key = (uint32_t*)(w + 2 * a);
+    uint32_t* keys_sorted = (uint32_t*)(w + 3 * a);
+    int32_t* by_group = (int32_t*)(w + 4 * a);
+    uint32_t* cost_in = (uint32_t*)(w + 5 * a);
+    unsigned char* sort_ws = w + 6 * a;
+    const size_t sort_bytes = workspace_bytes - 6 * a;
+    cudaStream_t st = (cudaStream_t)s;
+    const int blocks = ceil_div(total_tiles, 256);
+    tile_group_keys_kernel<<<blocks, 256, 0, st>>>(total_tiles, (const int2*)tile_bins, tile_view,
+                                                   (const BatchView*)views_dev, group, group_key, ids, cost_key);
     int rc = check_launch("batch_tile_order");
     if (rc) return rc;
-    return gstex_sort_pairs32(total_tiles, nullptr, 32, keys, ids, keys_sorted, order, w + 3 * a,
-                              workspace_bytes - 3 * a, s);
+    if (group == 1)  // tiles are already in tile order
+        return gstex_sort_pairs32(total_tiles, nullptr, 32, cost_key, ids, keys_sorted, order, sort_ws, sort_bytes, s);
+    int bits = 1;
+    while (bits < 31 && (1u << bits) < (uint32_t)total_tiles) bits++;
+    rc = gstex_sort_pairs32(total_tiles, nullptr, bits, group_key, ids, keys_sorted, by_group, sort_ws, sort_bytes, s);
+    if (rc) return rc;
+    gather_keys_kernel<<<blocks, 256, 0, st>>>(total_tiles, by_group, cost_key, cost_in);
+    rc = check_launch("batch_tile_order");
+    if (rc) return rc;
+    return gstex_sort_pairs32(total_tiles, nullptr, 32, cost_in, by_group, keys_sorted, order, sort_ws, sort_bytes, s);
 }
 
 extern "C" int gstex_batch_gather_counts(int n, const int32_t* order, const int32_t* counts, int32_t* out,

@@ -352,13 +352,17 @@ int gstex_batch_emit_sorted(int num_points, int num_views, const void* views_dev
                             uint32_t* keys, int32_t* gaussian_ids, int64_t* count, int* overflow,
                             gstex_stream_t stream);
 
-/* Queue order of the global tiles by decreasing intersection count (ties in
- * tile order) from tile_bins [total_tiles, 2]; pass it as in->tile_order to
- * gstex_batch_forward so the heaviest tiles start first.  (The backward is
- * faster in tile order: neighbouring tiles share splats in L2.)  Workspace:
+/* Queue order of the global tiles for gstex_batch_forward (in->tile_order)
+ * from tile_bins [total_tiles, 2]: groups of group x group neighbouring
+ * tiles of a view (tile_view / views_dev from gstex_batch_prepare; unused for
+ * group 1) by decreasing intersection count of the group, ties in tile order,
+ * the tiles of a group back to back in tile order.  The heaviest work starts
+ * first, and the tiles of a group, which share most of their splats, run
+ * close together.  (The backward is faster in plain tile order.)  Workspace:
  * gstex_batch_tile_order_workspace_bytes(total_tiles), 16-byte aligned. */
 size_t gstex_batch_tile_order_workspace_bytes(int total_tiles);
-int gstex_batch_tile_order(int total_tiles, const int32_t* tile_bins, int32_t* order, void* workspace,
+int gstex_batch_tile_order(int total_tiles, const int32_t* tile_bins, const int32_t* tile_view,
+                           const void* views_dev, int group, int32_t* order, void* workspace,
                            size_t workspace_bytes, gstex_stream_t stream);
 
 typedef struct gstex_batch_inputs {

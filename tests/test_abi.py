@@ -108,7 +108,7 @@ def test_batch_layout_and_workspace_sizes_on_host():
     assert L.gstex_batch_records_bytes(1000, 4) == 1000 * 4 * 224
     assert L.gstex_sort32_workspace_bytes(1 << 20) >= (1 << 20) * 8
     assert L.gstex_sort_workspace_bytes(1 << 20) >= (1 << 20) * 12
-    assert L.gstex_batch_tile_order_workspace_bytes(96464) >= 96464 * 12 + L.gstex_sort32_workspace_bytes(96464)
+    assert L.gstex_batch_tile_order_workspace_bytes(96464) >= 96464 * 24 + L.gstex_sort32_workspace_bytes(96464)
 
 
 def test_static_scratch_sort_rejects_bad_arguments_without_gpu():

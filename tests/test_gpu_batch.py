@@ -235,8 +235,9 @@ def test_plain_per_view_step_matches_batched_step(setup):
 
 
 def test_forward_tile_order_does_not_change_outputs(setup):
-    """The forward's heaviest-first queue order changes which CTA renders a
-    tile, not what it renders: outputs are bit-identical to tile order."""
+    """The forward's heaviest-first queue order (groups of 4 x 4 tiles)
+    changes which CTA renders a tile, not what it renders: outputs are
+    bit-identical to tile order."""
     from gstex_cuda_gb300 import batch as B
     spec, cams, r, scene, _ = setup
     bcams = [B.Camera(c.viewmat, c.fx, c.fy, c.cx, c.cy, c.width, c.height) for c in cams]
@@ -250,9 +251,37 @@ def test_forward_tile_order_does_not_change_outputs(setup):
     torch.cuda.synchronize()
     order = r.tile_order.cpu().numpy()
     cost = (r.bins[:, 1] - r.bins[:, 0]).cpu().numpy()
-    assert np.array_equal(np.sort(order), np.arange(r.total_tiles)) and np.all(np.diff(cost[order]) <= 0)
+    assert np.array_equal(np.sort(order), np.arange(r.total_tiles))
+    # groups of G x G tiles of a view: heaviest group first, a group's tiles
+    # back to back in tile order
+    G, bw = r.order_group, r.bw
+    group = np.empty(r.total_tiles, np.int64)
+    off = 0
+    for cam in cams:
+        tx, ty = (cam.width + bw - 1) // bw, (cam.height + bw - 1) // bw
+        local = np.arange(tx * ty)
+        group[off:off + tx * ty] = off + (local // tx // G * G) * tx + (local % tx // G * G)
+        off += tx * ty
+    gcost = np.bincount(group, weights=cost, minlength=r.total_tiles)
+    seq = group[order]
+    starts = np.flatnonzero(np.r_[True, seq[1:] != seq[:-1]])
+    assert len(starts) == len(np.unique(group)), "a group's tiles are contiguous in the order"
+    assert np.all(np.diff(gcost[seq[starts]]) <= 0)
+    for a, b in zip(starts, np.r_[starts[1:], len(order)]):
+        assert np.all(np.diff(order[a:b]) > 0)
+    # groups of one tile: tiles by decreasing cost, ties in tile order
+    r3 = B.BatchRenderer(bcams, spec.num_points, capacity=1 << 20, block_width=r.bw, fwd_ppt=r.fwd_ppt,
+                         bwd_ppt=r.bwd_ppt, bwd_group=r.bwd_group, order_group=1)
+    r3.bin(scene)
+    r3.forward(scene)
+    torch.cuda.synchronize()
+    o3 = r3.tile_order.cpu().numpy()
+    assert np.array_equal(np.sort(o3), np.arange(r.total_tiles)) and np.all(np.diff(cost[o3]) <= 0)
+    ties = np.diff(cost[o3]) == 0
+    assert np.all(np.diff(o3)[ties] > 0)
     for k in ("img", "depth", "reg", "texture", "normal", "final_T", "final_idx", "depth_idx", "reg_s"):
         assert np.array_equal(r.out[k].cpu().numpy(), r2.out[k].cpu().numpy()), k
+        assert np.array_equal(r3.out[k].cpu().numpy(), r2.out[k].cpu().numpy()), k
 
 
 @pytest.mark.parametrize("fwd_batch,bwd_batch", [(64, 128), (128, 64), (32, 32)])
