@@ -125,29 +125,43 @@ __device__ __forceinline__ void resolve_count(const int64_t* n_dev, int& n, int&
     }
 }
 
+// Per-block digit counts: each warp loads its kSortItems keys per thread of a
+// 2048-item tile up front (so the loads overlap) and counts them in its own
+// shared-memory histogram with plain atomics; the warps' histograms are summed
+// at the end.
 template <typename K>
 __global__ void __launch_bounds__(kSortThreads) radix_hist_kernel(const K* __restrict__ keys, int n, int chunk,
                                                                   const int64_t* __restrict__ n_dev, int shift,
                                                                   uint32_t* __restrict__ hist) {
-    __shared__ uint32_t h[kRadix];
-    for (int i = threadIdx.x; i < kRadix; i += blockDim.x) h[i] = 0;
+    __shared__ uint32_t h[kSortWarps][kRadix];
+    for (int i = threadIdx.x; i < kSortWarps * kRadix; i += blockDim.x) (&h[0][0])[i] = 0;
     resolve_count(n_dev, n, chunk);
     __syncthreads();
     const int start = blockIdx.x * chunk;
     const int end = min(start + chunk, n);
-    const unsigned lane = threadIdx.x & 31;
-    for (int base = start; base < end; base += blockDim.x) {
-        const int i = base + threadIdx.x;
-        const bool valid = i < end;
-        const unsigned mask = __ballot_sync(0xffffffffu, valid);
-        if (valid) {
-            const unsigned d = (unsigned)(keys[i] >> shift) & (kRadix - 1);
-            const unsigned peers = __match_any_sync(mask, d);
-            if (lane == (unsigned)(__ffs(peers) - 1)) atomicAdd(&h[d], (uint32_t)__popc(peers));
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    uint32_t* hw = h[warp];
+    for (int tbase = start; tbase < end; tbase += kSortTile) {
+        K key[kSortItems];
+#pragma unroll
+        for (int k = 0; k < kSortItems; k++) {
+            const int i = tbase + warp * (32 * kSortItems) + k * 32 + lane;
+            key[k] = i < end ? keys[i] : K(0);
+        }
+#pragma unroll
+        for (int k = 0; k < kSortItems; k++) {
+            const int i = tbase + warp * (32 * kSortItems) + k * 32 + lane;
+            if (i < end) atomicAdd(&hw[(unsigned)(key[k] >> shift) & (kRadix - 1)], 1u);
         }
     }
     __syncthreads();
-    for (int d = threadIdx.x; d < kRadix; d += blockDim.x) hist[(size_t)d * gridDim.x + blockIdx.x] = h[d];
+    for (int d = threadIdx.x; d < kRadix; d += blockDim.x) {
+        uint32_t c = 0;
+#pragma unroll
+        for (int w = 0; w < kSortWarps; w++) c += h[w][d];
+        hist[(size_t)d * gridDim.x + blockIdx.x] = c;
+    }
 }
 
 // Block-wide exclusive scan of one value per thread (blockDim.x == kSortThreads);
@@ -228,6 +242,13 @@ __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
         K key[kSortItems];
         uint32_t val[kSortItems];
         uint32_t rank[kSortItems];
+        // all loads first, so that they overlap
+#pragma unroll
+        for (int k = 0; k < kSortItems; k++) {
+            const int i = tbase + warp * (32 * kSortItems) + k * 32 + (int)lane;
+            key[k] = i < end ? kin[i] : K(0);
+            val[k] = i < end ? vin[i] : 0u;
+        }
 #pragma unroll
         for (int k = 0; k < kSortItems; k++) {
             const int i = tbase + warp * (32 * kSortItems) + k * 32 + (int)lane;
@@ -235,8 +256,6 @@ __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
             const unsigned mask = __ballot_sync(0xffffffffu, valid);
             uint32_t d = 0, before = 0, peers = 0;
             if (valid) {
-                key[k] = kin[i];
-                val[k] = vin[i];
                 d = (uint32_t)(key[k] >> shift) & (kRadix - 1);
                 peers = __match_any_sync(mask, d);
                 before = wcnt[warp][d];
