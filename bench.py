@@ -462,21 +462,26 @@ def main():
     log(f"graph: {graph_fps}")
 
     # end to end through the public API with host inputs: pinned host copies of
-    # every scene input are uploaded each step, the loss is read back
+    # every scene input are uploaded each step (HostInputStepper: the next
+    # step's upload overlaps the current step's compute), the loss is read back
+    # every step
     e2e = None
     if not args.no_e2e:
-        host = {k: getattr(scene, k).cpu().pin_memory() for k in
-                ("means", "scales", "quats", "opacity", "sh_coeffs", "uv0", "umap", "vmap", "texture_dims", "texture")}
-        h2d = sum(t.numel() * t.element_size() for t in host.values())
+        names = ("means", "scales", "quats", "opacity", "sh_coeffs", "uv0", "umap", "vmap", "texture_dims", "texture")
+        host = B.Scene(**{**scene.__dict__, **{k: getattr(scene, k).cpu().pin_memory() for k in names}})
+        h2d = sum(getattr(host, k).numel() * getattr(host, k).element_size() for k in names)
+        stepper = B.HostInputStepper(r, like=scene)
+        stepper.upload(host)
+        float(stepper.step(tgt_img, tgt_tex).item())  # warm-up of the second buffer's first use
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
-        for _ in range(args.steps):
-            for k, t in host.items():
-                getattr(scene, k).copy_(t, non_blocking=True)
-            loss = r.step(scene, tgt_img, tgt_tex)
+        stepper.upload(host)
+        for k in range(args.steps):
+            loss = stepper.step(tgt_img, tgt_tex, next_host=host if k + 1 < args.steps else None)
             float(loss.item())
         torch.cuda.synchronize(dev)
         el = time.perf_counter() - t0
+        del stepper
         e2e = {"value": world * nviews * args.steps / el, "unit": "frames/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": 4}
         log(f"e2e: {e2e}")

@@ -581,6 +581,69 @@ class BatchRenderer:
         return t.reshape(H, W, *t.shape[1:])
 
 
+_SCENE_TENSORS = ("means", "scales", "quats", "opacity", "sh_coeffs", "uv0", "umap", "vmap", "texture_dims",
+                  "texture")
+
+
+class HostInputStepper:
+    """Steps of a BatchRenderer whose scene tensors come from host memory each
+    step (a trainer that keeps its parameters on the host, or streams scenes).
+
+    Two device copies of the scene alternate: while step k computes on one,
+    the inputs of step k + 1 are uploaded into the other on a copy stream, so
+    the host-to-device copies overlap the compositor instead of preceding it.
+    Host tensors should be pinned for the copies to run asynchronously, and
+    must not change until the step that uploads them has been issued and the
+    device synchronised or the next step's loss read.
+
+        stepper = HostInputStepper(renderer, like=device_scene)
+        stepper.upload(host_scene)                        # inputs of the first step
+        for k in range(steps):
+            loss = stepper.step(tgt_img, tgt_tex, next_host=host_scene_of(k + 1))
+    """
+
+    def __init__(self, renderer: "BatchRenderer", like: Scene):
+        self.r = renderer
+        self.dev = renderer.dev
+        mk = lambda: Scene(**{**like.__dict__, **{k: torch.empty_like(getattr(like, k)) for k in _SCENE_TENSORS}})
+        self.bufs = [mk(), mk()]
+        self.copy_stream = torch.cuda.Stream(device=self.dev)
+        self.ready = [torch.cuda.Event(), torch.cuda.Event()]
+        self.free = [torch.cuda.Event(), torch.cuda.Event()]
+        self.i = 0
+        self.loaded = False
+
+    def _upload(self, host: Scene, slot: int):
+        dst = self.bufs[slot]
+        with torch.cuda.stream(self.copy_stream):
+            self.copy_stream.wait_event(self.free[slot])  # the step that read this buffer is done
+            for k in _SCENE_TENSORS:
+                getattr(dst, k).copy_(getattr(host, k), non_blocking=True)
+            self.ready[slot].record(self.copy_stream)
+
+    def upload(self, host: Scene):
+        """Upload the inputs of the next step (the first one, or after a step
+        taken without next_host)."""
+        self._upload(host, self.i % 2)
+        self.loaded = True
+
+    def step(self, tgt_img, tgt_tex, next_host: Optional[Scene] = None):
+        """One step on the uploaded inputs; next_host's upload starts at once on
+        the copy stream.  Returns the loss tensor (device)."""
+        if not self.loaded:
+            raise RuntimeError("HostInputStepper.step: no inputs uploaded")
+        cur = self.i % 2
+        stream = torch.cuda.current_stream(self.dev)
+        stream.wait_event(self.ready[cur])
+        if next_host is not None:
+            self._upload(next_host, 1 - cur)
+        loss = self.r.step(self.bufs[cur], tgt_img, tgt_tex)
+        self.free[cur].record(stream)
+        self.i += 1
+        self.loaded = next_host is not None
+        return loss
+
+
 def plain_step(s: Scene, cameras: Sequence[Camera], tgt_img, tgt_tex, pix_offsets, *, block_width=16,
                settings=1 << 8, background=None, loss_weights=None, timers=None):
     """The per-view path a caller of the reference API takes: for every camera,

@@ -163,28 +163,57 @@ __global__ void batch_emit_sorted_kernel(int VN, int N, const BatchView* __restr
                                          const int32_t* __restrict__ order, const int32_t* __restrict__ cum,
                                          const uint2* __restrict__ rects, long long capacity,
                                          uint32_t* __restrict__ keys, int32_t* __restrict__ vals) {
+    // A warp emits the slots of its 32 pairs, which are contiguous: each lane
+    // takes every 32nd slot of the range, finds its pair by a binary search
+    // over the pairs' first slots and writes one key, so the stores are
+    // coalesced whatever the pairs' tile counts.
+    const unsigned lane = threadIdx.x & 31;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= VN) return;
-    long long lo = p == 0 ? 0 : (long long)(uint32_t)cum[p - 1];
-    long long hi = (long long)(uint32_t)cum[p];
-    if (hi > capacity) hi = capacity;
-    if (lo >= hi) return;
-    const int j = order[p];
-    const int v = j / N;
-    const int i = j - v * N;
-    const BatchView& bv = views[v];
-    const uint2 rc = rects[j];
-    const int x0 = (int)(rc.x & 0xffffu), x1 = (int)(rc.x >> 16), y0 = (int)(rc.y & 0xffffu), y1 = (int)(rc.y >> 16);
-    long long cur = lo;
-    for (int ty = y0; ty < y1 && cur < hi; ++ty)
-        for (int tx = x0; tx < x1 && cur < hi; ++tx) {
-            keys[cur] = ((uint32_t)(bv.tile_offset + ty * bv.tiles_x + tx) << 1) | 1u;
-            vals[cur] = i;
-            ++cur;
+    const long long last = VN > 0 ? min((long long)(uint32_t)cum[VN - 1], capacity) : 0;
+    long long lo = last, hi = last;
+    if (p < VN) {
+        lo = min(p == 0 ? 0 : (long long)(uint32_t)cum[p - 1], capacity);
+        hi = min((long long)(uint32_t)cum[p], capacity);
+    }
+    uint32_t rx = 0, ry = 0;
+    int toff = 0, tiles_x = 1, gi = 0;
+    if (lo < hi) {
+        const int j = order[p];
+        const int v = j / N;
+        gi = j - v * N;
+        const uint2 rc = rects[j];
+        rx = rc.x;
+        ry = rc.y;
+        toff = views[v].tile_offset;
+        tiles_x = views[v].tiles_x;
+    }
+    const long long wlo = __shfl_sync(0xffffffffu, lo, 0);
+    const long long whi = __shfl_sync(0xffffffffu, hi, 31);
+    for (long long base = wlo; base < whi; base += 32) {  // warp-uniform trip count
+        const long long t = base + lane;
+        int q = 0;  // the last lane whose first slot is <= t (its pair owns t)
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1) {
+            const long long l = __shfl_sync(0xffffffffu, lo, q + step);
+            if (l <= t) q += step;
         }
-    for (; cur < hi; ++cur) {
-        keys[cur] = (uint32_t)bv.tile_offset << 1;
-        vals[cur] = 0;
+        const long long qlo = __shfl_sync(0xffffffffu, lo, q);
+        const uint32_t qx = __shfl_sync(0xffffffffu, rx, q), qy = __shfl_sync(0xffffffffu, ry, q);
+        const int qoff = __shfl_sync(0xffffffffu, toff, q), qtx = __shfl_sync(0xffffffffu, tiles_x, q);
+        const int qgi = __shfl_sync(0xffffffffu, gi, q);
+        if (t < whi) {
+            const int x0 = (int)(qx & 0xffffu), x1 = (int)(qx >> 16), y0 = (int)(qy & 0xffffu), y1 = (int)(qy >> 16);
+            const int w = x1 - x0;
+            const long long u = t - qlo;
+            if (w > 0 && y1 > y0 && u < (long long)w * (y1 - y0)) {
+                const int ty = y0 + (int)(u / w), tx = x0 + (int)(u % w);
+                keys[t] = ((uint32_t)(qoff + ty * qtx + tx) << 1) | 1u;
+                vals[t] = qgi;
+            } else {  // slots beyond the tiles emitted: the reference's zero entries
+                keys[t] = (uint32_t)qoff << 1;
+                vals[t] = 0;
+            }
+        }
     }
 }
 

@@ -61,6 +61,8 @@ __global__ void emit_kernel(int n, int num_isect, const float2* __restrict__ cen
 // Tile ranges (reference csrc/forward.cu:76-98); tiles outside [0, num_tiles)
 // are ignored.
 // ---------------------------------------------------------------------------
+constexpr int kEdgeItems = 4;
+
 // Tile of a sorted key: bits [shift, ...) of a 64-bit (tile | depth) key or of
 // a 32-bit (tile | filler bit) key.
 template <typename K>
@@ -70,17 +72,25 @@ __global__ void bin_edges_kernel(int n, const int64_t* __restrict__ n_dev, const
         const int64_t m = *n_dev;
         n = (int)(m < (int64_t)n ? (m > 0 ? m : 0) : n);
     }
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int cur = (int)(sorted[i] >> shift);
-    const bool ok = cur >= 0 && cur < num_tiles;
-    if (i == 0 && ok) bins[cur].x = 0;
-    if (i == n - 1 && ok) bins[cur].y = n;
-    if (i == 0) return;
-    const int prev = (int)(sorted[i - 1] >> shift);
-    if (prev != cur) {
-        if (prev >= 0 && prev < num_tiles) bins[prev].y = i;
-        if (ok) bins[cur].x = i;
+    // kEdgeItems consecutive items per thread, their keys loaded up front
+    const long long i0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * kEdgeItems;
+    if (i0 >= n) return;
+    int tile[kEdgeItems + 1];
+    tile[0] = i0 > 0 ? (int)(sorted[i0 - 1] >> shift) : -1;
+#pragma unroll
+    for (int q = 0; q < kEdgeItems; q++) tile[q + 1] = i0 + q < n ? (int)(sorted[i0 + q] >> shift) : -1;
+#pragma unroll
+    for (int q = 0; q < kEdgeItems; q++) {
+        const int i = (int)i0 + q;
+        if (i >= n) break;
+        const int prev = tile[q], cur = tile[q + 1];
+        const bool ok = cur >= 0 && cur < num_tiles;
+        if (i == 0 && ok) bins[cur].x = 0;
+        if (i == n - 1 && ok) bins[cur].y = n;
+        if (i > 0 && prev != cur) {
+            if (prev >= 0 && prev < num_tiles) bins[prev].y = i;
+            if (ok) bins[cur].x = i;
+        }
     }
 }
 
@@ -405,7 +415,7 @@ extern "C" int gstex_get_tile_bin_edges(int num_isect, const int64_t* sorted, in
     if (e != cudaSuccess) { set_cuda_error(e, "tile_bin_edges memset"); return GSTEX_ERR_CUDA; }
     if (num_isect == 0) return GSTEX_OK;
     GSTEX_REQUIRE(sorted);
-    bin_edges_kernel<int64_t><<<ceil_div(num_isect, 256), 256, 0, stream>>>(num_isect, nullptr, sorted, 32,
+    bin_edges_kernel<int64_t><<<ceil_div(num_isect, 256 * kEdgeItems), 256, 0, stream>>>(num_isect, nullptr, sorted, 32,
                                                                              num_tiles, (int2*)bins);
     return check_launch("get_tile_bin_edges");
 }
@@ -418,7 +428,7 @@ extern "C" int gstex_get_tile_bin_edges_dyn(int capacity, const int64_t* count, 
     if (e != cudaSuccess) { set_cuda_error(e, "tile_bin_edges memset"); return GSTEX_ERR_CUDA; }
     if (capacity == 0) return GSTEX_OK;
     GSTEX_REQUIRE(sorted);
-    bin_edges_kernel<int64_t><<<ceil_div(capacity, 256), 256, 0, stream>>>(capacity, count, sorted, 32, num_tiles,
+    bin_edges_kernel<int64_t><<<ceil_div(capacity, 256 * kEdgeItems), 256, 0, stream>>>(capacity, count, sorted, 32, num_tiles,
                                                                             (int2*)bins);
     return check_launch("get_tile_bin_edges_dyn");
 }
@@ -431,7 +441,7 @@ extern "C" int gstex_get_tile_bin_edges32_dyn(int capacity, const int64_t* count
     if (e != cudaSuccess) { set_cuda_error(e, "tile_bin_edges32 memset"); return GSTEX_ERR_CUDA; }
     if (capacity == 0) return GSTEX_OK;
     GSTEX_REQUIRE(sorted);
-    bin_edges_kernel<uint32_t><<<ceil_div(capacity, 256), 256, 0, stream>>>(capacity, count, sorted, shift, num_tiles,
+    bin_edges_kernel<uint32_t><<<ceil_div(capacity, 256 * kEdgeItems), 256, 0, stream>>>(capacity, count, sorted, shift, num_tiles,
                                                                              (int2*)bins);
     return check_launch("get_tile_bin_edges32_dyn");
 }

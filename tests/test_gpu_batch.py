@@ -311,6 +311,36 @@ def test_gaussians_per_batch_does_not_change_results(setup, fwd_batch, bwd_batch
         assert np.abs(a - b).max() <= 1e-4 * (np.abs(b).max() + 1e-12), k
 
 
+def test_host_input_stepper_matches_device_step(setup):
+    """Steps fed from pinned host tensors through HostInputStepper (the next
+    step's upload overlapping the current step) give the device step's loss
+    and gradients; a changed host scene reaches the next step."""
+    from gstex_cuda_gb300 import batch as B
+    spec, cams, r, scene, _ = setup
+    gen = torch.Generator().manual_seed(1)
+    tgt_img = torch.rand(r.total_pixels, 3, generator=gen).to(DEV)
+    tgt_tex = torch.rand(r.total_pixels, 3, generator=gen).to(DEV)
+    names = ("means", "scales", "quats", "opacity", "sh_coeffs", "uv0", "umap", "vmap", "texture_dims", "texture")
+    host = B.Scene(**{**scene.__dict__, **{k: getattr(scene, k).cpu().pin_memory() for k in names}})
+    host2 = B.Scene(**{**host.__dict__, "opacity": (host.opacity * 0.5).pin_memory()})
+    scene2 = B.Scene(**{**scene.__dict__, "opacity": scene.opacity * 0.5})
+    l_ref = float(r.step(scene, tgt_img, tgt_tex).item())
+    g_ref = {k: v.clone() for k, v in r.grads.items()}
+    l_ref2 = float(r.step(scene2, tgt_img, tgt_tex).item())
+    st = B.HostInputStepper(r, like=scene)
+    st.upload(host)
+    losses = []
+    for nxt in (host, host2, None):
+        losses.append(float(st.step(tgt_img, tgt_tex, next_host=nxt).item()))
+        if len(losses) == 1:
+            g1 = {k: v.clone() for k, v in r.grads.items()}
+    torch.cuda.synchronize()
+    assert abs(losses[0] - l_ref) <= 1e-5 * abs(l_ref) and abs(losses[1] - l_ref) <= 1e-5 * abs(l_ref)
+    assert abs(losses[2] - l_ref2) <= 1e-5 * abs(l_ref2)
+    for k, v in g_ref.items():
+        torch.testing.assert_close(g1[k], v, atol=1e-5 * (float(v.abs().max()) + 1e-9), rtol=1e-4)
+
+
 def test_batch_graph_replay_matches_eager(setup):
     spec, cams, r, scene, _ = setup
     P = r.total_pixels
