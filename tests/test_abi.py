@@ -124,3 +124,31 @@ def test_static_scratch_sort_rejects_bad_arguments_without_gpu():
     assert f(10, 65, None, None, None, None, None) == 1
     assert f(10, -1, None, None, None, None, None) == 1
     assert f((1 << 20) + 1, 45, None, None, None, None, None) == 2
+
+
+def test_batch_knobs_and_tile_order_rejected_without_gpu():
+    """The batched entry points check the launch knobs and the queue-order
+    arguments before any device work: a negative Gaussians-per-batch or
+    resident-CTA count, a tile-order group outside [1, 64], a group above 1
+    without the views, or a short workspace."""
+    import ctypes
+    from gstex_cuda_gb300 import batch as B
+    L = B._L()
+    bi = B.BatchInputs()
+    bi.num_points, bi.num_views, bi.total_tiles, bi.block_width, bi.channels = 10, 1, 4, 8, 3
+    dummy = ctypes.c_void_p(16)
+    bi.views = bi.tile_view = bi.tile_bins = bi.background = bi.queue = dummy
+    bi.gaussian_ids_sorted = bi.colors = bi.texture_dims = bi.opacities = bi.means = dummy
+    bi.scales = bi.quats = bi.uv0 = bi.umap = bi.vmap = dummy
+    fwd = L.gstex_batch_forward
+    for field, value in (("batch_size", -1), ("resident_ctas", -1)):
+        setattr(bi, field, value)
+        assert fwd(ctypes.byref(bi), None, None) == 1, field
+        setattr(bi, field, 0)
+    order = L.gstex_batch_tile_order
+    ws = L.gstex_batch_tile_order_workspace_bytes(100)
+    assert order(100, dummy, dummy, dummy, 0, dummy, dummy, ws, None) == 1
+    assert order(100, dummy, dummy, dummy, 65, dummy, dummy, ws, None) == 1
+    assert order(100, dummy, None, None, 4, dummy, dummy, ws, None) == 1
+    assert order(100, dummy, dummy, dummy, 4, dummy, dummy, ws - 1, None) == 2
+    assert order(0, None, None, None, 4, None, None, 0, None) == 0
