@@ -219,12 +219,13 @@ def reference_kernels_leg(spec, dev, steps, warmup=1):
 # launch on the full 32-view workload, from single-pass ncu captures of the
 # launches of one step (profiles/compositor_dram_traffic_32views.txt gives the
 # commands and the raw figures).  Keyed by (kernel, tile width); tile width 8
-# is the backward variant compiled for 10 CTAs per SM with 8-lane groups, 16
-# the general backward kernel with 8-lane groups (figures printed in GB with
-# two decimals).  Used only for the default workload.
+# is the autotuned configuration (forward and 10-CTA backward with 8-lane
+# groups, both compiled for the default settings; forward queue in 4x4-tile
+# groups), 16 the general kernels with 8-lane groups (figures printed in GB
+# with two decimals).  Used only for the default workload.
 DRAM_BYTES_PER_LAUNCH = {
-    ("forward", 8): 20_606_735_360 + 1_797_965_568,
-    ("backward", 8): 21_534_149_120 + 7_764_672_256,
+    ("forward", 8): 12_075_774_720 + 1_747_140_608,
+    ("backward", 8): 21_443_585_792 + 7_728_033_280,
     ("forward", 16): 13.14e9 + 1.77e9,
     ("backward", 16): 20.45e9 + 7.37e9,
 }
