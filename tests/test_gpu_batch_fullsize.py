@@ -64,11 +64,16 @@ def _workload(which):
     return synthetic.stress(seed=4, n=1_000_000, texels=32_000_000, views=8)
 
 
-@pytest.mark.parametrize("which,bw", [("multiview_32x_500k_16M", 16), ("multiview_32x_500k_16M", 8),
-                                      ("stress_8x1080p_1M_32M", 16)])
-def test_batched_step_at_full_size_vs_reference_kernels(which, bw):
-    """Tile widths 16 (the reference's) and 8 (the autotuner's choice on the
-    32-view scene): the reference's kernels run with the same width."""
+# (scene, tile width, backward lanes per walk, backward CTAs per SM, Gaussians per batch):
+# the reference's 16x16 tiles, and the configurations the autotuner picks
+@pytest.mark.parametrize("which,bw,gs,ctas,nb", [("multiview_32x_500k_16M", 16, 8, 0, 0),
+                                                ("multiview_32x_500k_16M", 8, 8, 10, 0),
+                                                ("stress_8x1080p_1M_32M", 16, 8, 0, 0),
+                                                ("stress_8x1080p_1M_32M", 8, 32, 10, 48)])
+def test_batched_step_at_full_size_vs_reference_kernels(which, bw, gs, ctas, nb):
+    """Tile widths 16 (the reference's) and 8 (the autotuner's choice on both
+    scenes, with the backward variant it picks): the reference's kernels run
+    with the same width."""
     from gstex_cuda_gb300 import batch as B
     from oracle import refkern as R
     spec = _workload(which)
@@ -83,9 +88,8 @@ def test_batched_step_at_full_size_vs_reference_kernels(which, bw):
                     sh_coeffs=d(sh16), sh_degree=spec.sh_degree, uv0=d(spec.uv0), umap=d(spec.umap),
                     vmap=d(spec.vmap), texture_dims=d(spec.texture_dims), texture=d(t16))
     bcams = [B.Camera(c.viewmat, c.fx, c.fy, c.cx, c.cy, c.width, c.height) for c in cams]
-    # 8x8 tiles: the backward compiled for 10 CTAs per SM, as the autotuner picks
     r = B.BatchRenderer(bcams, spec.num_points, texture_dtype=torch.bfloat16, device=DEV, block_width=bw,
-                        bwd_ctas=10 if bw == 8 else 0)
+                        bwd_group=gs, bwd_ctas=ctas, bwd_batch=nb)
     gen = torch.Generator().manual_seed(11)
     tgt_img = torch.rand(r.total_pixels, 3, generator=gen).to(DEV)
     tgt_tex = torch.rand(r.total_pixels, 3, generator=gen).to(DEV)
