@@ -64,6 +64,8 @@ def parse():
     p.add_argument("--bwd-group", type=int, default=8)
     p.add_argument("--bwd-ctas", type=int, default=10,
                    help="with --no-autotune: backward kernel compiled for this many CTAs per SM (8x8 tiles)")
+    p.add_argument("--bwd-batch", type=int, default=0,
+                   help="with --no-autotune: Gaussians per batch of the backward (0: one per thread)")
     p.add_argument("--tile-widths", default="16,8",
                    help="tile widths the autotuner tries (each bins the scene anew); the last is used "
                         "with --no-autotune")
@@ -216,28 +218,34 @@ def reference_kernels_leg(spec, dev, steps, warmup=1):
 
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one compositor
-# launch on the full 32-view workload, from single-pass ncu captures of the
-# launches of one step (profiles/compositor_dram_traffic_32views.txt gives the
-# commands and the raw figures).  Keyed by (kernel, tile width); tile width 8
-# is the autotuned configuration (forward and 10-CTA backward with 8-lane
-# groups, both compiled for the default settings; forward queue in 4x4-tile
-# groups), 16 the general kernels with 8-lane groups (figures printed in GB
-# with two decimals).  Used only for the default workload.
+# launch on the full workloads, from single-pass ncu captures of the launches
+# of one step (profiles/compositor_dram_traffic_full_workloads.txt gives the
+# commands and the raw figures).  Keyed by (workload, kernel, tile width), for
+# the kernels the autotuner picks at that width: 8x8 tiles, forward compiled
+# for the default settings with its queue in 4x4-tile groups and the 10-CTA
+# backward (8-lane groups on the 32-view scene; 32-lane walk and 48 Gaussians
+# per batch on the stress scene); 16x16 tiles, the general backward (8-lane
+# groups on the 32-view scene, 32-lane walk on the stress scene).
 DRAM_BYTES_PER_LAUNCH = {
-    ("forward", 8): 12_075_774_720 + 1_747_140_608,
-    ("backward", 8): 21_443_585_792 + 7_728_033_280,
-    ("forward", 16): 13.14e9 + 1.77e9,
-    ("backward", 16): 20.45e9 + 7.37e9,
+    ("batched", "forward", 8): 12_075_774_720 + 1_747_140_608,
+    ("batched", "backward", 8): 21_443_585_792 + 7_728_033_280,
+    ("batched", "forward", 16): 9_822_225_152 + 1_737_394_176,
+    ("batched", "backward", 16): 20_452_395_264 + 7_372_365_824,
+    ("stress", "forward", 8): 5_279_288_320 + 1_163_496_192,
+    ("stress", "backward", 8): 8_169_039_360 + 2_389_876_992,
+    ("stress", "forward", 16): 4_011_032_064 + 1_154_998_272,
+    ("stress", "backward", 16): 7_881_462_272 + 2_271_416_064,
 }
-TRAFFIC_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch, 32-view workload"
+DEFAULT_VIEWS = {"batched": 32, "stress": 8}
+TRAFFIC_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of this workload"
 
 
 def dram_traffic_model(kernel, block_width, workload="batched", views=32):
-    """Measured DRAM bytes of one launch of `kernel` at this tile width on the
-    default workload, or None (other workloads or widths)."""
-    if workload != "batched" or views != 32:
+    """Measured DRAM bytes of one launch of `kernel` at this tile width on a
+    default workload, or None (other view counts or widths)."""
+    if views != DEFAULT_VIEWS.get(workload):
         return None
-    return DRAM_BYTES_PER_LAUNCH.get((kernel, block_width))
+    return DRAM_BYTES_PER_LAUNCH.get((workload, kernel, block_width))
 
 
 def algorithmic_bytes(I, tiles, T, P, C, N, tex_bytes_per_texel, grad_texel_bytes, backward):
@@ -373,9 +381,9 @@ def main():
     tgt_img = torch.rand(P, 3, generator=gen).to(dev)
     tgt_tex = torch.rand(P, 3, generator=gen).to(dev)
     if args.no_autotune:
-        r = make_renderer(widths[-1], bwd_group=args.bwd_group, bwd_ctas=args.bwd_ctas)
+        r = make_renderer(widths[-1], bwd_group=args.bwd_group, bwd_ctas=args.bwd_ctas, bwd_batch=args.bwd_batch)
         tuned = {"fixed": True, "block_width": r.bw, "fwd_ppt": r.fwd_ppt, "bwd_ppt": r.bwd_ppt,
-                 "bwd_group": r.bwd_group, "bwd_ctas": r.bwd_ctas}
+                 "bwd_group": r.bwd_group, "bwd_ctas": r.bwd_ctas, "bwd_batch": r.bwd_batch or "threads"}
     else:
         # tile width: each candidate bins the scene anew, is tuned on its own
         # and timed over whole steps; the fastest renderer is kept
