@@ -197,6 +197,77 @@ def test_batch_forward_backward_vs_oracle(setup):
     assert err < 5e-4, ("sh", err)
 
 
+@pytest.mark.parametrize("settings", [(1 << 8) | (1 << 9), (1 << 8) | (1 << 10), (1 << 8) | (1 << 2), 0],
+                         ids=["blur", "ndc", "nearest", "no_uv_grad"])
+@pytest.mark.parametrize("bw,tex", [(16, "f32"), (8, "f32"), (8, "bf16")])
+def test_batch_settings_variants_vs_oracle(settings, bw, tex):
+    """Settings other than the default (blur, NDC depth, nearest texels, uv
+    gradients not propagated) take the general compositor kernels instead of
+    the ones compiled for the default settings (with bf16 texels and 8x8
+    tiles, the 10-CTA backward compiled for run-time settings): the batched
+    step still matches the fp64 oracle per view."""
+    from gstex_cuda_gb300 import batch as B, synthetic
+    g = torch.Generator().manual_seed(31)
+    cams = synthetic.sphere_cameras(g, 2, radius=8.0, resolutions=[(96, 64), (80, 80)])
+    spec = synthetic._finish_with_area(g, torch.empty(1500, 3).uniform_(-3, 3, generator=g), 0.01, 0.1, 3, "normal",
+                                       cams, 20_000, "multi", {})
+    texture, tex_np = spec.texture, spec.texture.numpy()
+    if tex == "bf16":
+        texture = torch.zeros(spec.texture.shape[0], 4, dtype=torch.bfloat16)
+        texture[:, :3] = spec.texture.to(torch.bfloat16)
+        tex_np = texture[:, :3].float().numpy()
+    scene = B.Scene(means=spec.means.to(DEV), scales=spec.scales.to(DEV), quats=spec.quats.to(DEV),
+                    opacity=spec.opacity.to(DEV), sh_coeffs=spec.sh_coeffs.to(DEV), sh_degree=3,
+                    uv0=spec.uv0.to(DEV), umap=spec.umap.to(DEV), vmap=spec.vmap.to(DEV),
+                    texture_dims=spec.texture_dims.to(DEV), texture=texture.to(DEV))
+    bcams = [B.Camera(c.viewmat, c.fx, c.fy, c.cx, c.cy, c.width, c.height) for c in cams]
+    r = B.BatchRenderer(bcams, spec.num_points, capacity=1 << 20, block_width=bw, settings=settings,
+                        texture_dtype=torch.bfloat16 if tex == "bf16" else torch.float32,
+                        bwd_ctas=10 if bw == 8 else 0)
+    gen = torch.Generator().manual_seed(3)
+    tgt_img = torch.rand(r.total_pixels, 3, generator=gen).to(DEV)
+    tgt_tex = torch.rand(r.total_pixels, 3, generator=gen).to(DEV)
+    r.step(scene, tgt_img, tgt_tex)
+    torch.cuda.synchronize()
+    gs = r.gids_sorted.cpu().numpy()
+    bins = r.bins.cpu().numpy()
+    ups = {k: v.cpu().numpy() for k, v in r.ups.items()}
+    tot, toff = None, 0
+    for v, cam in enumerate(cams):
+        sc = _scene_np(spec, r.colors[v].cpu().numpy())
+        sc = oracle.Scene(**{**sc.__dict__, "texture": tex_np})
+        oc = oracle.Camera(cam.viewmat.numpy(), cam.c2w.numpy(), cam.fx, cam.fy, cam.cx, cam.cy, cam.height,
+                           cam.width)
+        nt = ((cam.width + bw - 1) // bw) * ((cam.height + bw - 1) // bw)
+        vb = bins[toff:toff + nt]
+        toff += nt
+        ref = oracle.texture_forward(sc, oc, gs, vb, bw, settings, np.zeros(3), prec="f64")
+        # (depth is the camera depth of the splat where T crosses 0.5: a pixel
+        # whose T lands within rounding of 0.5 takes the neighbouring splat's)
+        for k in ("img", "texture", "normal", "final_T"):
+            got = r.view_output(k, v).cpu().numpy()
+            err = np.abs(got - ref[k].reshape(got.shape))
+            assert (err > 1e-4).mean() <= 1e-3 and err.max() < 1e-2, (k, v, float(err.max()))
+        a, b = r.pix_offsets_host[v], r.pix_offsets_host[v + 1]
+        H, W = cam.height, cam.width
+        up = dict(img=ups["img"][a:b].reshape(H, W, 3), texture=ups["texture"][a:b].reshape(H, W, 3),
+                  normal=ups["normal"][a:b].reshape(H, W, 3), reg=ups["reg"][a:b].reshape(H, W))
+        gr = oracle.texture_backward(sc, oc, gs, vb, bw, settings, np.zeros(3), ref, up["img"], np.zeros((H, W)),
+                                     up["reg"], np.zeros((H, W)), up["texture"], up["normal"], prec="f64")
+        tot = gr if tot is None else {k: tot[k] + gr[k] for k in tot}
+    G = r.grads
+    for k in ("opacity", "means", "scales", "quats", "uv0", "umap", "vmap", "texture"):
+        got = G[k].cpu().numpy()
+        ref = tot[k]
+        if k == "texture":  # bf16 texels: gradients [T, 4], the fourth column unused
+            got = got[:, :ref.shape[1]]
+        got, ref = got.reshape(-1), ref.reshape(-1)
+        err = np.abs(got - ref).max() / (np.abs(ref).max() + 1e-12)
+        # 1e-3 of the largest entry (5e-4 at the default settings): the blur
+        # terms add an exp and a second alpha branch per pair
+        assert err < 1e-3, (k, err)
+
+
 def test_batch_loss_value(setup):
     spec, cams, r, scene, loss = setup
     o = r.out
