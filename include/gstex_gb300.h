@@ -392,8 +392,8 @@ typedef struct gstex_batch_inputs {
     const void* records;                /* optional: gstex_batch_records output (16-byte aligned);
                                            null = each tile derives the records it stages */
     int group_lanes;                    /* backward: lanes per splat walk (see gstex_raster_inputs) */
-    int batch_size;                     /* Gaussians a tile stages per round, 1..threads per CTA;
-                                           0 = one per thread (the reference's bw^2) */
+    int batch_size;                     /* Gaussians a tile stages per round; 0, or at least the
+                                           threads of a CTA: one per thread (the reference's bw^2) */
     int resident_ctas;                  /* backward, 8x8 tiles with bf16 RGB texels and 8-lane groups (or
                                            32 at the default settings): 10 selects a kernel compiled for
                                            10 CTAs per SM (96 registers per thread instead of 124); other
