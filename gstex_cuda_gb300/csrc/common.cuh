@@ -185,6 +185,41 @@ struct Recs {
 __device__ __forceinline__ float4 f4(float3 v, float w) { return make_float4(v.x, v.y, v.z, w); }
 __device__ __forceinline__ float3 f3(float4 v) { return make_float3(v.x, v.y, v.z); }
 
+// Pairs of fp32 values in one instruction (the f32x2 add / mul / fma of this
+// GPU): each half is the IEEE fp32 operation, rounded to nearest; fma2 is a
+// fused multiply-add per half.
+__device__ __forceinline__ unsigned long long pack2(float2 a) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+    return r;
+}
+__device__ __forceinline__ float2 unpack2(unsigned long long r) {
+    float2 a;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
+    return a;
+}
+__device__ __forceinline__ float2 add2(float2 a, float2 b) {
+    unsigned long long r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pack2(a)), "l"(pack2(b)));
+    return unpack2(r);
+}
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+    unsigned long long r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pack2(a)), "l"(pack2(b)));
+    return unpack2(r);
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
+    unsigned long long r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pack2(a)), "l"(pack2(b)));
+    return unpack2(r);
+}
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+    unsigned long long r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(pack2(a)), "l"(pack2(b)), "l"(pack2(c)));
+    return unpack2(r);
+}
+__device__ __forceinline__ float2 dup2(float a) { return make_float2(a, a); }
+
 // Near-edge-on splats (|n_c . d0| < kEdgeOn): the plane coefficients in
 // double.  Writes H.org, H.nop.x/.y, H.lc and Wm.uvm.
 constexpr float kEdgeOn = 0.05f;
@@ -404,8 +439,9 @@ __device__ __forceinline__ float clamp_denom(float d) {
 // direct form (computed by the caller from the Gaussian's parameters).
 __device__ __forceinline__ Hit intersect(const RecHot& Hr, const PixelRay& P) {
     Hit H;
-    H.du = P.px - Hr.org.x;
-    H.dv = P.py - Hr.org.y;
+    const float2 d = sub2(make_float2(P.px, P.py), make_float2(Hr.org.x, Hr.org.y));
+    H.du = d.x;
+    H.dv = d.y;
     const float den = Hr.org.z + Hr.nop.x * H.du + Hr.nop.y * H.dv;
     H.nd = den;
     H.direct = __float_as_int(Hr.nop.w) != 0 || !(fabsf(den) >= kDenomEps * P.dn);
@@ -413,8 +449,10 @@ __device__ __forceinline__ Hit intersect(const RecHot& Hr, const PixelRay& P) {
     H.inv = inv;
     H.tcam = Hr.org.w * inv;
     H.t = H.tcam * P.dn;
-    H.l1s = (Hr.lc.x * H.du + Hr.lc.y * H.dv) * inv;
-    H.l2s = (Hr.lc.z * H.du + Hr.lc.w * H.dv) * inv;
+    const float2 l = mul2(fma2(make_float2(Hr.lc.y, Hr.lc.w), dup2(H.dv),
+                               mul2(make_float2(Hr.lc.x, Hr.lc.z), dup2(H.du))), dup2(inv));
+    H.l1s = l.x;
+    H.l2s = l.y;
     return H;
 }
 
@@ -439,9 +477,11 @@ __device__ __forceinline__ void intersect_direct(Hit& H, const PixelRay& P, floa
 
 // Texture coordinates of the hit (before clamping).
 __device__ __forceinline__ float2 hit_uv(const Hit& H, const RecWarm& Wm) {
-    if (!H.direct)
-        return make_float2(Wm.uvs.x + (Wm.uvm.x * H.du + Wm.uvm.y * H.dv) * H.inv,
-                           Wm.uvs.y + (Wm.uvm.z * H.du + Wm.uvm.w * H.dv) * H.inv);
+    if (!H.direct) {
+        const float2 t = fma2(make_float2(Wm.uvm.y, Wm.uvm.w), dup2(H.dv),
+                              mul2(make_float2(Wm.uvm.x, Wm.uvm.z), dup2(H.du)));
+        return fma2(t, dup2(H.inv), make_float2(Wm.uvs.x, Wm.uvs.y));
+    }
     return make_float2(H.tu, H.tv);
 }
 
@@ -462,14 +502,17 @@ struct Bilerp {
 
 __device__ __forceinline__ Bilerp bilerp(int h, int w, int start, float u, float v, bool bilinear) {
     Bilerp B;
-    const float tcx = (float)h * u, tcy = (float)w * v;
+    const float2 tc = mul2(make_float2((float)h, (float)w), make_float2(u, v));
+    const float tcx = tc.x, tcy = tc.y;
     int iix = __float2int_rz(tcx), iiy = __float2int_rz(tcy);
     const int jjx = min(iix + 1, h - 1), jjy = min(iiy + 1, w - 1);
     const float wx = tcx - (float)iix, wy = tcy - (float)iiy;
     iix = min(iix, h - 1);
     iiy = min(iiy, w - 1);
     B.fx = wx; B.fy = wy;
-    const float w00 = (1.f - wx) * (1.f - wy), w01 = (1.f - wx) * wy, w10 = wx * (1.f - wy), w11 = wx * wy;
+    const float2 wyy = make_float2(1.f - wy, wy);
+    const float2 w0 = mul2(dup2(1.f - wx), wyy), w1 = mul2(dup2(wx), wyy);
+    const float w00 = w0.x, w01 = w0.y, w10 = w1.x, w11 = w1.y;
     B.i00 = start + iix * w + iiy;
     B.i01 = start + iix * w + jjy;
     B.i10 = start + jjx * w + iiy;

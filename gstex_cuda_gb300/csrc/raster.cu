@@ -346,12 +346,22 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
                 // outside the outline: the colour; on it: white (bit 24) or nothing
                 const bool plain = !alpha_vis || pixel_dis > outline_bound;
                 const float wv = plain ? 0.f : (white_outline ? vis : 0.f);
-                out[p].x = out[p].x + (plain ? col.x * vis : wv);
-                out[p].y = out[p].y + (plain ? col.y * vis : wv);
-                out[p].z = out[p].z + (plain ? col.z * vis : wv);
+                if (!alpha_vis) {
+                    const float2 o2 = fma2(make_float2(col.x, col.y), dup2(vis), make_float2(out[p].x, out[p].y));
+                    out[p].x = o2.x;
+                    out[p].y = o2.y;
+                    out[p].z = out[p].z + col.z * vis;
+                } else {
+                    out[p].x = out[p].x + (plain ? col.x * vis : wv);
+                    out[p].y = out[p].y + (plain ? col.y * vis : wv);
+                    out[p].z = out[p].z + (plain ? col.z * vis : wv);
+                }
                 float3 hn = f3(Wm.nrm);
                 if (flip && H.nd > 0.f) hn = make_float3(-hn.x, -hn.y, -hn.z);
-                nrm[p].x += vis * hn.x; nrm[p].y += vis * hn.y; nrm[p].z += vis * hn.z;
+                const float2 n2 = fma2(dup2(vis), make_float2(hn.x, hn.y), make_float2(nrm[p].x, nrm[p].y));
+                nrm[p].x = n2.x;
+                nrm[p].y = n2.y;
+                nrm[p].z += vis * hn.z;
                 if (C > 0) {
                     const float2 uv = hit_uv(H, Wm);
                     const int4 tx = Wm.tex;
@@ -359,11 +369,22 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
                     if (CT == 3) {
                         float c[4][3];
                         fetch3<TM>(a.tex, B, c);
+                        if (!alpha_vis) {  // channels 0 and 1 as one pair
+                            float2 v = mul2(dup2(B.w00), make_float2(c[0][0], c[0][1]));
+                            v = fma2(dup2(B.w01), make_float2(c[1][0], c[1][1]), v);
+                            v = fma2(dup2(B.w10), make_float2(c[2][0], c[2][1]), v);
+                            v = fma2(dup2(B.w11), make_float2(c[3][0], c[3][1]), v);
+                            const float2 o2 = fma2(dup2(vis), v, make_float2(otex[p][0], otex[p][1]));
+                            otex[p][0] = o2.x;
+                            otex[p][1] = o2.y;
+                            otex[p][2] += vis * (B.w00 * c[0][2] + B.w01 * c[1][2] + B.w10 * c[2][2] + B.w11 * c[3][2]);
+                        } else {
 #pragma unroll
-                        for (int ch = 0; ch < 3; ch++)
-                            otex[p][ch] += plain ? vis * (B.w00 * c[0][ch] + B.w01 * c[1][ch] + B.w10 * c[2][ch] +
-                                                          B.w11 * c[3][ch])
-                                                 : wv;
+                            for (int ch = 0; ch < 3; ch++)
+                                otex[p][ch] += plain ? vis * (B.w00 * c[0][ch] + B.w01 * c[1][ch] + B.w10 * c[2][ch] +
+                                                              B.w11 * c[3][ch])
+                                                     : wv;
+                        }
                     } else if (CT != 0) {
                         const float* t = (const float*)a.tex;
                         for (int ch = 0; ch < C; ch++) {
@@ -378,8 +399,9 @@ __device__ __forceinline__ void fwd_tile(const SceneArgs& a, const TileJob& J, c
                 const float dv = use_ndc ? (kTFar * t_view - kTFar * kTNear) / ((kTFar - kTNear) * t_view) : H.t;
                 reg[p] += vis * (dv * dv * ts[p].x + ts[p].z - 2.f * dv * ts[p].y);
                 ts[p].x += vis;
-                ts[p].y += vis * dv;
-                ts[p].z += vis * dv * dv;
+                const float2 t2 = fma2(dup2(vis), make_float2(dv, dv * dv), make_float2(ts[p].y, ts[p].z));
+                ts[p].y = t2.x;
+                ts[p].z = t2.y;
                 T[p] = next_T;
                 cur[p] = bstart + k;
             }
@@ -583,27 +605,29 @@ __device__ __forceinline__ void bwd_pair(const SceneArgs& a, const BwdArgs& g, c
     v_t += P.idn * v_t_view;
     const float vtd = v_t * (P.dn * H.inv);  // v_t / (n . r)
     const float v_sb = -bf * Hr.nop.z * eb * v_alpha;
-    m[0] += vis * vout.x;
-    m[1] += vis * vout.y;
+    // (pairs of moments as one f32x2 operation where they line up)
+    const float2 ls = make_float2(H.l1s, H.l2s);
+    float2 t2 = fma2(dup2(vis), make_float2(vout.x, vout.y), make_float2(m[0], m[1]));
+    m[0] = t2.x; m[1] = t2.y;
     m[2] += vis * vout.z;
     m[3] += (nbf * e + bf * eb) * v_alpha;
-    m[4] += H.l1s * p1;  // = l1 v_l1;  v_scale1 = -is1 glob m4
-    m[5] += H.l2s * p2;  // = l2 v_l2
+    t2 = fma2(ls, make_float2(p1, p2), make_float2(m[4], m[5]));  // l1 v_l1, l2 v_l2; v_scale1 = -is1 glob m4
+    m[4] = t2.x; m[5] = t2.y;
     m[6] += H.l1s * p2;  // l2 v_l1 = (is1 / is2) m6, l1 v_l2 = (is2 / is1) m6
-    m[7] += p1;          // v_l1 / is1
-    m[8] += p2;
+    t2 = add2(make_float2(m[7], m[8]), make_float2(p1, p2));  // v_l1 / is1, v_l2 / is2
+    m[7] = t2.x; m[8] = t2.y;
     m[9] += vtd;
-    m[10] += H.l1s * vtd;  // l1 vtd is1
-    m[11] += H.l2s * vtd;
-    m[12] += vis * vnorm.x;
-    m[13] += vis * vnorm.y;
+    t2 = fma2(ls, dup2(vtd), make_float2(m[10], m[11]));  // l1 vtd is1, l2 vtd is2
+    m[10] = t2.x; m[11] = t2.y;
+    t2 = fma2(dup2(vis), make_float2(vnorm.x, vnorm.y), make_float2(m[12], m[13]));
+    m[12] = t2.x; m[13] = t2.y;
     m[14] += vis * vnorm.z;
-    m[15] += v_u;
-    m[16] += v_v;
-    m[17] += H.l1s * v_u;  // l1 v_u is1
-    m[18] += H.l2s * v_u;
-    m[19] += H.l1s * v_v;
-    m[20] += H.l2s * v_v;
+    t2 = add2(make_float2(m[15], m[16]), make_float2(v_u, v_v));
+    m[15] = t2.x; m[16] = t2.y;
+    t2 = fma2(ls, dup2(v_u), make_float2(m[17], m[18]));  // l1 v_u is1, l2 v_u is2
+    m[17] = t2.x; m[18] = t2.y;
+    t2 = fma2(ls, dup2(v_v), make_float2(m[19], m[20]));
+    m[19] = t2.x; m[20] = t2.y;
     if constexpr (NM == kMoments) {
         m[21] += kBlurFsq * v_sb * (Wm.uvs.z - P.px);
         m[22] += kBlurFsq * v_sb * (Wm.uvs.w - P.py);
