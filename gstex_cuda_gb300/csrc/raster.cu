@@ -447,13 +447,17 @@ struct Ragged {
     static constexpr int OUT = Ragged<H, OFF / 2>::OUT;
     static __device__ __forceinline__ void reduce(float* m, unsigned lane) {
         const bool upper = lane & OFF;
+        // two values per step: their sums as one f32x2 add
 #pragma unroll
-        for (int j = 0; j < H; j++) {
-            const float lo = m[j];
-            const float hi = j + H < N ? m[j + H] : 0.f;
-            const float send = upper ? lo : hi;
-            const float keep = upper ? hi : lo;
-            m[j] = keep + __shfl_xor_sync(0xffffffffu, send, OFF);
+        for (int j = 0; j < H; j += 2) {
+            const int j1 = j + 1 < H ? j + 1 : j;
+            const float lo0 = m[j], lo1 = m[j1];
+            const float hi0 = j + H < N ? m[j + H] : 0.f, hi1 = j1 + H < N ? m[j1 + H] : 0.f;
+            const float r0 = __shfl_xor_sync(0xffffffffu, upper ? lo0 : hi0, OFF);
+            const float r1 = __shfl_xor_sync(0xffffffffu, upper ? lo1 : hi1, OFF);
+            const float2 sum = add2(make_float2(upper ? hi0 : lo0, upper ? hi1 : lo1), make_float2(r0, r1));
+            m[j] = sum.x;
+            if (j + 1 < H) m[j1] = sum.y;
         }
         Ragged<H, OFF / 2>::reduce(m, lane);
     }
@@ -515,27 +519,41 @@ __device__ __forceinline__ void bwd_pair(const SceneArgs& a, const BwdArgs& g, c
         if (CT == 3) {
             float c[4][3];
             fetch3<TEXMODE>(a.tex, B, c);
-            float gv[3];
-#pragma unroll
-            for (int ch = 0; ch < 3; ch++) {
-                const float val = B.w00 * c[0][ch] + B.w01 * c[1][ch] + B.w10 * c[2][ch] + B.w11 * c[3][ch];
-                const float vv = vis * S.vtex[ch];
-                gv[ch] = vv;
-                if (bilinear && prop_uv) {
-                    v_u += fh * (vv * (-(1.f - B.fy) * c[0][ch] - B.fy * c[1][ch] + (1.f - B.fy) * c[2][ch] + B.fy * c[3][ch]));
-                    v_v += fw * (vv * (-(1.f - B.fx) * c[0][ch] + (1.f - B.fx) * c[1][ch] - B.fx * c[2][ch] + B.fx * c[3][ch]));
-                }
-                v_vis += val * S.vtex[ch];
+            // channels 0 and 1 as f32x2 pairs, channel 2 alone
+            const float2 c0 = make_float2(c[0][0], c[0][1]), c1 = make_float2(c[1][0], c[1][1]);
+            const float2 c2 = make_float2(c[2][0], c[2][1]), c3 = make_float2(c[3][0], c[3][1]);
+            const float2 vt = make_float2(S.vtex[0], S.vtex[1]);
+            float2 val = mul2(dup2(B.w00), c0);
+            val = fma2(dup2(B.w01), c1, val);
+            val = fma2(dup2(B.w10), c2, val);
+            val = fma2(dup2(B.w11), c3, val);
+            const float val2 = B.w00 * c[0][2] + B.w01 * c[1][2] + B.w10 * c[2][2] + B.w11 * c[3][2];
+            const float2 gv01 = mul2(dup2(vis), vt);
+            const float gv2 = vis * S.vtex[2];
+            if (bilinear && prop_uv) {
+                // d(val)/d(tcx) = (1 - fy)(c10 - c00) + fy (c11 - c01),
+                // d(val)/d(tcy) = (1 - fx)(c01 - c00) + fx (c11 - c10)
+                const float2 du = fma2(dup2(B.fy), sub2(c3, c1), mul2(dup2(1.f - B.fy), sub2(c2, c0)));
+                const float2 dv = fma2(dup2(B.fx), sub2(c3, c2), mul2(dup2(1.f - B.fx), sub2(c1, c0)));
+                const float du2 = (1.f - B.fy) * (c[2][2] - c[0][2]) + B.fy * (c[3][2] - c[1][2]);
+                const float dv2 = (1.f - B.fx) * (c[1][2] - c[0][2]) + B.fx * (c[3][2] - c[2][2]);
+                const float2 pu = mul2(gv01, du), pv = mul2(gv01, dv);
+                v_u += fh * (pu.x + pu.y + gv2 * du2);
+                v_v += fw * (pv.x + pv.y + gv2 * dv2);
             }
-            if (gv[0] != 0.f || gv[1] != 0.f || gv[2] != 0.f) {
+            const float2 vs = mul2(val, vt);
+            v_vis += vs.x + vs.y + val2 * S.vtex[2];
+            if (gv01.x != 0.f || gv01.y != 0.f || gv2 != 0.f) {
                 const int rows[4] = { B.i00, B.i01, B.i10, B.i11 };
                 const float wts[4] = { B.w00, B.w01, B.w10, B.w11 };
+                const float gv[3] = { gv01.x, gv01.y, gv2 };
 #pragma unroll
                 for (int q = 0; q < 4; q++) {
                     if (wts[q] == 0.f) continue;
                     if (TEXMODE == 1) {
+                        const float2 g01 = mul2(dup2(wts[q]), gv01);
                         atomicAdd(reinterpret_cast<float4*>(g.v_texgrad) + rows[q],
-                                  make_float4(wts[q] * gv[0], wts[q] * gv[1], wts[q] * gv[2], 0.f));
+                                  make_float4(g01.x, g01.y, wts[q] * gv2, 0.f));
                     } else {
                         float* dst = g.v_texgrad + 3 * (size_t)rows[q];
                         atomicAdd(dst + 0, wts[q] * gv[0]);
