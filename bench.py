@@ -391,7 +391,7 @@ def main():
         r, tuned, grid = None, None, {}
         for bw in widths:
             cand = make_renderer(bw)
-            t = cand.autotune(scene, tgt_img, tgt_tex)
+            t = cand.autotune(scene, tgt_img, tgt_tex, use_cache=False)  # always time the grid
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             cand.step(scene, tgt_img, tgt_tex)
             e0.record(stream)

@@ -17,6 +17,9 @@ their gradients -> persistent backward -> SH adjoint over views.
 from __future__ import annotations
 
 import ctypes
+import json
+import os
+from collections import Counter
 from dataclasses import dataclass
 from typing import List, Optional, Sequence
 
@@ -151,6 +154,46 @@ LOSS_WEIGHTS = dict(img=1.0, texture=1.0, reg=100.0, normal=0.05)
 # serve (the library's kFixedBwdMask / kFixedBwdSettings).
 FIXED_BWD_MASK = (1 << 2) | (1 << 8) | (1 << 9) | (1 << 10)
 FIXED_BWD_SETTINGS = 1 << 8
+
+# Launch knobs the autotuner chooses, and its cache: in this process, and in
+# the JSON file named by GSTEX_AUTOTUNE_CACHE when that is set.
+TUNED_KNOBS = ("fwd_ppt", "fwd_batch", "bwd_ppt", "bwd_group", "bwd_ctas", "bwd_batch")
+_tune_cache: dict = {}
+
+
+def autotune_key(sizes, num_points, channels, texmode, settings, block_width, device_name) -> str:
+    """Cache key of a tuning: the multiset of view resolutions, the Gaussian
+    count, the texel layout, the settings word, the tile width and the GPU."""
+    mix = ",".join(f"{w}x{h}*{n}" for (h, w), n in sorted(Counter(sizes).items()))
+    return (f"views={mix};N={num_points};C={channels};tex={texmode};settings={settings};bw={block_width};"
+            f"gpu={device_name}")
+
+
+def autotune_cache_load(path: Optional[str] = None) -> dict:
+    """Tunings in the cache file (and remembered in this process)."""
+    path = path if path is not None else os.environ.get("GSTEX_AUTOTUNE_CACHE")
+    if path and os.path.exists(path):
+        with open(path) as f:
+            for k, v in json.load(f).items():
+                _tune_cache.setdefault(k, v)
+    return _tune_cache
+
+
+def autotune_cache_store(key: str, knobs: dict, path: Optional[str] = None) -> None:
+    """Remember a tuning in this process and, if a cache file is named, in it
+    (read, merged and rewritten whole)."""
+    _tune_cache[key] = {k: int(knobs[k]) for k in TUNED_KNOBS}
+    path = path if path is not None else os.environ.get("GSTEX_AUTOTUNE_CACHE")
+    if path:
+        data = {}
+        if os.path.exists(path):
+            with open(path) as f:
+                data = json.load(f)
+        data[key] = _tune_cache[key]
+        tmp = path + ".tmp"
+        with open(tmp, "w") as f:
+            json.dump(data, f, indent=1, sort_keys=True)
+        os.replace(tmp, path)
 
 
 class BatchRenderer:
@@ -473,14 +516,30 @@ class BatchRenderer:
         return loss
 
     # ------------------------------------------------------------------
-    def autotune(self, s: Scene, tgt_img, tgt_tex, reps: int = 2) -> dict:
+    def tune_key(self) -> str:
+        return autotune_key(self.sizes, self.N, self.C, self.texmode, self.settings, self.bw,
+                            torch.cuda.get_device_name(self.dev))
+
+    def autotune(self, s: Scene, tgt_img, tgt_tex, reps: int = 2, use_cache: bool = True) -> dict:
         """Choose pixels-per-thread and Gaussians per batch (64, 128 or one per
         thread) of the forward kernel, and pixels-per-thread, lanes per splat
         walk (32, 16, 8, 4), the resident-CTA variant and Gaussians per batch
         (48, 64, 128 or one per thread) of the backward kernel, by timing each
         candidate on this scene and these cameras (CUDA events).
         The tile width is fixed per renderer (it sets the binning): to tune
-        it, build a renderer per block_width and time whole steps."""
+        it, build a renderer per block_width and time whole steps.
+        With use_cache, a tuning of the same resolution mix, Gaussian count,
+        texel layout, settings, tile width and GPU (this process, or the file
+        named by GSTEX_AUTOTUNE_CACHE) is applied without timing; new tunings
+        are stored there."""
+        key = self.tune_key()
+        if use_cache:
+            hit = autotune_cache_load().get(key)
+            if hit is not None:
+                for k in TUNED_KNOBS:
+                    setattr(self, k, int(hit[k]))
+                self.graph = None
+                return dict(hit, cached=True)
         stream = torch.cuda.current_stream(self.dev)
         self.bin(s)
 
@@ -535,6 +594,7 @@ class BatchRenderer:
         result.update(fwd_ppt=self.fwd_ppt, fwd_batch=self.fwd_batch or "threads", bwd_ppt=self.bwd_ppt,
                       bwd_group=self.bwd_group, bwd_batch=self.bwd_batch or "threads",
                       bwd_ctas=self.bwd_ctas or "default")
+        autotune_cache_store(key, {k: getattr(self, k) for k in TUNED_KNOBS})
         self.graph = None
         return result
 

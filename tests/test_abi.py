@@ -152,3 +152,22 @@ def test_batch_knobs_and_tile_order_rejected_without_gpu():
     assert order(100, dummy, None, None, 4, dummy, dummy, ws, None) == 1
     assert order(100, dummy, dummy, dummy, 4, dummy, dummy, ws - 1, None) == 2
     assert order(0, None, None, None, 4, None, None, 0, None) == 0
+
+
+def test_autotune_cache_key_and_file(tmp_path):
+    """The autotuner's cache key is the multiset of view resolutions (order
+    free), the Gaussian count, texel layout, settings, tile width and GPU;
+    tunings round-trip through the cache file."""
+    from gstex_cuda_gb300 import batch as B
+    k1 = B.autotune_key([(1080, 1920), (512, 512), (1080, 1920)], 500000, 3, 1, 256, 8, "GB300")
+    k2 = B.autotune_key([(512, 512), (1080, 1920), (1080, 1920)], 500000, 3, 1, 256, 8, "GB300")
+    assert k1 == k2 and "1920x1080*2" in k1 and "512x512*1" in k1
+    assert B.autotune_key([(1080, 1920)], 500000, 3, 1, 256, 16, "GB300") != \
+        B.autotune_key([(1080, 1920)], 500000, 3, 1, 256, 8, "GB300")
+    path = str(tmp_path / "tune.json")
+    knobs = dict(fwd_ppt=1, fwd_batch=0, bwd_ppt=1, bwd_group=8, bwd_ctas=10, bwd_batch=0, extra=5)
+    B.autotune_cache_store(k1, knobs, path=path)
+    B._tune_cache.clear()
+    got = B.autotune_cache_load(path)
+    assert got[k1] == {k: knobs[k] for k in B.TUNED_KNOBS}
+    B._tune_cache.clear()

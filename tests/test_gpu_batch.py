@@ -412,6 +412,39 @@ def test_host_input_stepper_matches_device_step(setup):
         torch.testing.assert_close(g1[k], v, atol=1e-5 * (float(v.abs().max()) + 1e-9), rtol=1e-4)
 
 
+def test_autotune_grid_and_cache():
+    """The autotuner times its grid and reports the chosen point; a second
+    renderer of the same resolution mix, Gaussian count and settings takes
+    the cached choice without timing."""
+    from gstex_cuda_gb300 import batch as B, synthetic
+    g = torch.Generator().manual_seed(37)
+    cams = synthetic.sphere_cameras(g, 2, radius=8.0, resolutions=[(96, 64), (80, 80)])
+    spec = synthetic._finish_with_area(g, torch.empty(1200, 3).uniform_(-3, 3, generator=g), 0.01, 0.1, 3, "normal",
+                                       cams, 15_000, "multi", {})
+    t16 = torch.zeros(spec.texture.shape[0], 4, dtype=torch.bfloat16)
+    t16[:, :3] = spec.texture.to(torch.bfloat16)
+    scene = B.Scene(means=spec.means.to(DEV), scales=spec.scales.to(DEV), quats=spec.quats.to(DEV),
+                    opacity=spec.opacity.to(DEV), sh_coeffs=spec.sh_coeffs.to(DEV), sh_degree=3,
+                    uv0=spec.uv0.to(DEV), umap=spec.umap.to(DEV), vmap=spec.vmap.to(DEV),
+                    texture_dims=spec.texture_dims.to(DEV), texture=t16.to(DEV))
+    bcams = [B.Camera(c.viewmat, c.fx, c.fy, c.cx, c.cy, c.width, c.height) for c in cams]
+    gen = torch.Generator().manual_seed(3)
+    P = sum(c.width * c.height for c in cams)
+    tgt_img, tgt_tex = torch.rand(P, 3, generator=gen).to(DEV), torch.rand(P, 3, generator=gen).to(DEV)
+    r = B.BatchRenderer(bcams, spec.num_points, texture_dtype=torch.bfloat16, capacity=1 << 20, block_width=8)
+    B._tune_cache.pop(r.tune_key(), None)
+    res = r.autotune(scene, tgt_img, tgt_tex)
+    assert "cached" not in res and "backward_ppt1_g8_ms" in res and "backward_ppt1_g8_ctas10_ms" in res
+    knobs = {k: getattr(r, k) for k in B.TUNED_KNOBS}
+    r2 = B.BatchRenderer(bcams, spec.num_points, texture_dtype=torch.bfloat16, capacity=1 << 20, block_width=8)
+    res2 = r2.autotune(scene, tgt_img, tgt_tex)
+    assert res2.get("cached") is True and {k: getattr(r2, k) for k in B.TUNED_KNOBS} == knobs
+    loss1 = float(r.step(scene, tgt_img, tgt_tex).item())
+    loss2 = float(r2.step(scene, tgt_img, tgt_tex).item())
+    assert abs(loss1 - loss2) <= 1e-5 * abs(loss1)
+    B._tune_cache.pop(r.tune_key(), None)
+
+
 def test_batch_graph_replay_matches_eager(setup):
     spec, cams, r, scene, _ = setup
     P = r.total_pixels
